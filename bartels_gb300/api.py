@@ -1,0 +1,364 @@
+"""Python mirror of the reference's mesh-level API over the C ABI.
+
+Names, argument order and array conventions follow Bartels' ``sim::`` functions
+(e.g. ``linear_tetmesh_neohookean_dq2(V, E, q, dphidX, volume, params)`` in
+include/linear_tetmesh_neohookean_dq2.h:14-21). Sparse results are
+``scipy.sparse.csr_matrix`` with the reference's assembled pattern (explicit
+zeros kept). Every call runs on the GPU through libbartels_gpu.so; failures
+raise ``BartelsError`` (the reference has no error returns: it asserts or
+calls exit()).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import hashlib
+from collections import OrderedDict
+
+import numpy as np
+import scipy.sparse as sp
+
+from . import _lib
+from ._lib import BartelsError, check, lib
+
+MODELS = {"neohookean": _lib.NEOHOOKEAN, "stvk": _lib.STVK, "corotational": _lib.COROTATIONAL,
+          "neohookean_isochoric": _lib.NEOHOOKEAN_ISOCHORIC}
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _iptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _colmajor(a, dtype):
+    return np.ascontiguousarray(np.asarray(a, dtype=dtype).ravel(order="F"))
+
+
+class Context:
+    """A device, a stream and workspace (bartels_ctx)."""
+
+    _default = None
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        check(lib().bartels_ctx_create(device, C.byref(h)), "bartels_ctx_create")
+        self.handle = h
+        self.device = device
+
+    @classmethod
+    def default(cls) -> "Context":
+        if cls._default is None:
+            cls._default = Context(0)
+        return cls._default
+
+    def synchronize(self):
+        check(lib().bartels_ctx_synchronize(self.handle), "bartels_ctx_synchronize")
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(lib().bartels_ctx_kernel_launches(self.handle))
+
+    def close(self):
+        if self.handle:
+            lib().bartels_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class MeshPlan:
+    """A mesh plan (bartels_mesh_plan): pattern, incidence lists, element data."""
+
+    def __init__(self, V, E, ctx: Context | None = None):
+        self.ctx = ctx or Context.default()
+        self.V = _f64(V)
+        self.E = np.ascontiguousarray(E, dtype=np.int32)
+        if self.V.ndim != 2 or self.V.shape[1] != 3 or self.E.ndim != 2 or self.E.shape[1] != 4:
+            raise BartelsError(_lib.E_INVALID_ARG, "MeshPlan", "V must be (nV,3) and E (nT,4)")
+        self.nV, self.nT = len(self.V), len(self.E)
+        vcm = _colmajor(self.V, np.float64)
+        ecm = _colmajor(self.E, np.int32)
+        h = C.c_void_p()
+        check(lib().bartels_plan_create(self.ctx.handle, self.nV, _dptr(vcm), self.nT, _iptr(ecm), C.byref(h)),
+              "bartels_plan_create")
+        self.handle = h
+        n = C.c_int()
+        nnz = C.c_int64()
+        check(lib().bartels_plan_csr_size(h, C.byref(n), C.byref(nnz)), "bartels_plan_csr_size")
+        self.n, self.nnz = n.value, nnz.value
+        self._pattern = None
+
+    def pattern(self):
+        if self._pattern is None:
+            rp = np.zeros(self.n + 1, np.int32)
+            ci = np.zeros(self.nnz, np.int32)
+            check(lib().bartels_plan_csr_pattern(self.handle, _iptr(rp), _iptr(ci)), "bartels_plan_csr_pattern")
+            self._pattern = (rp, ci)
+        return self._pattern
+
+    def csr(self, values):
+        rp, ci = self.pattern()
+        return sp.csr_matrix((values, ci.copy(), rp.copy()), shape=(self.n, self.n))
+
+    def set_element_data(self, dphidX=None, volume=None, params=None, density=None):
+        keep = []
+
+        def opt(a, cm=False):
+            if a is None:
+                return None
+            arr = _colmajor(a, np.float64) if cm else _f64(np.ravel(a))
+            keep.append(arr)
+            return _dptr(arr)
+
+        check(lib().bartels_plan_set_element_data(self.handle, opt(dphidX, True), opt(volume), opt(params, True),
+                                                  opt(density)), "bartels_plan_set_element_data")
+
+    # --- energy / gradient / Hessian ------------------------------------
+    def _elem(self, dphidX, volume, params):
+        keep = []
+        out = []
+        for a, cm in ((dphidX, True), (volume, False), (params, True)):
+            if a is None:
+                out.append(None)
+            else:
+                arr = _colmajor(a, np.float64) if cm else _f64(np.ravel(a))
+                keep.append(arr)
+                out.append(_dptr(arr))
+        return keep, out
+
+    def q(self, model, q, dphidX=None, volume=None, params=None) -> float:
+        keep, (d, v, p) = self._elem(dphidX, volume, params)
+        qa = _f64(q)
+        e = C.c_double()
+        check(lib().bartels_tetmesh_q(self.ctx.handle, self.handle, MODELS[model], _dptr(qa), d, v, p, C.byref(e)),
+              "bartels_tetmesh_q")
+        return e.value
+
+    def dq(self, model, q, dphidX=None, volume=None, params=None):
+        keep, (d, v, p) = self._elem(dphidX, volume, params)
+        qa = _f64(q)
+        g = np.zeros(3 * self.nV)
+        check(lib().bartels_tetmesh_dq(self.ctx.handle, self.handle, MODELS[model], _dptr(qa), d, v, p, _dptr(g)),
+              "bartels_tetmesh_dq")
+        return g
+
+    def dq2_values(self, model, q, dphidX=None, volume=None, params=None, psd_tol=None, corot_exact=False):
+        keep, (d, v, p) = self._elem(dphidX, volume, params)
+        qa = _f64(q)
+        vals = np.zeros(self.nnz)
+        psd = _lib.PSD_NONE if psd_tol is None else _lib.PSD_SIMPLE_FIX
+        flags = _lib.DQ2_COROT_EXACT if corot_exact else 0
+        check(lib().bartels_tetmesh_dq2(self.ctx.handle, self.handle, MODELS[model], _dptr(qa), d, v, p, psd,
+                                        float(psd_tol or 0.0), flags, _dptr(vals)), "bartels_tetmesh_dq2")
+        return vals
+
+    def dq2(self, model, q, dphidX=None, volume=None, params=None, psd_tol=None, corot_exact=False):
+        return self.csr(self.dq2_values(model, q, dphidX, volume, params, psd_tol, corot_exact))
+
+    def mass_matrix(self, density, volume=None):
+        d = _f64(np.ravel(density))
+        v = None if volume is None else _f64(np.ravel(volume))
+        vals = np.zeros(self.nnz)
+        check(lib().bartels_tetmesh_mass_matrix(self.ctx.handle, self.handle, _dptr(d),
+                                                None if v is None else _dptr(v), _dptr(vals)),
+              "bartels_tetmesh_mass_matrix")
+        return self.csr(vals)
+
+    def const_ext_force(self, volume, traction):
+        v = None if volume is None else _f64(np.ravel(volume))
+        t = _f64(np.ravel(traction))
+        f = np.zeros(3 * self.nV)
+        check(lib().bartels_tetmesh_const_ext_force(self.ctx.handle, self.handle, None if v is None else _dptr(v),
+                                                    _dptr(t), _dptr(f)), "bartels_tetmesh_const_ext_force")
+        return f
+
+    # --- Newton ---------------------------------------------------------------
+    def set_problem(self, q_base=None, x_hat=None, f_ext=None, pinned=None):
+        arrs = [None if a is None else _f64(a) for a in (q_base, x_hat, f_ext)]
+        pin = None if pinned is None else np.ascontiguousarray(pinned, dtype=np.uint8)
+        check(lib().bartels_newton_set_problem(
+            self.handle, *[None if a is None else _dptr(a) for a in arrs],
+            None if pin is None else pin.ctypes.data_as(C.POINTER(C.c_ubyte))), "bartels_newton_set_problem")
+
+    def newton_solve(self, x, params: "_lib.NewtonParams"):
+        xa = _f64(x).copy()
+        rep = _lib.NewtonReport()
+        check(lib().bartels_newton_solve(self.ctx.handle, self.handle, C.byref(params), _dptr(xa), C.byref(rep)),
+              "bartels_newton_solve")
+        return xa, rep
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().bartels_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def newton_params(**kw) -> "_lib.NewtonParams":
+    p = _lib.NewtonParams()
+    lib().bartels_newton_default_params(C.byref(p))
+    for k, v in kw.items():
+        if k == "model" and isinstance(v, str):
+            v = MODELS[v]
+        if k in ("rel_tol", "max_iters", "inner_rel_tol", "max_refinements"):
+            setattr(p.pcg, k, v)
+        else:
+            setattr(p, k, v)
+    return p
+
+
+# ---------------------------------------------------------------- drop-ins --
+_plans: "OrderedDict[str, MeshPlan]" = OrderedDict()
+
+
+def _plan_for(V, E) -> MeshPlan:
+    V = _f64(V)
+    E = np.ascontiguousarray(E, dtype=np.int32)
+    key = hashlib.sha1(V.tobytes() + b"|" + E.tobytes()).hexdigest()
+    p = _plans.get(key)
+    if p is None:
+        p = MeshPlan(V, E)
+        _plans[key] = p
+        while len(_plans) > 4:
+            _plans.popitem(last=False)[1].close()
+    else:
+        _plans.move_to_end(key)
+    return p
+
+
+def linear_tetmesh_dphi_dX(V, E):
+    """src/linear_tetmesh_dphi_dX.cpp:5-18 -> (nT, 12)."""
+    V = np.asarray(V, np.float64)
+    E = np.asarray(E, np.int32)
+    vcm = _colmajor(V, np.float64)
+    ecm = _colmajor(E, np.int32)
+    out = np.zeros(12 * len(E))
+    check(lib().bartels_tetmesh_dphi_dX(Context.default().handle, len(V), _dptr(vcm), len(E), _iptr(ecm),
+                                        _dptr(out)), "bartels_tetmesh_dphi_dX")
+    return out.reshape(12, len(E)).T.copy()
+
+
+def volume(V, E):
+    V = np.asarray(V, np.float64)
+    E = np.asarray(E, np.int32)
+    vcm = _colmajor(V, np.float64)
+    ecm = _colmajor(E, np.int32)
+    out = np.zeros(len(E))
+    check(lib().bartels_tetmesh_volume(Context.default().handle, len(V), _dptr(vcm), len(E), _iptr(ecm),
+                                       _dptr(out)), "bartels_tetmesh_volume")
+    return out
+
+
+def _make(model):
+    def q_fn(V, E, q, dphidX, volume, params):
+        return _plan_for(V, E).q(model, q, dphidX, volume, params)
+
+    def dq_fn(V, E, q, dphidX, volume, params):
+        return _plan_for(V, E).dq(model, q, dphidX, volume, params)
+
+    def dq2_fn(V, E, q, dphidX, volume, params, psd_tol=None, corot_exact=False):
+        return _plan_for(V, E).dq2(model, q, dphidX, volume, params, psd_tol, corot_exact)
+
+    q_fn.__name__ = f"linear_tetmesh_{model}_q"
+    dq_fn.__name__ = f"linear_tetmesh_{model}_dq"
+    dq2_fn.__name__ = f"linear_tetmesh_{model}_dq2"
+    return q_fn, dq_fn, dq2_fn
+
+
+linear_tetmesh_neohookean_q, linear_tetmesh_neohookean_dq, linear_tetmesh_neohookean_dq2 = _make("neohookean")
+linear_tetmesh_stvk_q, linear_tetmesh_stvk_dq, linear_tetmesh_stvk_dq2 = _make("stvk")
+linear_tetmesh_corotational_q, linear_tetmesh_corotational_dq, linear_tetmesh_corotational_dq2 = _make(
+    "corotational")
+
+
+def linear_tetmesh_mass_matrix(V, E, density, volume):
+    """src/linear_tetmesh_mass_matrix.cpp:7-24."""
+    return _plan_for(V, E).mass_matrix(density, volume)
+
+
+def linear_tetmesh_const_ext_force(V, E, volume, traction):
+    """src/linear_tetmesh_const_ext_force.cpp:5-18."""
+    return _plan_for(V, E).const_ext_force(volume, traction)
+
+
+def fixed_point_constraint_matrix(V, fixed_indices):
+    """src/fixed_point_constraint_matrix.cpp:7-38 (fixed_indices sorted ascending)."""
+    V = np.asarray(V)
+    nV, dim = V.shape
+    f = np.ascontiguousarray(fixed_indices, dtype=np.int32)
+    rows = C.c_int()
+    check(lib().bartels_fixed_point_constraint_matrix(nV, dim, _iptr(f), len(f), C.byref(rows), None, None, None),
+          "bartels_fixed_point_constraint_matrix")
+    rp = np.zeros(rows.value + 1, np.int32)
+    ci = np.zeros(rows.value, np.int32)
+    va = np.zeros(rows.value)
+    check(lib().bartels_fixed_point_constraint_matrix(nV, dim, _iptr(f), len(f), C.byref(rows), _iptr(rp), _iptr(ci),
+                                                      _dptr(va)), "bartels_fixed_point_constraint_matrix")
+    return sp.csr_matrix((va, ci, rp), shape=(rows.value, nV * dim))
+
+
+def find_min_vertices(V, dim, tol=1e-3):
+    """src/find_min_vertices.cpp:5-21."""
+    vcm = _colmajor(np.asarray(V, np.float64), np.float64)
+    out = np.zeros(len(V), np.int32)
+    cnt = C.c_int()
+    check(lib().bartels_find_min_vertices(len(V), _dptr(vcm), dim, tol, _iptr(out), C.byref(cnt)),
+          "bartels_find_min_vertices")
+    return out[:cnt.value].copy()
+
+
+def search_direction_newton_sparse(g, H, rel_tol=1e-8, max_iters=20000):
+    """src/search_direction_newton_sparse.cpp:5-26: d = -H^{-1} g (PCG instead of SparseLU).
+    Returns (d, ok, report); ok mirrors the reference's bool."""
+    H = sp.csr_matrix(H)
+    H.sort_indices()
+    g = _f64(g)
+    rp = np.ascontiguousarray(H.indptr, np.int32)
+    ci = np.ascontiguousarray(H.indices, np.int32)
+    va = _f64(H.data)
+    d = np.zeros_like(g)
+    prm = _lib.PcgParams()
+    lib().bartels_pcg_default_params(C.byref(prm))
+    prm.rel_tol = rel_tol
+    prm.max_iters = max_iters
+    rep = _lib.PcgReport()
+    s = lib().bartels_search_direction_newton_sparse(Context.default().handle, len(g), _iptr(rp), _iptr(ci),
+                                                     _dptr(va), _dptr(g), _dptr(d), C.byref(prm), C.byref(rep))
+    if s not in (_lib.OK, _lib.E_NOT_CONVERGED):
+        check(s, "bartels_search_direction_newton_sparse")
+    return d, s == _lib.OK, rep
+
+
+def linesearch_backtracking_bisection(x, d, f, g, max_iterations, alpha, c, p):
+    """src/linesearch_backtracking_bisection.cpp:5-31 for a Python objective f(x).
+    Updates x in place; returns CONVERGED or MAX_ITERATIONS_REACHED."""
+    if x.dtype != np.float64 or not x.flags.c_contiguous:
+        raise BartelsError(_lib.E_INVALID_ARG, "linesearch", "x must be a contiguous float64 array")
+    dd = _f64(d)
+    gg = _f64(g)
+
+    @_lib.OBJECTIVE_FN
+    def cb(ptr, n, user):
+        return float(f(np.ctypeslib.as_array(ptr, shape=(n,)).copy()))
+
+    status = C.c_int()
+    a = C.c_double()
+    check(lib().bartels_linesearch_backtracking_bisection(len(x), _dptr(x), _dptr(dd), cb, None, _dptr(gg),
+                                                          max_iterations, alpha, c, p, C.byref(status), C.byref(a)),
+          "bartels_linesearch_backtracking_bisection")
+    return status.value

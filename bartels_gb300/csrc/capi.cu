@@ -1,0 +1,545 @@
+// extern "C" entry points (include/bartels_gpu.h).
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "devmath.cuh"
+#include "internal.cuh"
+
+namespace bartels {
+int plan_set_element_data(bartels_mesh_plan plan, const double *dphidX, const double *vol, const double *params,
+                          const double *density);
+void plan_free(bartels_mesh_plan plan);
+int launch_prep_u(bartels_ctx ctx, bartels_mesh_plan plan, const double *x, const double *q_base, double scale,
+                  bool displacement, float4 *u);
+int launch_hess(bartels_ctx ctx, bartels_mesh_plan plan, int model, int psd_mode, const float4 *u, int add_identity,
+                float cK, float cM, float tol, int flags, float *values);
+int launch_mass64(bartels_ctx ctx, bartels_mesh_plan plan, const double *density, const double *vol,
+                  double *values);
+int newton_iterate(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params &p, double *x,
+                   double g0_norm, int *done, bartels_newton_report *rep);
+int newton_solve(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params &p, double *x,
+                 bartels_newton_report *rep);
+int csr_search_direction(bartels_ctx ctx, int n, const int *rp, const int *ci, const double *vals, const double *g,
+                         double *d, const bartels_pcg_params &prm, bartels_pcg_report *rep);
+int advance_implicit_euler(bartels_ctx ctx, bartels_mesh_plan plan, double dt, const double *v);
+int plan_spmv(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const float *x, float *y);
+}  // namespace bartels
+
+using namespace bartels;
+
+namespace {
+
+bool valid_model(int m) { return m >= 0 && m <= 3; }
+
+int check_ctx(bartels_ctx ctx) {
+  if (!ctx) return fail(BARTELS_E_INVALID_ARG, "null context");
+  BT_CUDA(cudaSetDevice(ctx->device));
+  return BARTELS_OK;
+}
+
+int check_plan(bartels_ctx ctx, bartels_mesh_plan plan) {
+  BT_CHECK(check_ctx(ctx));
+  if (!plan) return fail(BARTELS_E_INVALID_ARG, "null plan");
+  if (plan->ctx != ctx) return fail(BARTELS_E_INVALID_ARG, "plan belongs to another context");
+  return BARTELS_OK;
+}
+
+// upload a 3nV host vector into a context staging buffer
+int stage_vec(bartels_ctx ctx, DevBuf &buf, const double *h, size_t n, double **d) {
+  BT_CHECK(buf.ensure(sizeof(double) * std::max<size_t>(n, 1)));
+  if (n) BT_CUDA(cudaMemcpyAsync(buf.p, h, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+  *d = buf.as<double>();
+  return BARTELS_OK;
+}
+
+double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *bartels_status_string(int s) {
+  switch (s) {
+    case BARTELS_OK: return "ok";
+    case BARTELS_E_INVALID_ARG: return "invalid argument";
+    case BARTELS_E_NONFINITE: return "non-finite value";
+    case BARTELS_E_NOT_CONVERGED: return "not converged";
+    case BARTELS_E_DEVICE: return "CUDA device error";
+    case BARTELS_E_TIMEOUT: return "timeout";
+    case BARTELS_E_UNSUPPORTED: return "unsupported input";
+    case BARTELS_E_NO_DEVICE: return "no CUDA device";
+    default: return "unknown status";
+  }
+}
+
+const char *bartels_last_error(void) { return last_error_cstr(); }
+
+int bartels_ctx_create(int device, bartels_ctx *out) {
+  if (!out) return fail(BARTELS_E_INVALID_ARG, "null output");
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0) return fail(BARTELS_E_NO_DEVICE, "no CUDA device available");
+  if (device < 0 || device >= count) return fail(BARTELS_E_INVALID_ARG, "device index out of range");
+  BT_CUDA(cudaSetDevice(device));
+  auto ctx = new bartels_ctx_s;
+  ctx->device = device;
+  BT_CUDA(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
+  BT_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+  BT_CUDA(cudaMallocHost(&ctx->host_scalars, 64 * sizeof(double)));
+  *out = ctx;
+  return BARTELS_OK;
+}
+
+int bartels_ctx_destroy(bartels_ctx ctx) {
+  if (!ctx) return BARTELS_OK;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  ctx->partials.release();
+  ctx->scalars.release();
+  ctx->stage_a.release();
+  ctx->stage_b.release();
+  ctx->stage_c.release();
+  ctx->stage_d.release();
+  ctx->stage_e.release();
+  if (ctx->host_scalars) cudaFreeHost(ctx->host_scalars);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return BARTELS_OK;
+}
+
+int bartels_ctx_synchronize(bartels_ctx ctx) {
+  BT_CHECK(check_ctx(ctx));
+  BT_CUDA(cudaStreamSynchronize(ctx->stream));
+  return BARTELS_OK;
+}
+
+void *bartels_ctx_stream(bartels_ctx ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+int64_t bartels_ctx_kernel_launches(bartels_ctx ctx) { return ctx ? ctx->launches : 0; }
+
+int bartels_tetmesh_dphi_dX(bartels_ctx ctx, int nV, const double *V, int nT, const int *E, double *dphidX) {
+  BT_CHECK(check_ctx(ctx));
+  if (nV < 0 || nT < 0 || (!V && nV) || (!E && nT) || (!dphidX && nT))
+    return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  if (nT == 0) return BARTELS_OK;
+  std::vector<double> X(3 * (size_t)nV);
+  for (int v = 0; v < nV; ++v)
+    for (int d = 0; d < 3; ++d) X[3 * (size_t)v + d] = V[v + (size_t)nV * d];
+  std::vector<int4> E4(nT);
+  for (int t = 0; t < nT; ++t) {
+    E4[t] = make_int4(E[t], E[t + (size_t)nT], E[t + 2 * (size_t)nT], E[t + 3 * (size_t)nT]);
+    const int id[4] = {E4[t].x, E4[t].y, E4[t].z, E4[t].w};
+    for (int a = 0; a < 4; ++a)
+      if (id[a] < 0 || id[a] >= nV) return fail(BARTELS_E_INVALID_ARG, "element index out of range");
+  }
+  BT_CHECK(ctx->stage_a.ensure(sizeof(double) * X.size()));
+  BT_CHECK(ctx->stage_b.ensure(sizeof(int4) * E4.size()));
+  BT_CHECK(ctx->stage_c.ensure(sizeof(double) * 12 * (size_t)nT));
+  BT_CUDA(cudaMemcpyAsync(ctx->stage_a.p, X.data(), sizeof(double) * X.size(), cudaMemcpyHostToDevice, ctx->stream));
+  BT_CUDA(cudaMemcpyAsync(ctx->stage_b.p, E4.data(), sizeof(int4) * E4.size(), cudaMemcpyHostToDevice, ctx->stream));
+  BT_CHECK(launch_dphi_vol(ctx, nV, ctx->stage_a.as<double>(), nT, ctx->stage_b.as<int4>(), ctx->stage_c.as<double>(),
+                           nullptr, nullptr));
+  BT_CUDA(cudaMemcpyAsync(dphidX, ctx->stage_c.p, sizeof(double) * 12 * (size_t)nT, cudaMemcpyDeviceToHost,
+                          ctx->stream));
+  BT_CUDA(cudaStreamSynchronize(ctx->stream));
+  return BARTELS_OK;
+}
+
+int bartels_tetmesh_volume(bartels_ctx ctx, int nV, const double *V, int nT, const int *E, double *vol) {
+  BT_CHECK(check_ctx(ctx));
+  if (nV < 0 || nT < 0 || (!V && nV) || (!E && nT) || (!vol && nT)) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  if (nT == 0) return BARTELS_OK;
+  std::vector<double> X(3 * (size_t)nV);
+  for (int v = 0; v < nV; ++v)
+    for (int d = 0; d < 3; ++d) X[3 * (size_t)v + d] = V[v + (size_t)nV * d];
+  std::vector<int4> E4(nT);
+  for (int t = 0; t < nT; ++t) {
+    E4[t] = make_int4(E[t], E[t + (size_t)nT], E[t + 2 * (size_t)nT], E[t + 3 * (size_t)nT]);
+    const int id[4] = {E4[t].x, E4[t].y, E4[t].z, E4[t].w};
+    for (int a = 0; a < 4; ++a)
+      if (id[a] < 0 || id[a] >= nV) return fail(BARTELS_E_INVALID_ARG, "element index out of range");
+  }
+  BT_CHECK(ctx->stage_a.ensure(sizeof(double) * X.size()));
+  BT_CHECK(ctx->stage_b.ensure(sizeof(int4) * E4.size()));
+  BT_CHECK(ctx->stage_c.ensure(sizeof(double) * (size_t)nT));
+  BT_CUDA(cudaMemcpyAsync(ctx->stage_a.p, X.data(), sizeof(double) * X.size(), cudaMemcpyHostToDevice, ctx->stream));
+  BT_CUDA(cudaMemcpyAsync(ctx->stage_b.p, E4.data(), sizeof(int4) * E4.size(), cudaMemcpyHostToDevice, ctx->stream));
+  BT_CHECK(launch_dphi_vol(ctx, nV, ctx->stage_a.as<double>(), nT, ctx->stage_b.as<int4>(), nullptr, nullptr,
+                           ctx->stage_c.as<double>()));
+  BT_CUDA(cudaMemcpyAsync(vol, ctx->stage_c.p, sizeof(double) * (size_t)nT, cudaMemcpyDeviceToHost, ctx->stream));
+  BT_CUDA(cudaStreamSynchronize(ctx->stream));
+  return BARTELS_OK;
+}
+
+int bartels_plan_create(bartels_ctx ctx, int nV, const double *V, int nT, const int *E, bartels_mesh_plan *out) {
+  BT_CHECK(check_ctx(ctx));
+  if (!out || nV <= 0 || nT < 0 || !V || (!E && nT)) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  auto plan = new bartels_mesh_plan_s;
+  plan->ctx = ctx;
+  plan->nV = nV;
+  plan->nT = nT;
+  int s = plan_build(plan, V, E);
+  if (s != BARTELS_OK) {
+    plan_free(plan);
+    delete plan;
+    return s;
+  }
+  *out = plan;
+  return BARTELS_OK;
+}
+
+int bartels_plan_destroy(bartels_mesh_plan plan) {
+  if (!plan) return BARTELS_OK;
+  cudaSetDevice(plan->ctx->device);
+  cudaStreamSynchronize(plan->ctx->stream);
+  plan_free(plan);
+  delete plan;
+  return BARTELS_OK;
+}
+
+int bartels_plan_set_element_data(bartels_mesh_plan plan, const double *dphidX, const double *vol,
+                                  const double *params, const double *density) {
+  if (!plan) return fail(BARTELS_E_INVALID_ARG, "null plan");
+  BT_CHECK(check_ctx(plan->ctx));
+  return plan_set_element_data(plan, dphidX, vol, params, density);
+}
+
+int bartels_plan_csr_size(bartels_mesh_plan plan, int *n, int64_t *nnz) {
+  if (!plan) return fail(BARTELS_E_INVALID_ARG, "null plan");
+  if (n) *n = 3 * plan->nV;
+  if (nnz) *nnz = 9 * plan->nnzb;
+  return BARTELS_OK;
+}
+
+int bartels_plan_csr_pattern(bartels_mesh_plan plan, int *row_ptr, int *col_idx) {
+  if (!plan) return fail(BARTELS_E_INVALID_ARG, "null plan");
+  BT_CHECK(check_ctx(plan->ctx));
+  BT_CHECK(plan_build_csr_pattern(plan));
+  bartels_ctx ctx = plan->ctx;
+  if (row_ptr)
+    BT_CUDA(cudaMemcpyAsync(row_ptr, plan->csr_rp, sizeof(int) * (3 * (size_t)plan->nV + 1), cudaMemcpyDeviceToHost,
+                            ctx->stream));
+  if (col_idx)
+    BT_CUDA(cudaMemcpyAsync(col_idx, plan->csr_col, sizeof(int) * 9 * (size_t)plan->nnzb, cudaMemcpyDeviceToHost,
+                            ctx->stream));
+  BT_CUDA(cudaStreamSynchronize(ctx->stream));
+  return BARTELS_OK;
+}
+
+int bartels_tetmesh_q(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q, const double *dphidX,
+                      const double *vol, const double *params, double *energy_out) {
+  BT_CHECK(check_plan(ctx, plan));
+  if (!valid_model(model) || !q || !energy_out) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  BT_CHECK(plan_set_element_data(plan, dphidX, vol, params, nullptr));
+  double *dq;
+  BT_CHECK(stage_vec(ctx, ctx->stage_e, q, 3 * (size_t)plan->nV, &dq));
+  BT_CHECK(ctx->scalars.ensure(64 * sizeof(double)));
+  ObjectiveDev obj;
+  BT_CHECK(energy(ctx, plan, model, obj, dq, ctx->scalars.as<double>()));
+  BT_CUDA(cudaMemcpyAsync(ctx->host_scalars, ctx->scalars.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  BT_CUDA(cudaStreamSynchronize(ctx->stream));
+  *energy_out = ctx->host_scalars[0];
+  if (!std::isfinite(*energy_out)) return fail(BARTELS_E_NONFINITE, "energy is not finite (J <= 0 for Neo-Hookean?)");
+  return BARTELS_OK;
+}
+
+int bartels_tetmesh_dq(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q, const double *dphidX,
+                       const double *vol, const double *params, double *g) {
+  BT_CHECK(check_plan(ctx, plan));
+  if (!valid_model(model) || !q || !g) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  BT_CHECK(plan_set_element_data(plan, dphidX, vol, params, nullptr));
+  const size_t n = 3 * (size_t)plan->nV;
+  double *dq;
+  BT_CHECK(stage_vec(ctx, ctx->stage_e, q, n, &dq));
+  BT_CHECK(plan->w_vec.ensure(sizeof(double) * (3 * n + 16)));
+  ObjectiveDev obj;
+  BT_CHECK(gradient(ctx, plan, model, obj, dq, plan->w_vec.as<double>()));
+  BT_CUDA(cudaMemcpyAsync(g, plan->w_vec.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  BT_CUDA(cudaStreamSynchronize(ctx->stream));
+  for (size_t i = 0; i < n; ++i)
+    if (!std::isfinite(g[i])) return fail(BARTELS_E_NONFINITE, "gradient is not finite");
+  return BARTELS_OK;
+}
+
+int bartels_tetmesh_dq2(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q, const double *dphidX,
+                        const double *vol, const double *params, int psd_mode, double psd_tol, int flags,
+                        double *csr_values) {
+  BT_CHECK(check_plan(ctx, plan));
+  if (!valid_model(model) || !q || !csr_values || (psd_mode != BARTELS_PSD_NONE && psd_mode != BARTELS_PSD_SIMPLE_FIX))
+    return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  BT_CHECK(plan_set_element_data(plan, dphidX, vol, params, nullptr));
+  const size_t n = 3 * (size_t)plan->nV;
+  const int64_t nnz = 9 * plan->nnzb;
+  double *dq;
+  BT_CHECK(stage_vec(ctx, ctx->stage_e, q, n, &dq));
+  BT_CHECK(plan->w_u.ensure(sizeof(float4) * (size_t)plan->nV));
+  BT_CHECK(plan->w_values.ensure(sizeof(float) * nnz));
+  BT_CHECK(ctx->stage_d.ensure(sizeof(double) * nnz));
+  float4 *u = plan->w_u.as<float4>();
+  BT_CHECK(launch_prep_u(ctx, plan, dq, nullptr, 1.0, plan->dphi_matches_rest, u));
+  BT_CHECK(launch_hess(ctx, plan, model, psd_mode, u, plan->dphi_matches_rest ? 1 : 0, 1.f, 0.f, (float)psd_tol, flags,
+                       plan->w_values.as<float>()));
+  BT_CHECK(values_to_double(ctx, plan->w_values.as<float>(), ctx->stage_d.as<double>(), nnz));
+  BT_CUDA(cudaMemcpyAsync(csr_values, ctx->stage_d.p, sizeof(double) * nnz, cudaMemcpyDeviceToHost, ctx->stream));
+  BT_CUDA(cudaStreamSynchronize(ctx->stream));
+  return BARTELS_OK;
+}
+
+#define BT_NAMED(name, M)                                                                                         \
+  int bartels_tetmesh_##name##_q(bartels_ctx c, bartels_mesh_plan p, const double *q, const double *d,          \
+                                 const double *v, const double *pr, double *e) {                                 \
+    return bartels_tetmesh_q(c, p, M, q, d, v, pr, e);                                                          \
+  }                                                                                                             \
+  int bartels_tetmesh_##name##_dq(bartels_ctx c, bartels_mesh_plan p, const double *q, const double *d,         \
+                                  const double *v, const double *pr, double *g) {                               \
+    return bartels_tetmesh_dq(c, p, M, q, d, v, pr, g);                                                         \
+  }                                                                                                             \
+  int bartels_tetmesh_##name##_dq2(bartels_ctx c, bartels_mesh_plan p, const double *q, const double *d,        \
+                                   const double *v, const double *pr, int psd, double tol, double *vals) {      \
+    return bartels_tetmesh_dq2(c, p, M, q, d, v, pr, psd, tol, 0, vals);                                        \
+  }
+BT_NAMED(neohookean, BARTELS_NEOHOOKEAN)
+BT_NAMED(stvk, BARTELS_STVK)
+BT_NAMED(corotational, BARTELS_COROTATIONAL)
+#undef BT_NAMED
+
+int bartels_tetmesh_mass_matrix(bartels_ctx ctx, bartels_mesh_plan plan, const double *density, const double *vol,
+                                double *csr_values) {
+  BT_CHECK(check_plan(ctx, plan));
+  if (!csr_values) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  const size_t nT = (size_t)plan->nT;
+  const int64_t nnz = 9 * plan->nnzb;
+  BT_CHECK(plan_set_element_data(plan, nullptr, vol, nullptr, density));
+  BT_CHECK(ctx->stage_d.ensure(sizeof(double) * nnz));
+  BT_CHECK(launch_mass64(ctx, plan, plan->density, plan->vol, ctx->stage_d.as<double>()));
+  (void)nT;
+  BT_CUDA(cudaMemcpyAsync(csr_values, ctx->stage_d.p, sizeof(double) * nnz, cudaMemcpyDeviceToHost, ctx->stream));
+  BT_CUDA(cudaStreamSynchronize(ctx->stream));
+  return BARTELS_OK;
+}
+
+int bartels_tetmesh_const_ext_force(bartels_ctx ctx, bartels_mesh_plan plan, const double *vol,
+                                    const double traction[3], double *f) {
+  BT_CHECK(check_plan(ctx, plan));
+  if (!traction || !f) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  BT_CHECK(plan_set_element_data(plan, nullptr, vol, nullptr, nullptr));
+  const size_t n = 3 * (size_t)plan->nV;
+  BT_CHECK(ctx->stage_d.ensure(sizeof(double) * n));
+  BT_CHECK(ext_force(ctx, plan, traction, ctx->stage_d.as<double>()));
+  BT_CUDA(cudaMemcpyAsync(f, ctx->stage_d.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  BT_CUDA(cudaStreamSynchronize(ctx->stream));
+  return BARTELS_OK;
+}
+
+int bartels_fixed_point_constraint_matrix(int nV, int dim, const int *fixed, int nfix, int *rows, int *row_ptr,
+                                          int *col_idx, double *values) {
+  if (nV < 0 || dim <= 0 || nfix < 0 || (nfix && !fixed)) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  for (int i = 1; i < nfix; ++i)
+    if (fixed[i] <= fixed[i - 1]) return fail(BARTELS_E_INVALID_ARG, "fixed indices must be sorted ascending");
+  for (int i = 0; i < nfix; ++i)
+    if (fixed[i] < 0 || fixed[i] >= nV) return fail(BARTELS_E_INVALID_ARG, "fixed index out of range");
+  const int nr = dim * (nV - nfix);
+  if (rows) *rows = nr;
+  if (!row_ptr) return BARTELS_OK;
+  // src/fixed_point_constraint_matrix.cpp:20-34: single merge pass over vertices
+  int jj = 0, r = 0;
+  row_ptr[0] = 0;
+  for (int ii = 0; ii < nV * dim; ii += dim) {
+    if (jj < nfix && fixed[jj] == ii / dim) {
+      jj += 1;
+    } else {
+      for (int kk = 0; kk < dim; ++kk) {
+        if (col_idx) col_idx[r] = ii + kk;
+        if (values) values[r] = 1.0;
+        r++;
+        row_ptr[r] = r;
+      }
+    }
+  }
+  return BARTELS_OK;
+}
+
+int bartels_find_min_vertices(int nV, const double *V, int dim, double tol, int *indices, int *count) {
+  if (nV <= 0 || !V || dim < 0 || dim > 2 || !count) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  double mn = V[(size_t)nV * dim];
+  for (int v = 0; v < nV; ++v) mn = V[v + (size_t)nV * dim] < mn ? V[v + (size_t)nV * dim] : mn;
+  int k = 0;
+  for (int v = 0; v < nV; ++v)
+    if (std::fabs(V[v + (size_t)nV * dim] - mn) <= tol) {
+      if (indices) indices[k] = v;
+      k++;
+    }
+  *count = k;
+  return BARTELS_OK;
+}
+
+void bartels_pcg_default_params(bartels_pcg_params *p) {
+  if (!p) return;
+  p->rel_tol = 1e-8;
+  p->max_iters = 20000;
+  p->inner_rel_tol = 1e-4;
+  p->max_refinements = 8;
+}
+
+int bartels_search_direction_newton_sparse(bartels_ctx ctx, int n, const int *row_ptr, const int *col_idx,
+                                           const double *values, const double *g, double *d,
+                                           const bartels_pcg_params *params, bartels_pcg_report *report) {
+  BT_CHECK(check_ctx(ctx));
+  if (n < 0 || (n && (!row_ptr || !col_idx || !values || !g || !d))) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  bartels_pcg_params p;
+  bartels_pcg_default_params(&p);
+  if (params) p = *params;
+  bartels_pcg_report rep;
+  std::memset(&rep, 0, sizeof(rep));
+  if (n == 0) {
+    if (report) *report = rep;
+    return BARTELS_OK;
+  }
+  int s = csr_search_direction(ctx, n, row_ptr, col_idx, values, g, d, p, &rep);
+  if (report) *report = rep;
+  return s;
+}
+
+int bartels_linesearch_backtracking_bisection(int n, double *x, const double *d, bartels_objective_fn f, void *user,
+                                              const double *g, int max_iterations, double alpha, double c, double p,
+                                              int *status, double *alpha_out) {
+  if (n < 0 || !x || !d || !f || !g || max_iterations < 0) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  // src/linesearch_backtracking_bisection.cpp:17-30, with f(x) evaluated once
+  std::vector<double> xt(n);
+  double gd = 0.0;
+  for (int i = 0; i < n; ++i) gd += g[i] * d[i];
+  const double fx = f(x, n, user);
+  int it = 0;
+  for (;;) {
+    for (int i = 0; i < n; ++i) xt[i] = x[i] + alpha * d[i];
+    if (!(f(xt.data(), n, user) > fx + c * gd && it < max_iterations)) break;
+    alpha *= p;
+    it++;
+  }
+  for (int i = 0; i < n; ++i) x[i] += alpha * d[i];
+  if (status) *status = (it == max_iterations) ? BARTELS_MAX_ITERATIONS_REACHED : BARTELS_CONVERGED;
+  if (alpha_out) *alpha_out = alpha;
+  return BARTELS_OK;
+}
+
+void bartels_newton_default_params(bartels_newton_params *p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->model = BARTELS_NEOHOOKEAN;
+  p->psd_mode = BARTELS_PSD_NONE;
+  p->psd_tol = 1e-6;
+  p->dq2_flags = 0;
+  p->mass_coeff = 0.0;
+  p->scale = 1.0;
+  p->force_scale = 1.0;
+  p->gradient_tol = 1e-3;  // include/optimization_gradient_based.h:51-56
+  p->relative = 0;
+  p->max_iterations = 100;
+  p->max_iterations_ls = 100;
+  p->ls_alpha = 1.0;
+  p->ls_c = 1e-8;
+  p->ls_p = 0.5;
+  bartels_pcg_default_params(&p->pcg);
+}
+
+int bartels_newton_set_problem(bartels_mesh_plan plan, const double *q_base, const double *x_hat, const double *f_ext,
+                               const unsigned char *pinned) {
+  if (!plan) return fail(BARTELS_E_INVALID_ARG, "null plan");
+  bartels_ctx ctx = plan->ctx;
+  BT_CHECK(check_ctx(ctx));
+  const size_t n = 3 * (size_t)plan->nV;
+  auto put = [&](double **dst, const double *src) -> int {
+    if (!src) {
+      if (*dst) cudaFree(*dst);
+      *dst = nullptr;
+      return BARTELS_OK;
+    }
+    if (!*dst) BT_CUDA(cudaMalloc(dst, sizeof(double) * n));
+    BT_CUDA(cudaMemcpyAsync(*dst, src, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    return BARTELS_OK;
+  };
+  BT_CHECK(put(&plan->q_base, q_base));
+  BT_CHECK(put(&plan->x_hat, x_hat));
+  BT_CHECK(put(&plan->f_ext, f_ext));
+  if (pinned) {
+    if (!plan->pinned) BT_CUDA(cudaMalloc(&plan->pinned, (size_t)plan->nV));
+    BT_CUDA(cudaMemcpyAsync(plan->pinned, pinned, (size_t)plan->nV, cudaMemcpyHostToDevice, ctx->stream));
+  } else if (plan->pinned) {
+    cudaFree(plan->pinned);
+    plan->pinned = nullptr;
+  }
+  BT_CUDA(cudaStreamSynchronize(ctx->stream));
+  return BARTELS_OK;
+}
+
+int bartels_newton_solve_d(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params *params, double *x_d,
+                           bartels_newton_report *report) {
+  BT_CHECK(check_plan(ctx, plan));
+  if (!params || !x_d || !valid_model(params->model)) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  bartels_newton_report rep;
+  std::memset(&rep, 0, sizeof(rep));
+  int s = newton_solve(ctx, plan, *params, x_d, &rep);
+  if (report) *report = rep;
+  return s;
+}
+
+int bartels_newton_solve(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params *params, double *x,
+                         bartels_newton_report *report) {
+  BT_CHECK(check_plan(ctx, plan));
+  if (!params || !x || !valid_model(params->model)) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  const double t0 = now_s();
+  const size_t n = 3 * (size_t)plan->nV;
+  double *dx;
+  BT_CHECK(stage_vec(ctx, ctx->stage_e, x, n, &dx));
+  bartels_newton_report rep;
+  std::memset(&rep, 0, sizeof(rep));
+  int s = newton_solve(ctx, plan, *params, dx, &rep);
+  BT_CUDA(cudaMemcpyAsync(x, dx, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  BT_CUDA(cudaStreamSynchronize(ctx->stream));
+  rep.seconds = now_s() - t0;
+  if (report) *report = rep;
+  return s;
+}
+
+int bartels_newton_iterate_d(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params *params,
+                             double *x_d, double g0_norm, int *done, bartels_newton_report *report) {
+  BT_CHECK(check_plan(ctx, plan));
+  if (!params || !x_d || !done || !report || !valid_model(params->model))
+    return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  return newton_iterate(ctx, plan, *params, x_d, g0_norm, done, report);
+}
+
+int bartels_plan_hessian_d(bartels_ctx ctx, bartels_mesh_plan plan, int model, int psd_mode, double psd_tol,
+                           int flags, double coeff_K, double coeff_M, const double *q_d, float *values_d) {
+  BT_CHECK(check_plan(ctx, plan));
+  if (!valid_model(model) || !q_d || (psd_mode != BARTELS_PSD_NONE && psd_mode != BARTELS_PSD_SIMPLE_FIX))
+    return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  BT_CHECK(plan->w_u.ensure(sizeof(float4) * (size_t)plan->nV));
+  BT_CHECK(plan->w_values.ensure(sizeof(float) * 9 * (size_t)plan->nnzb));
+  float4 *u = plan->w_u.as<float4>();
+  BT_CHECK(launch_prep_u(ctx, plan, q_d, nullptr, 1.0, plan->dphi_matches_rest, u));
+  return launch_hess(ctx, plan, model, psd_mode, u, plan->dphi_matches_rest ? 1 : 0, (float)coeff_K, (float)coeff_M,
+                     (float)psd_tol, flags, values_d ? values_d : plan->w_values.as<float>());
+}
+
+int bartels_plan_spmv_d(bartels_ctx ctx, bartels_mesh_plan plan, const float *values_d, const float *x_d, float *y_d) {
+  BT_CHECK(check_plan(ctx, plan));
+  if (!x_d || !y_d) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  if (!values_d) {
+    if (plan->w_values.bytes < sizeof(float) * 9 * (size_t)plan->nnzb)
+      return fail(BARTELS_E_INVALID_ARG, "the plan has no assembled Hessian yet");
+    values_d = plan->w_values.as<float>();
+  }
+  return plan_spmv(ctx, plan, values_d, x_d, y_d);
+}
+
+int bartels_newton_advance_implicit_euler_d(bartels_ctx ctx, bartels_mesh_plan plan, double dt, const double *v_d) {
+  BT_CHECK(check_plan(ctx, plan));
+  if (!v_d) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  return advance_implicit_euler(ctx, plan, dt, v_d);
+}
+
+}  // extern "C"

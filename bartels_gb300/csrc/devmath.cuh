@@ -1,0 +1,664 @@
+// Element math of the tet-mesh hot path, written once for device and host.
+//
+// Compiled by nvcc into the CUDA kernels, and by g++ into a CPU unit-test
+// harness that checks these laws against the FP64 oracle. Nothing here
+// allocates or branches on the host; all arrays are small and fixed-size.
+//
+// Conventions: 3x3 matrices are column-major (m[i + 3 j]); F indexes the
+// deformation gradient with rows = spatial components, columns = material
+// directions, as in the reference's column-major flatten. phi_a is the
+// gradient of shape function a (row a of the reference's 4x3 dphidX).
+#pragma once
+
+#ifdef __CUDACC__
+#define BT_HD __host__ __device__ __forceinline__
+#define BT_HD_NOINLINE __host__ __device__ __noinline__
+#else
+#define BT_HD inline
+#define BT_HD_NOINLINE
+#include <cmath>
+#endif
+
+namespace bartels {
+
+#ifdef __CUDACC__
+BT_HD float bt_sqrt(float x) { return sqrtf(x); }
+BT_HD double bt_sqrt(double x) { return sqrt(x); }
+BT_HD float bt_log(float x) { return logf(x); }
+BT_HD double bt_log(double x) { return log(x); }
+BT_HD float bt_cbrt(float x) { return cbrtf(x); }
+BT_HD double bt_cbrt(double x) { return cbrt(x); }
+BT_HD float bt_abs(float x) { return fabsf(x); }
+BT_HD double bt_abs(double x) { return fabs(x); }
+#else
+BT_HD float bt_sqrt(float x) { return std::sqrt(x); }
+BT_HD double bt_sqrt(double x) { return std::sqrt(x); }
+BT_HD float bt_log(float x) { return std::log(x); }
+BT_HD double bt_log(double x) { return std::log(x); }
+BT_HD float bt_cbrt(float x) { return std::cbrt(x); }
+BT_HD double bt_cbrt(double x) { return std::cbrt(x); }
+BT_HD float bt_abs(float x) { return std::fabs(x); }
+BT_HD double bt_abs(double x) { return std::fabs(x); }
+#endif
+
+enum { MODEL_NH = 0, MODEL_STVK = 1, MODEL_COROT = 2, MODEL_NH_ISO = 3 };
+
+template <class T>
+BT_HD T det3(const T *A) {
+  return A[0] * (A[4] * A[8] - A[5] * A[7]) - A[3] * (A[1] * A[8] - A[2] * A[7]) +
+         A[6] * (A[1] * A[5] - A[2] * A[4]);
+}
+
+// cofactor matrix G = dJ/dF (column-major)
+template <class T>
+BT_HD void cof3(T *G, const T *F) {
+  G[0] = F[4] * F[8] - F[7] * F[5];
+  G[1] = F[6] * F[5] - F[3] * F[8];
+  G[2] = F[3] * F[7] - F[6] * F[4];
+  G[3] = F[7] * F[2] - F[1] * F[8];
+  G[4] = F[0] * F[8] - F[6] * F[2];
+  G[5] = F[6] * F[1] - F[0] * F[7];
+  G[6] = F[1] * F[5] - F[4] * F[2];
+  G[7] = F[3] * F[2] - F[0] * F[5];
+  G[8] = F[0] * F[4] - F[3] * F[1];
+}
+
+// y = A x
+template <class T>
+BT_HD void mv3(T *y, const T *A, const T *x) {
+  y[0] = A[0] * x[0] + A[3] * x[1] + A[6] * x[2];
+  y[1] = A[1] * x[0] + A[4] * x[1] + A[7] * x[2];
+  y[2] = A[2] * x[0] + A[5] * x[1] + A[8] * x[2];
+}
+// y = A^T x
+template <class T>
+BT_HD void mtv3(T *y, const T *A, const T *x) {
+  y[0] = A[0] * x[0] + A[1] * x[1] + A[2] * x[2];
+  y[1] = A[3] * x[0] + A[4] * x[1] + A[5] * x[2];
+  y[2] = A[6] * x[0] + A[7] * x[1] + A[8] * x[2];
+}
+template <class T>
+BT_HD T dot3(const T *a, const T *b) {
+  return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+template <class T>
+BT_HD void cross3(T *c, const T *a, const T *b) {
+  c[0] = a[1] * b[2] - a[2] * b[1];
+  c[1] = a[2] * b[0] - a[0] * b[2];
+  c[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+// Deformation gradient F = F0 + sum_{a=1..3} (x_a - x_0) phi_a^T, where F0 is
+// the identity when x holds displacements from a rest shape consistent with
+// phi, and zero when x holds positions.
+template <class T>
+BT_HD void def_grad(T *F, const T *x0, const T *x1, const T *x2, const T *x3, const T *dphi9, bool add_identity) {
+  T d1[3] = {x1[0] - x0[0], x1[1] - x0[1], x1[2] - x0[2]};
+  T d2[3] = {x2[0] - x0[0], x2[1] - x0[1], x2[2] - x0[2]};
+  T d3[3] = {x3[0] - x0[0], x3[1] - x0[1], x3[2] - x0[2]};
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      F[i + 3 * j] = d1[i] * dphi9[0 + j] + d2[i] * dphi9[3 + j] + d3[i] * dphi9[6 + j] +
+                     ((add_identity && i == j) ? T(1) : T(0));
+}
+
+// ----------------------------------------------------------------------------
+// Hessian block laws: block(pa, pb, K) returns the 3x3 block (row-major K[k*3+l])
+// K_ab[k][l] = sum_{i,j} pa_i pb_j d2psi/dF(k,i)dF(l,j), with psi already scaled
+// by the tet volume (pv = vol * params). All laws are bilinear in (pa, pb).
+// ----------------------------------------------------------------------------
+
+// Neo-Hookean, psi = C (I1 - 3 - 2 ln J) + D (J-1)^2 (src/psi_neohookean_F.cpp:31).
+// d2psi = 2C I + (2C/J^2 + 2D) g g^T + (2D (J-1) - 2C/J) d2J, g = cof F, so
+// K_ab = 2C (pa.pb) I + ca (G pa)(G pb)^T + cb [F (pa x pb)]_x.
+template <class T>
+struct LawNH {
+  T F[9], G[9], c2, ca, cb;
+  BT_HD LawNH(const T *F_, const T *pv) {
+    for (int i = 0; i < 9; ++i) F[i] = F_[i];
+    cof3(G, F);
+    T J = F[0] * G[0] + F[1] * G[1] + F[2] * G[2];
+    T C = pv[0], D = pv[1];
+    c2 = T(2) * C;
+    ca = T(2) * C / (J * J) + T(2) * D;
+    cb = T(2) * D * (J - T(1)) - T(2) * C / J;
+  }
+  BT_HD void block(const T *pa, const T *pb, T *K) const {
+    T ga[3], gb[3], c[3], w[3];
+    mv3(ga, G, pa);
+    mv3(gb, G, pb);
+    cross3(c, pa, pb);
+    mv3(w, F, c);
+    T d = c2 * dot3(pa, pb);
+    for (int k = 0; k < 3; ++k)
+      for (int l = 0; l < 3; ++l) K[3 * k + l] = ca * ga[k] * gb[l] + (k == l ? d : T(0));
+    K[1] += cb * w[2];
+    K[2] -= cb * w[1];
+    K[3] -= cb * w[2];
+    K[5] += cb * w[0];
+    K[6] += cb * w[1];
+    K[7] -= cb * w[0];
+  }
+};
+
+// Isochoric Neo-Hookean, psi = C (J^{-2/3} I1 - 3) + D (J-1)^2 (the
+// reference's earlier law, src/psi_neohookean_F.cpp:8-14):
+// d2psi = 2C J^-2/3 I - 4/3 C J^-5/3 (F g^T + g F^T) + (10/9 C I1 J^-8/3 + 2D) g g^T
+//       + (2D (J-1) - 2/3 C I1 J^-5/3) d2J.
+template <class T>
+struct LawNHIso {
+  T F[9], G[9], a0, a1, a2, a3;
+  BT_HD LawNHIso(const T *F_, const T *pv) {
+    for (int i = 0; i < 9; ++i) F[i] = F_[i];
+    cof3(G, F);
+    T J = F[0] * G[0] + F[1] * G[1] + F[2] * G[2];
+    T I1 = T(0);
+    for (int i = 0; i < 9; ++i) I1 += F[i] * F[i];
+    T c = bt_cbrt(J), Jm23 = T(1) / (c * c), Jm53 = Jm23 / J, Jm83 = Jm53 / J;
+    T C = pv[0], D = pv[1];
+    a0 = T(2) * C * Jm23;
+    a1 = -T(4) / T(3) * C * Jm53;
+    a2 = T(10) / T(9) * C * I1 * Jm83 + T(2) * D;
+    a3 = T(2) * D * (J - T(1)) - T(2) / T(3) * C * I1 * Jm53;
+  }
+  BT_HD void block(const T *pa, const T *pb, T *K) const {
+    T ga[3], gb[3], fa[3], fb[3], c[3], w[3];
+    mv3(ga, G, pa);
+    mv3(gb, G, pb);
+    mv3(fa, F, pa);
+    mv3(fb, F, pb);
+    cross3(c, pa, pb);
+    mv3(w, F, c);
+    T d = a0 * dot3(pa, pb);
+    for (int k = 0; k < 3; ++k)
+      for (int l = 0; l < 3; ++l)
+        K[3 * k + l] = a1 * (fa[k] * gb[l] + ga[k] * fb[l]) + a2 * ga[k] * gb[l] + (k == l ? d : T(0));
+    K[1] += a3 * w[2];
+    K[2] -= a3 * w[1];
+    K[3] -= a3 * w[2];
+    K[5] += a3 * w[0];
+    K[6] += a3 * w[1];
+    K[7] -= a3 * w[0];
+  }
+};
+
+// StVK, psi = mu tr(E^2) + lambda/2 tr(E)^2, E = (F^T F - I)/2, pv = vol (lambda, mu)
+// (src/psi_stvk_F.cpp:11-12). From dP = dF S + F dS, S = 2 mu E + lambda tr(E) I:
+// K_ab = (pa . S pb) I + mu ((F pb)(F pa)^T + (pa . pb) F F^T) + lambda (F pa)(F pb)^T.
+template <class T>
+struct LawStVK {
+  T F[9], S[9], FFt[6], lam, mu;
+  BT_HD LawStVK(const T *F_, const T *pv) {
+    for (int i = 0; i < 9; ++i) F[i] = F_[i];
+    lam = pv[0];
+    mu = pv[1];
+    T C[9];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        C[i + 3 * j] = F[0 + 3 * i] * F[0 + 3 * j] + F[1 + 3 * i] * F[1 + 3 * j] + F[2 + 3 * i] * F[2 + 3 * j];
+    T trE = T(0.5) * (C[0] + C[4] + C[8] - T(3));
+    for (int i = 0; i < 9; ++i) S[i] = mu * (C[i] - ((i % 4) == 0 ? T(1) : T(0)));
+    S[0] += lam * trE;
+    S[4] += lam * trE;
+    S[8] += lam * trE;
+    // F F^T (symmetric): 00 11 22 01 02 12
+    FFt[0] = F[0] * F[0] + F[3] * F[3] + F[6] * F[6];
+    FFt[1] = F[1] * F[1] + F[4] * F[4] + F[7] * F[7];
+    FFt[2] = F[2] * F[2] + F[5] * F[5] + F[8] * F[8];
+    FFt[3] = F[0] * F[1] + F[3] * F[4] + F[6] * F[7];
+    FFt[4] = F[0] * F[2] + F[3] * F[5] + F[6] * F[8];
+    FFt[5] = F[1] * F[2] + F[4] * F[5] + F[7] * F[8];
+  }
+  BT_HD void block(const T *pa, const T *pb, T *K) const {
+    T fa[3], fb[3], sb[3];
+    mv3(fa, F, pa);
+    mv3(fb, F, pb);
+    mv3(sb, S, pb);
+    T d = dot3(pa, sb), m = mu * dot3(pa, pb);
+    const T ff[9] = {FFt[0], FFt[3], FFt[4], FFt[3], FFt[1], FFt[5], FFt[4], FFt[5], FFt[2]};
+    for (int k = 0; k < 3; ++k)
+      for (int l = 0; l < 3; ++l)
+        K[3 * k + l] = mu * fb[k] * fa[l] + m * ff[3 * k + l] + lam * fa[k] * fb[l] + (k == l ? d : T(0));
+  }
+};
+
+// ----------------------------------------------------------------------------
+// 3x3 SVD, F = U diag(S) V^T with U, V proper rotations, |S0| >= |S1| >= |S2|,
+// S0, S1 >= 0 and S2 carrying the sign of det F (the convention of the
+// rotation-variant SVD the reference calls through igl::svd3x3). Method
+// (McAdams et al. 2011 structure): symmetric Jacobi on F^T F for V, sort the
+// columns of B = F V by norm, then a Givens QR of B for U and the signed S.
+// ----------------------------------------------------------------------------
+template <class T>
+BT_HD void jacobi_rot(T *A, T *V, int p, int q) {
+  T apq = A[p + 3 * q];
+  if (apq == T(0)) return;
+  T theta = (A[q + 3 * q] - A[p + 3 * p]) / (T(2) * apq);
+  T t = (theta >= T(0) ? T(1) : T(-1)) / (bt_abs(theta) + bt_sqrt(theta * theta + T(1)));
+  T c = T(1) / bt_sqrt(t * t + T(1)), s = t * c;
+  for (int k = 0; k < 3; ++k) {
+    T akp = A[k + 3 * p], akq = A[k + 3 * q];
+    A[k + 3 * p] = c * akp - s * akq;
+    A[k + 3 * q] = s * akp + c * akq;
+  }
+  for (int k = 0; k < 3; ++k) {
+    T apk = A[p + 3 * k], aqk = A[q + 3 * k];
+    A[p + 3 * k] = c * apk - s * aqk;
+    A[q + 3 * k] = s * apk + c * aqk;
+  }
+  for (int k = 0; k < 3; ++k) {
+    T vkp = V[k + 3 * p], vkq = V[k + 3 * q];
+    V[k + 3 * p] = c * vkp - s * vkq;
+    V[k + 3 * q] = s * vkp + c * vkq;
+  }
+}
+
+template <class T>
+BT_HD void givens_rows(T *B, T *Q, int i, int k, int col) {
+  T a = B[i + 3 * col], b = B[k + 3 * col];
+  T r = bt_sqrt(a * a + b * b);
+  T c = T(1), s = T(0);
+  if (r > T(0)) {
+    c = a / r;
+    s = b / r;
+  }
+  for (int j = 0; j < 3; ++j) {
+    T bi = B[i + 3 * j], bk = B[k + 3 * j];
+    B[i + 3 * j] = c * bi + s * bk;
+    B[k + 3 * j] = -s * bi + c * bk;
+    T qi = Q[i + 3 * j], qk = Q[k + 3 * j];
+    Q[i + 3 * j] = c * qi + s * qk;
+    Q[k + 3 * j] = -s * qi + c * qk;
+  }
+}
+
+template <class T>
+BT_HD void svd3(const T *F, T *U, T *S, T *V) {
+  T A[9];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      A[i + 3 * j] = F[0 + 3 * i] * F[0 + 3 * j] + F[1 + 3 * i] * F[1 + 3 * j] + F[2 + 3 * i] * F[2 + 3 * j];
+  for (int i = 0; i < 9; ++i) V[i] = (i % 4 == 0) ? T(1) : T(0);
+  const int sweeps = sizeof(T) == 4 ? 6 : 12;
+  for (int s = 0; s < sweeps; ++s) {
+    T off = A[3] * A[3] + A[6] * A[6] + A[7] * A[7];
+    T dia = A[0] * A[0] + A[4] * A[4] + A[8] * A[8];
+    if (off <= (sizeof(T) == 4 ? T(1e-14) : T(1e-32)) * dia) break;
+    jacobi_rot(A, V, 0, 1);
+    jacobi_rot(A, V, 0, 2);
+    jacobi_rot(A, V, 1, 2);
+  }
+  T B[9];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      B[i + 3 * j] = F[i + 0] * V[0 + 3 * j] + F[i + 3] * V[1 + 3 * j] + F[i + 6] * V[2 + 3 * j];
+  T n[3];
+  for (int j = 0; j < 3; ++j) n[j] = B[3 * j] * B[3 * j] + B[3 * j + 1] * B[3 * j + 1] + B[3 * j + 2] * B[3 * j + 2];
+  // sort columns by decreasing norm
+  for (int a = 0; a < 2; ++a) {
+    int m = a;
+    for (int b = a + 1; b < 3; ++b)
+      if (n[b] > n[m]) m = b;
+    if (m != a) {
+      T tn = n[a];
+      n[a] = n[m];
+      n[m] = tn;
+      for (int k = 0; k < 3; ++k) {
+        T tb = B[k + 3 * a];
+        B[k + 3 * a] = B[k + 3 * m];
+        B[k + 3 * m] = tb;
+        T tv = V[k + 3 * a];
+        V[k + 3 * a] = V[k + 3 * m];
+        V[k + 3 * m] = tv;
+      }
+    }
+  }
+  if (det3(V) < T(0))
+    for (int k = 0; k < 3; ++k) {
+      V[k + 6] = -V[k + 6];
+      B[k + 6] = -B[k + 6];
+    }
+  T Q[9] = {T(1), T(0), T(0), T(0), T(1), T(0), T(0), T(0), T(1)};
+  givens_rows(B, Q, 0, 1, 0);
+  givens_rows(B, Q, 0, 2, 0);
+  givens_rows(B, Q, 1, 2, 1);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) U[i + 3 * j] = Q[j + 3 * i];
+  S[0] = B[0];
+  S[1] = B[4];
+  S[2] = B[8];
+}
+
+// Corotational, psi(S) = mu sum (s_i - 1)^2 + lambda/2 (sum s_i - 3)^2,
+// pv = vol (lambda, mu) (src/psi_corotational_S.cpp:8). Hessian from the
+// eigen-system of a stretch-based energy: scaling block 2 mu I + lambda 1 1^T,
+// flip (dpsi_i - dpsi_j)/(s_i - s_j) = 2 mu (closed form for this law, the
+// exact limit the reference approximates by perturbing F at repeated singular
+// values, src/d2psi_stretch_dF2.cpp:25-28), twist (dpsi_i + dpsi_j)/(s_i + s_j).
+// With frame A (alpha = A^T pa) and output frame R:
+//   K_ab = R Khat R^T, Khat = 2 mu diag(alpha o beta) + lambda alpha beta^T + pair terms.
+// Exact Hessian: A = V, R = U. The reference's layout (d2psi stored row-major,
+// src/d2psi_stretch_dF2.cpp:37-45) equals the Hessian at F^T: A = U, R = V.
+template <class T>
+struct LawCorot {
+  T A[9], R[9], mu2, lam, lt[3], lf[3];
+  BT_HD LawCorot(const T *F, const T *pv, bool exact) {
+    T U[9], S[3], V[9];
+    svd3(F, U, S, V);
+    for (int i = 0; i < 9; ++i) {
+      A[i] = exact ? V[i] : U[i];
+      R[i] = exact ? U[i] : V[i];
+    }
+    lam = pv[0];
+    T mu = pv[1];
+    mu2 = T(2) * mu;
+    T tr = S[0] + S[1] + S[2] - T(3);
+    T d[3];
+    for (int i = 0; i < 3; ++i) d[i] = mu2 * (S[i] - T(1)) + lam * tr;
+    const int P[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+    for (int k = 0; k < 3; ++k) {
+      int i = P[k][0], j = P[k][1];
+      bool repeated = bt_abs(S[i] - S[j]) < T(1e-5);
+      bool stalled = !repeated && bt_abs(S[j] * S[j] - S[i] * S[i]) < T(1e-8);
+      T den = S[i] + S[j];
+      lf[k] = stalled ? T(0) : mu2;
+      lt[k] = (stalled || den == T(0)) ? T(0) : (d[i] + d[j]) / den;
+    }
+  }
+  BT_HD void block(const T *pa, const T *pb, T *K) const {
+    T al[3], be[3];
+    mtv3(al, A, pa);
+    mtv3(be, A, pb);
+    T H[9];
+    for (int k = 0; k < 3; ++k)
+      for (int l = 0; l < 3; ++l) H[3 * k + l] = lam * al[k] * be[l] + (k == l ? mu2 * al[k] * be[k] : T(0));
+    const int P[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+    for (int k = 0; k < 3; ++k) {
+      int i = P[k][0], j = P[k][1];
+      T sp = T(0.5) * (lt[k] + lf[k]), sm = T(0.5) * (lf[k] - lt[k]);
+      H[3 * i + i] += sp * al[j] * be[j];
+      H[3 * j + j] += sp * al[i] * be[i];
+      H[3 * i + j] += sm * al[j] * be[i];
+      H[3 * j + i] += sm * al[i] * be[j];
+    }
+    // K = R H R^T (H row-major, R column-major)
+    T RH[9];
+    for (int k = 0; k < 3; ++k)
+      for (int l = 0; l < 3; ++l)
+        RH[3 * k + l] = R[k + 0] * H[0 + l] + R[k + 3] * H[3 + l] + R[k + 6] * H[6 + l];
+    for (int k = 0; k < 3; ++k)
+      for (int l = 0; l < 3; ++l)
+        K[3 * k + l] = RH[3 * k + 0] * R[l + 0] + RH[3 * k + 1] * R[l + 3] + RH[3 * k + 2] * R[l + 6];
+  }
+};
+
+// ----------------------------------------------------------------------------
+// FP64 energy and first Piola-Kirchhoff stress (scaled by vol via pv)
+// ----------------------------------------------------------------------------
+template <class T>
+BT_HD T psi_model(int model, const T *F, const T *pv) {
+  if (model == MODEL_NH || model == MODEL_NH_ISO) {
+    T J = det3(F), I1 = T(0);
+    for (int i = 0; i < 9; ++i) I1 += F[i] * F[i];
+    if (model == MODEL_NH) return pv[0] * (I1 - T(3) - T(2) * bt_log(J)) + pv[1] * (J - T(1)) * (J - T(1));
+    T c = bt_cbrt(J);
+    return pv[0] * (I1 / (c * c) - T(3)) + pv[1] * (J - T(1)) * (J - T(1));
+  }
+  if (model == MODEL_STVK) {
+    T C[9];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        C[i + 3 * j] = F[0 + 3 * i] * F[0 + 3 * j] + F[1 + 3 * i] * F[1 + 3 * j] + F[2 + 3 * i] * F[2 + 3 * j];
+    T E[9];
+    for (int i = 0; i < 9; ++i) E[i] = T(0.5) * (C[i] - ((i % 4) == 0 ? T(1) : T(0)));
+    T trE = E[0] + E[4] + E[8], trEE = T(0);
+    for (int i = 0; i < 9; ++i) trEE += E[i] * E[i];  // E symmetric: tr(E E) = sum E_ij^2
+    return pv[1] * trEE + T(0.5) * pv[0] * trE * trE;
+  }
+  T U[9], S[3], V[9];
+  svd3(F, U, S, V);
+  T tr = S[0] + S[1] + S[2] - T(3);
+  return pv[1] * ((S[0] - T(1)) * (S[0] - T(1)) + (S[1] - T(1)) * (S[1] - T(1)) + (S[2] - T(1)) * (S[2] - T(1))) +
+         T(0.5) * pv[0] * tr * tr;
+}
+
+template <class T>
+BT_HD void pk1_model(int model, const T *F, const T *pv, T *P) {
+  if (model == MODEL_NH || model == MODEL_NH_ISO) {
+    T G[9];
+    cof3(G, F);
+    T J = F[0] * G[0] + F[1] * G[1] + F[2] * G[2];
+    if (model == MODEL_NH) {
+      T a = T(2) * pv[0], b = T(2) * pv[0] / J, c = T(2) * pv[1] * (J - T(1));
+      for (int i = 0; i < 9; ++i) P[i] = a * F[i] - b * G[i] + c * G[i];
+    } else {
+      T I1 = T(0);
+      for (int i = 0; i < 9; ++i) I1 += F[i] * F[i];
+      T cr = bt_cbrt(J), Jm23 = T(1) / (cr * cr), Jm53 = Jm23 / J;
+      for (int i = 0; i < 9; ++i)
+        P[i] = pv[0] * (T(2) * Jm23 * F[i] - T(2) / T(3) * I1 * Jm53 * G[i]) + T(2) * pv[1] * (J - T(1)) * G[i];
+    }
+    return;
+  }
+  if (model == MODEL_STVK) {
+    T C[9];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        C[i + 3 * j] = F[0 + 3 * i] * F[0 + 3 * j] + F[1 + 3 * i] * F[1 + 3 * j] + F[2 + 3 * i] * F[2 + 3 * j];
+    T trE = T(0.5) * (C[0] + C[4] + C[8] - T(3));
+    T S[9];
+    for (int i = 0; i < 9; ++i) S[i] = pv[1] * (C[i] - ((i % 4) == 0 ? T(1) : T(0)));
+    S[0] += pv[0] * trE;
+    S[4] += pv[0] * trE;
+    S[8] += pv[0] * trE;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) P[i + 3 * j] = F[i] * S[3 * j] + F[i + 3] * S[3 * j + 1] + F[i + 6] * S[3 * j + 2];
+    return;
+  }
+  // corotational with the reference's inversion fix (src/dpsi_stretch_dF.cpp:20-45)
+  T U[9], S[3], V[9];
+  svd3(F, U, S, V);
+  T det = S[0] * S[1] * S[2];
+  if (det <= T(-1e-10))
+    for (int i = 0; i < 3; ++i)
+      if (S[i] < T(0)) S[i] = -S[i];
+  if (det3(U) <= T(0))
+    for (int k = 0; k < 3; ++k) U[k + 6] = -U[k + 6];
+  if (det3(V) <= T(0))
+    for (int k = 0; k < 3; ++k) V[k + 6] = -V[k + 6];
+  T tr = S[0] + S[1] + S[2] - T(3), d[3];
+  for (int i = 0; i < 3; ++i) d[i] = T(2) * pv[1] * (S[i] - T(1)) + pv[0] * tr;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      P[i + 3 * j] = U[i] * d[0] * V[j] + U[i + 3] * d[1] * V[j + 3] + U[i + 6] * d[2] * V[j + 6];
+}
+
+// ----------------------------------------------------------------------------
+// PSD projection helpers for one element (simple_psd_fix, src/simple_psd_fix.cpp)
+// K = B^T S B with B = Phi^T (x) I3 (Phi = 4x3 stack of phi_a^T). The
+// translations span null(B) and are eigenvectors of K with eigenvalue 0, so
+// the projected K is  (Q (x) I) W max(L, tol) W^T (Q^T (x) I) + tol/4 (1 1^T (x) I)
+// with Phi = Q R (thin QR) and M = (R (x) I) S (R^T (x) I) = W L W^T (9x9).
+// Fast test: min eig M >= tol  <=>  S - tol (G^-1 (x) I) is PSD, G = Phi^T Phi.
+// ----------------------------------------------------------------------------
+
+// 9x9 symmetric S from a block law: S[(k + 3 i) + 9 (l + 3 j)] = block(e_i, e_j)[k][l]
+template <class Law, class T>
+BT_HD void law_matrix9(const Law &law, T *S) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      T ei[3] = {T(0), T(0), T(0)}, ej[3] = {T(0), T(0), T(0)};
+      ei[i] = T(1);
+      ej[j] = T(1);
+      T K[9];
+      law.block(ei, ej, K);
+      for (int k = 0; k < 3; ++k)
+        for (int l = 0; l < 3; ++l) S[(k + 3 * i) + 9 * (l + 3 * j)] = K[3 * k + l];
+    }
+}
+
+// Cholesky test of the symmetric 9x9 A (overwritten); true if all pivots > 0.
+template <class T>
+BT_HD bool chol9_ok(T *A) {
+  for (int j = 0; j < 9; ++j) {
+    T d = A[j + 9 * j];
+    for (int k = 0; k < j; ++k) d -= A[j + 9 * k] * A[j + 9 * k];
+    if (!(d > T(0))) return false;
+    T s = bt_sqrt(d);
+    A[j + 9 * j] = s;
+    T inv = T(1) / s;
+    for (int i = j + 1; i < 9; ++i) {
+      T v = A[i + 9 * j];
+      for (int k = 0; k < j; ++k) v -= A[i + 9 * k] * A[j + 9 * k];
+      A[i + 9 * j] = v * inv;
+    }
+  }
+  return true;
+}
+
+// inverse of a symmetric 3x3 (column-major)
+template <class T>
+BT_HD void inv3(T *R, const T *A) {
+  T G[9];
+  cof3(G, A);
+  T J = A[0] * G[0] + A[1] * G[1] + A[2] * G[2];
+  T inv = T(1) / J;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) R[i + 3 * j] = G[j + 3 * i] * inv;
+}
+
+// phi: 4 gradients (phi[a][d]). G = Phi^T Phi.
+template <class T>
+BT_HD void gram3(T *G, const T (*phi)[3]) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      T s = T(0);
+      for (int a = 0; a < 4; ++a) s += phi[a][i] * phi[a][j];
+      G[i + 3 * j] = s;
+    }
+}
+
+// fast-path test on the element law: true when K needs no eigenvalue change
+// beyond the translation modes (all non-null eigenvalues >= tol).
+template <class Law, class T>
+BT_HD bool psd_fast_ok(const Law &law, const T (*phi)[3], T tol) {
+  T S[81], G[9], Gi[9];
+  law_matrix9(law, S);
+  gram3(G, phi);
+  inv3(Gi, G);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      for (int k = 0; k < 3; ++k) S[(k + 3 * i) + 9 * (k + 3 * j)] -= tol * Gi[i + 3 * j];
+  return chol9_ok(S);
+}
+
+// Cyclic Jacobi eigen-decomposition of a symmetric n x n A (column-major,
+// overwritten by a near-diagonal matrix), W = eigenvectors.
+template <int N, class T>
+BT_HD void jacobi_eig(T *A, T *W, int sweeps) {
+  for (int i = 0; i < N * N; ++i) W[i] = (i % (N + 1) == 0) ? T(1) : T(0);
+  for (int s = 0; s < sweeps; ++s) {
+    T off = T(0), tot = T(0);
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < N; ++j) {
+        T v = A[i + N * j] * A[i + N * j];
+        tot += v;
+        if (i != j) off += v;
+      }
+    if (off <= (sizeof(T) == 4 ? T(1e-13) : T(1e-30)) * tot) break;
+    for (int p = 0; p < N - 1; ++p)
+      for (int q = p + 1; q < N; ++q) {
+        T apq = A[p + N * q];
+        if (apq == T(0)) continue;
+        T theta = (A[q + N * q] - A[p + N * p]) / (T(2) * apq);
+        T t = (theta >= T(0) ? T(1) : T(-1)) / (bt_abs(theta) + bt_sqrt(theta * theta + T(1)));
+        T c = T(1) / bt_sqrt(t * t + T(1)), sn = t * c;
+        for (int k = 0; k < N; ++k) {
+          T akp = A[k + N * p], akq = A[k + N * q];
+          A[k + N * p] = c * akp - sn * akq;
+          A[k + N * q] = sn * akp + c * akq;
+        }
+        for (int k = 0; k < N; ++k) {
+          T apk = A[p + N * k], aqk = A[q + N * k];
+          A[p + N * k] = c * apk - sn * aqk;
+          A[q + N * k] = sn * apk + c * aqk;
+        }
+        for (int k = 0; k < N; ++k) {
+          T wkp = W[k + N * p], wkq = W[k + N * q];
+          W[k + N * p] = c * wkp - sn * wkq;
+          W[k + N * q] = sn * wkp + c * wkq;
+        }
+      }
+  }
+}
+
+// Slow path: the 4 projected blocks K_ab (b = 0..3) of row a (out[b][k*3+l]),
+// without the tol/4 translation term.
+template <class Law, class T>
+BT_HD_NOINLINE void psd_row_slow(const Law &law, const T (*phi)[3], T tol, int a, T (*out)[9]) {
+  T S[81];
+  law_matrix9(law, S);
+  // thin QR of Phi (4x3) by modified Gram-Schmidt on its columns
+  T Q[4][3], Rm[9];
+  for (int j = 0; j < 3; ++j) {
+    T v[4];
+    for (int r = 0; r < 4; ++r) v[r] = phi[r][j];
+    for (int i = 0; i < j; ++i) {
+      T d = T(0);
+      for (int r = 0; r < 4; ++r) d += Q[r][i] * v[r];
+      Rm[i + 3 * j] = d;
+      for (int r = 0; r < 4; ++r) v[r] -= d * Q[r][i];
+    }
+    T nrm = T(0);
+    for (int r = 0; r < 4; ++r) nrm += v[r] * v[r];
+    nrm = bt_sqrt(nrm);
+    Rm[j + 3 * j] = nrm;
+    for (int i = j + 1; i < 3; ++i) Rm[i + 3 * j] = T(0);
+    T inv = nrm > T(0) ? T(1) / nrm : T(0);
+    for (int r = 0; r < 4; ++r) Q[r][j] = v[r] * inv;
+  }
+  // M[(k + 3c), (l + 3d)] = sum_{i,j} R[c][i] R[d][j] S[(k + 3i), (l + 3j)]
+  T Tm[81], M[81];
+  for (int col = 0; col < 9; ++col)
+    for (int k = 0; k < 3; ++k)
+      for (int c = 0; c < 3; ++c) {
+        T s = T(0);
+        for (int i = 0; i < 3; ++i) s += Rm[c + 3 * i] * S[(k + 3 * i) + 9 * col];
+        Tm[(k + 3 * c) + 9 * col] = s;
+      }
+  for (int row = 0; row < 9; ++row)
+    for (int l = 0; l < 3; ++l)
+      for (int d = 0; d < 3; ++d) {
+        T s = T(0);
+        for (int j = 0; j < 3; ++j) s += Rm[d + 3 * j] * Tm[row + 9 * (l + 3 * j)];
+        M[row + 9 * (l + 3 * d)] = s;
+      }
+  for (int i = 0; i < 9; ++i)
+    for (int j = i + 1; j < 9; ++j) {
+      T s = T(0.5) * (M[i + 9 * j] + M[j + 9 * i]);
+      M[i + 9 * j] = s;
+      M[j + 9 * i] = s;
+    }
+  T W[81];
+  jacobi_eig<9>(M, W, sizeof(T) == 4 ? 12 : 30);
+  T lam[9];
+  for (int i = 0; i < 9; ++i) lam[i] = M[i + 9 * i] < tol ? tol : M[i + 9 * i];
+  // N = W diag(lam) W^T
+  T N[81];
+  for (int i = 0; i < 9; ++i)
+    for (int j = 0; j < 9; ++j) {
+      T s = T(0);
+      for (int k = 0; k < 9; ++k) s += W[i + 9 * k] * lam[k] * W[j + 9 * k];
+      N[i + 9 * j] = s;
+    }
+  for (int b = 0; b < 4; ++b)
+    for (int k = 0; k < 3; ++k)
+      for (int l = 0; l < 3; ++l) {
+        T s = T(0);
+        for (int c = 0; c < 3; ++c)
+          for (int d = 0; d < 3; ++d) s += Q[a][c] * Q[b][d] * N[(k + 3 * c) + 9 * (l + 3 * d)];
+        out[b][3 * k + l] = s;
+      }
+}
+
+}  // namespace bartels

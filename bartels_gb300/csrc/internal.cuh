@@ -1,0 +1,177 @@
+// Internal declarations of the GB300 tet-mesh library: context and plan
+// structures, per-tet records, error plumbing and small device math.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "bartels_gpu.h"
+
+namespace bartels {
+
+// ----------------------------------------------------------------- errors ---
+void set_error(const std::string &msg);
+int fail(int status, const std::string &msg);
+const char *last_error_cstr();
+
+#define BT_CUDA(call)                                                                       \
+  do {                                                                                      \
+    cudaError_t e_ = (call);                                                                \
+    if (e_ != cudaSuccess)                                                                  \
+      return ::bartels::fail(BARTELS_E_DEVICE, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+#define BT_CHECK(call)            \
+  do {                            \
+    int s_ = (call);              \
+    if (s_ != BARTELS_OK) return s_; \
+  } while (0)
+
+// Launch bookkeeping: every kernel launch goes through this so the context can
+// count launches and report launch errors.
+#define BT_LAUNCH(ctx, kernel, grid, block, smem, ...)                                     \
+  do {                                                                                      \
+    kernel<<<(grid), (block), (smem), (ctx)->stream>>>(__VA_ARGS__);                        \
+    (ctx)->launches++;                                                                      \
+    cudaError_t e_ = cudaGetLastError();                                                    \
+    if (e_ != cudaSuccess)                                                                  \
+      return ::bartels::fail(BARTELS_E_DEVICE, std::string("launch ") + #kernel + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+// ------------------------------------------------------------------ records ---
+// FP32 record of one tet for the Hessian kernels: 64 bytes, one aligned line
+// pair, loaded with four 16-byte loads.
+//   idx     : the 4 vertex ids
+//   dphi    : gradients of shape functions 1..3 (rows 1..3 of the reference's
+//             4x3 dphidX), phi_0 = -(phi_1 + phi_2 + phi_3)
+//   pv      : vol * params (both laws are linear in params)
+//   mass    : density * vol
+struct alignas(16) TetRec32 {
+  int4 idx;
+  float dphi[9];  // dphi[3*(a-1) + d] = d phi_a / d X_d, a = 1..3
+  float pv[2];
+  float mass;
+};
+static_assert(sizeof(TetRec32) == 64, "TetRec32 must be 64 bytes");
+
+// FP64 record for energy / gradient kernels (thread per tet): 128 bytes.
+struct alignas(16) TetRec64 {
+  double dphi[9];
+  double pv[2];
+  double mass;
+  int4 idx;
+  double vol;
+  double pad;
+};
+static_assert(sizeof(TetRec64) == 128, "TetRec64 must be 128 bytes");
+
+// Device buffer with geometric growth.
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  int ensure(size_t n);
+  void release();
+  template <class T>
+  T *as() const { return static_cast<T *>(p); }
+};
+
+}  // namespace bartels
+
+struct bartels_ctx_s {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  int64_t launches = 0;
+  // pinned host staging for small read-backs
+  double *host_scalars = nullptr;
+  // device scratch for reductions
+  bartels::DevBuf partials, scalars;
+  // large host<->device staging (grown on demand)
+  bartels::DevBuf stage_a, stage_b, stage_c, stage_d, stage_e;
+};
+
+struct bartels_mesh_plan_s {
+  bartels_ctx ctx = nullptr;
+  int nV = 0, nT = 0;
+  // rest geometry
+  double *X = nullptr;        // 3 nV interleaved rest positions
+  int4 *E = nullptr;          // nT
+  // element data (FP64 master copies)
+  double *dphi64 = nullptr;   // nT x 9 (rows 1..3 of dphidX, per tet contiguous)
+  double *vol = nullptr;      // nT
+  double *params = nullptr;   // nT x 2 (per tet contiguous)
+  double *density = nullptr;  // nT
+  bartels::TetRec32 *rec32 = nullptr;
+  bartels::TetRec64 *rec64 = nullptr;
+  // incidence lists: for vertex v, entries inc_ptr[v] .. inc_ptr[v+1]-1 in tet order
+  int *inc_ptr = nullptr;     // nV + 1
+  int *inc_tet = nullptr;     // 4 nT : tet * 4 + local slot
+  uint32_t *inc_pos = nullptr;// 4 nT : 4 x 8-bit block positions in the row of v
+  // block pattern (3x3 blocks), values stored in scalar-CSR order
+  int *brp = nullptr;         // nV + 1
+  int *bcol = nullptr;        // nnzb
+  int *diag_pos = nullptr;    // nV: position of the diagonal block within its row
+  int64_t nnzb = 0;
+  int max_row_blocks = 0;
+  // assembly chunks (consecutive vertex ranges whose values fit in shared memory)
+  int *chunk_v = nullptr;     // nchunks + 1
+  int nchunks = 0;
+  std::vector<int> h_brp, h_bcol, h_chunk_v;  // host copies
+  // lazily built scalar CSR pattern (device)
+  int *csr_rp = nullptr, *csr_col = nullptr;
+  // Newton problem data
+  double *q_base = nullptr, *x_hat = nullptr, *f_ext = nullptr;
+  unsigned char *pinned = nullptr;
+  // true when dphidX is the rest shape's own (F = I + sum (u_a - u_0) phi_a^T)
+  bool dphi_matches_rest = true;
+  // solver workspace
+  bartels::DevBuf w_values, w_minv, w_vec, w_grad_e, w_energy, w_u, w_pcg;
+};
+
+namespace bartels {
+
+constexpr int kChunkFloats = 16384;  // 64 KB of shared memory per assembly CTA
+constexpr int kChunkMaxVerts = 128;
+
+// value offset of block row v (first value of row 3v)
+__host__ __device__ inline int64_t row_value_base(const int *brp, int v) { return 9ll * brp[v]; }
+
+// Kernel-side entry points implemented in the .cu files.
+int plan_build(bartels_mesh_plan plan, const double *V_host, const int *E_host);
+int plan_refresh_records(bartels_mesh_plan plan);
+int plan_build_csr_pattern(bartels_mesh_plan plan);
+
+int launch_dphi_vol(bartels_ctx ctx, int nV, const double *X3, int nT, const int4 *E, double *dphidX_colmajor,
+                    double *dphi9, double *vol);
+
+struct ObjectiveDev {
+  double mass_coeff = 0.0;  // multiplies the mass terms
+  double scale = 1.0;       // q = q_base + scale * x
+  double force_scale = 0.0; // multiplies x^T f_ext
+  const double *q_base = nullptr;
+  const double *x_hat = nullptr;
+  const double *f_ext = nullptr;
+  const unsigned char *pinned = nullptr;
+};
+
+// energy of the objective at x; result (FP64) left in *d_out (device) and
+// returned through the pinned scalar if host_out != nullptr.
+int energy(bartels_ctx ctx, bartels_mesh_plan plan, int model, const ObjectiveDev &obj, const double *x,
+           double *d_out);
+int gradient(bartels_ctx ctx, bartels_mesh_plan plan, int model, const ObjectiveDev &obj, const double *x,
+             double *g);
+int hessian(bartels_ctx ctx, bartels_mesh_plan plan, int model, int psd_mode, float psd_tol, int flags,
+            double coeff_K, double coeff_M, const double *q_or_null, const ObjectiveDev &obj, const double *x,
+            float *values);
+int mass_values(bartels_ctx ctx, bartels_mesh_plan plan, float *values32, double *values64);
+int ext_force(bartels_ctx ctx, bartels_mesh_plan plan, const double traction[3], double *f);
+int values_to_double(bartels_ctx ctx, const float *v32, double *v64, int64_t n);
+
+// sums n doubles deterministically into *out (device)
+int reduce_sum(bartels_ctx ctx, const double *in, int n, double *out);
+int dot(bartels_ctx ctx, const double *a, const double *b, int n, double *out);
+
+}  // namespace bartels

@@ -1,0 +1,781 @@
+// Linear solve and Newton driver.
+//
+// PCG: FP32 SpMV / vectors with a 3x3 block-Jacobi preconditioner, captured as
+// CUDA graphs of a fixed number of iterations that become no-ops once the
+// device-side convergence flag is set. An outer FP64 loop recomputes the true
+// residual b - A x in FP64 and restarts PCG on it (iterative refinement) until
+// ||b - A x|| <= rel_tol ||b||.
+//
+// Newton: gradient (FP64) -> Hessian (FP32, fused assembly) -> PCG -> the
+// reference's backtracking line search (src/linesearch_backtracking_bisection.cpp:17-30)
+// on the device-evaluated FP64 objective, following newtons_method_bisection
+// (include/optimization_gradient_based.h:77-106).
+#include <chrono>
+#include <cmath>
+#include <cstring>
+
+#include "devmath.cuh"
+#include "internal.cuh"
+
+namespace bartels {
+
+int launch_prep_u(bartels_ctx ctx, bartels_mesh_plan plan, const double *x, const double *q_base, double scale,
+                  bool displacement, float4 *u);
+int launch_hess(bartels_ctx ctx, bartels_mesh_plan plan, int model, int psd_mode, const float4 *u, int add_identity,
+                float cK, float cM, float tol, int flags, float *values);
+
+constexpr int kVecBlocksPerSM = 4;
+constexpr int kSpmvBlocksPerSM = 8;
+
+struct PcgState {
+  double rz[2];
+  double rr0;
+  double rr;
+  double tol2;
+  int it;
+  int done;
+  int max_it;
+  int pad;
+};
+
+// ------------------------------------------------------------- reductions ---
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_sumf(float v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// sum of blockDim-strided values of one double per thread; returns in thread 0
+__device__ __forceinline__ double cta_sum(double v) {
+  __shared__ double red[32];
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (w == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    s = lane < nw ? red[lane] : 0.0;
+    s = warp_sum(s);
+  }
+  __syncthreads();
+  return s;
+}
+
+// every block: deterministic sum of n partials, broadcast to all threads
+__device__ __forceinline__ double cta_sum_array(const double *__restrict__ a, int n) {
+  __shared__ double bcast;
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) acc += a[i];
+  double s = cta_sum(acc);
+  if (threadIdx.x == 0) bcast = s;
+  __syncthreads();
+  s = bcast;
+  __syncthreads();
+  return s;
+}
+
+// ------------------------------------------------------------------ SpMV ---
+// Block layout: one warp per vertex row. Lanes walk the (block, component)
+// pairs of the row; each lane reads the three scalar rows at that column.
+template <bool DOT>
+__global__ void __launch_bounds__(256)
+k_spmv_blk(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, const float *__restrict__ val,
+           const float *__restrict__ x, float *__restrict__ y, const unsigned char *__restrict__ pinned,
+           double *__restrict__ partial, const PcgState *__restrict__ st) {
+  if (st && st->done) return;
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  double acc = 0.0;
+  for (int v = warp; v < nV; v += nwarps) {
+    const int rb = brp[v];
+    const int rs = 3 * (brp[v + 1] - rb);
+    const float *r0 = val + 9ll * rb;
+    float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+    for (int e = lane; e < rs; e += 32) {
+      const int j = e / 3, l = e - 3 * j;
+      const float xv = __ldg(x + 3 * __ldg(bcol + rb + j) + l);
+      s0 += __ldg(r0 + e) * xv;
+      s1 += __ldg(r0 + rs + e) * xv;
+      s2 += __ldg(r0 + 2 * rs + e) * xv;
+    }
+    s0 = warp_sumf(s0);
+    s1 = warp_sumf(s1);
+    s2 = warp_sumf(s2);
+    if (pinned && pinned[v]) s0 = s1 = s2 = 0.f;
+    if (lane == 0) {
+      y[3 * v] = s0;
+      y[3 * v + 1] = s1;
+      y[3 * v + 2] = s2;
+      if (DOT) acc += (double)(x[3 * v] * s0 + x[3 * v + 1] * s1 + x[3 * v + 2] * s2);
+    }
+  }
+  if (DOT) {
+    double s = cta_sum(acc);
+    if (threadIdx.x == 0) partial[blockIdx.x] = s;
+  }
+}
+
+// FP64 residual r = b - A x (block layout), partial sums of r.r
+__global__ void __launch_bounds__(256)
+k_resid_blk64(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, const float *__restrict__ val,
+              const double *__restrict__ x, const double *__restrict__ b, double *__restrict__ r,
+              const unsigned char *__restrict__ pinned, double *__restrict__ partial) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  double acc = 0.0;
+  for (int v = warp; v < nV; v += nwarps) {
+    const int rb = brp[v];
+    const int rs = 3 * (brp[v + 1] - rb);
+    const float *r0 = val + 9ll * rb;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    for (int e = lane; e < rs; e += 32) {
+      const int j = e / 3, l = e - 3 * j;
+      const double xv = x[3 * bcol[rb + j] + l];
+      s0 += (double)r0[e] * xv;
+      s1 += (double)r0[rs + e] * xv;
+      s2 += (double)r0[2 * rs + e] * xv;
+    }
+    s0 = warp_sum(s0);
+    s1 = warp_sum(s1);
+    s2 = warp_sum(s2);
+    if (lane == 0) {
+      double q0 = b[3 * v] - s0, q1 = b[3 * v + 1] - s1, q2 = b[3 * v + 2] - s2;
+      if (pinned && pinned[v]) q0 = q1 = q2 = 0.0;
+      r[3 * v] = q0;
+      r[3 * v + 1] = q1;
+      r[3 * v + 2] = q2;
+      acc += q0 * q0 + q1 * q1 + q2 * q2;
+    }
+  }
+  double s = cta_sum(acc);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+// generic scalar CSR (drop-in search direction): one warp per row
+template <bool DOT>
+__global__ void __launch_bounds__(256)
+k_spmv_csr(int n, const int *__restrict__ rp, const int *__restrict__ ci, const float *__restrict__ val,
+           const float *__restrict__ x, float *__restrict__ y, double *__restrict__ partial,
+           const PcgState *__restrict__ st) {
+  if (st && st->done) return;
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  double acc = 0.0;
+  for (int i = warp; i < n; i += nwarps) {
+    float s = 0.f;
+    for (int k = rp[i] + lane; k < rp[i + 1]; k += 32) s += val[k] * __ldg(x + ci[k]);
+    s = warp_sumf(s);
+    if (lane == 0) {
+      y[i] = s;
+      if (DOT) acc += (double)(x[i] * s);
+    }
+  }
+  if (DOT) {
+    double s = cta_sum(acc);
+    if (threadIdx.x == 0) partial[blockIdx.x] = s;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+k_resid_csr64(int n, const int *__restrict__ rp, const int *__restrict__ ci, const float *__restrict__ val,
+              const double *__restrict__ x, const double *__restrict__ b, double *__restrict__ r,
+              double *__restrict__ partial) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  double acc = 0.0;
+  for (int i = warp; i < n; i += nwarps) {
+    double s = 0.0;
+    for (int k = rp[i] + lane; k < rp[i + 1]; k += 32) s += (double)val[k] * x[ci[k]];
+    s = warp_sum(s);
+    if (lane == 0) {
+      double q = b[i] - s;
+      r[i] = q;
+      acc += q * q;
+    }
+  }
+  double s = cta_sum(acc);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+// ------------------------------------------------------- block Jacobi ------
+// inverse of each 3x3 diagonal block (FP64 inversion, FP32 storage). Blocks
+// that are pinned get 0; singular or indefinite blocks fall back to the
+// inverse diagonal.
+__device__ void store_inv3(const double *A, float *out) {
+  double G[9];
+  cof3(G, A);
+  double det = A[0] * G[0] + A[1] * G[1] + A[2] * G[2];
+  bool ok = det > 0.0 && isfinite(det);
+  for (int i = 0; i < 9; ++i) out[i] = 0.f;
+  if (ok) {
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) out[3 * i + j] = (float)(G[j + 3 * i] / det);  // row-major inverse
+  } else {
+    for (int i = 0; i < 3; ++i) {
+      double d = A[i + 3 * i];
+      out[4 * i] = (d != 0.0 && isfinite(d)) ? (float)(1.0 / d) : 1.f;
+    }
+  }
+}
+
+__global__ void k_minv_blk(int nV, const int *__restrict__ brp, const int *__restrict__ diag_pos,
+                           const float *__restrict__ val, const unsigned char *__restrict__ pinned,
+                           float *__restrict__ minv) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nV; v += gridDim.x * blockDim.x) {
+    const int rb = brp[v], rs = 3 * (brp[v + 1] - rb), j = diag_pos[v];
+    const float *r0 = val + 9ll * rb;
+    double A[9];
+    for (int k = 0; k < 3; ++k)
+      for (int l = 0; l < 3; ++l) A[k + 3 * l] = r0[k * rs + 3 * j + l];
+    float out[9];
+    if (pinned && pinned[v]) {
+      for (int i = 0; i < 9; ++i) out[i] = 0.f;
+    } else {
+      store_inv3(A, out);
+    }
+    for (int i = 0; i < 9; ++i) minv[9ll * v + i] = out[i];
+  }
+}
+
+__global__ void k_minv_csr(int nb, int n, const int *__restrict__ rp, const int *__restrict__ ci,
+                           const float *__restrict__ val, float *__restrict__ minv) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nb; v += gridDim.x * blockDim.x) {
+    double A[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < 3; ++k) {
+      const int row = 3 * v + k;
+      if (row >= n) {
+        A[k + 3 * k] = 1.0;
+        continue;
+      }
+      for (int e = rp[row]; e < rp[row + 1]; ++e) {
+        const int c = ci[e] - 3 * v;
+        if (c >= 0 && c < 3) A[k + 3 * c] += val[e];
+      }
+    }
+    float out[9];
+    store_inv3(A, out);
+    for (int i = 0; i < 9; ++i) minv[9ll * v + i] = out[i];
+  }
+}
+
+// ------------------------------------------------------------ PCG vectors ---
+__device__ __forceinline__ void apply_minv(const float *__restrict__ minv, int v, const float *r, float *z) {
+  const float *m = minv + 9ll * v;
+  z[0] = m[0] * r[0] + m[1] * r[1] + m[2] * r[2];
+  z[1] = m[3] * r[0] + m[4] * r[1] + m[5] * r[2];
+  z[2] = m[6] * r[0] + m[7] * r[1] + m[8] * r[2];
+}
+
+// start of an inner solve: x = 0, r = (float) r64, z = M^-1 r, p = z
+__global__ void k_pcg_init(int nb, int n, const double *__restrict__ r64, const float *__restrict__ minv,
+                           float *__restrict__ x, float *__restrict__ r, float *__restrict__ z,
+                           float *__restrict__ p, double *__restrict__ part_rz, double *__restrict__ part_rr) {
+  double arz = 0.0, arr = 0.0;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nb; v += gridDim.x * blockDim.x) {
+    float rv[3], zv[3];
+    for (int k = 0; k < 3; ++k) rv[k] = (3 * v + k < n) ? (float)r64[3 * v + k] : 0.f;
+    apply_minv(minv, v, rv, zv);
+    for (int k = 0; k < 3; ++k) {
+      const int i = 3 * v + k;
+      if (i < n) {
+        x[i] = 0.f;
+        r[i] = rv[k];
+        z[i] = zv[k];
+        p[i] = zv[k];
+        arz += (double)rv[k] * zv[k];
+        arr += (double)rv[k] * rv[k];
+      }
+    }
+  }
+  double s = cta_sum(arz);
+  if (threadIdx.x == 0) part_rz[blockIdx.x] = s;
+  s = cta_sum(arr);
+  if (threadIdx.x == 0) part_rr[blockIdx.x] = s;
+}
+
+__global__ void k_pcg_setup_state(int nparts, const double *__restrict__ part_rz, const double *__restrict__ part_rr,
+                                  double inner_rel2, double abs_tol2, int max_it, PcgState *__restrict__ st) {
+  const double rz = cta_sum_array(part_rz, nparts);
+  const double rr = cta_sum_array(part_rr, nparts);
+  if (threadIdx.x == 0) {
+    st->rz[0] = rz;
+    st->rz[1] = rz;
+    st->rr0 = rr;
+    st->rr = rr;
+    st->tol2 = fmax(inner_rel2 * rr, abs_tol2);
+    st->it = -1;
+    st->max_it = max_it;
+    st->done = (rr <= st->tol2 || max_it <= 0) ? 1 : 0;
+  }
+}
+
+// iteration counter (one thread) -- runs before the SpMV of each iteration
+__global__ void k_pcg_tick(PcgState *__restrict__ st) {
+  if (!st->done) st->it += 1;
+}
+
+// alpha = rz / pAp; x += alpha p; r -= alpha Ap; z = M^-1 r; partial r.z, r.r
+__global__ void k_pcg_update(int nb, int n, int nparts, const double *__restrict__ part_pap,
+                             const float *__restrict__ minv, const float *__restrict__ p, const float *__restrict__ ap,
+                             float *__restrict__ x, float *__restrict__ r, float *__restrict__ z,
+                             double *__restrict__ part_rz, double *__restrict__ part_rr,
+                             const PcgState *__restrict__ st) {
+  if (st->done) return;
+  const double pap = cta_sum_array(part_pap, nparts);
+  const float alpha = (float)(st->rz[st->it & 1] / pap);
+  double arz = 0.0, arr = 0.0;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nb; v += gridDim.x * blockDim.x) {
+    float rv[3], zv[3];
+    for (int k = 0; k < 3; ++k) {
+      const int i = 3 * v + k;
+      if (i < n) {
+        x[i] += alpha * p[i];
+        rv[k] = r[i] - alpha * ap[i];
+        r[i] = rv[k];
+      } else {
+        rv[k] = 0.f;
+      }
+    }
+    apply_minv(minv, v, rv, zv);
+    for (int k = 0; k < 3; ++k) {
+      const int i = 3 * v + k;
+      if (i < n) {
+        z[i] = zv[k];
+        arz += (double)rv[k] * zv[k];
+        arr += (double)rv[k] * rv[k];
+      }
+    }
+  }
+  double s = cta_sum(arz);
+  if (threadIdx.x == 0) part_rz[blockIdx.x] = s;
+  s = cta_sum(arr);
+  if (threadIdx.x == 0) part_rr[blockIdx.x] = s;
+}
+
+// beta = rz_new / rz; p = z + beta p; convergence test
+__global__ void k_pcg_dir(int n, int nparts, const double *__restrict__ part_rz, const double *__restrict__ part_rr,
+                          const float *__restrict__ z, float *__restrict__ p, PcgState *__restrict__ st) {
+  if (st->done) return;
+  const double rz_new = cta_sum_array(part_rz, nparts);
+  const double rr = cta_sum_array(part_rr, nparts);
+  const int par = st->it & 1;
+  const float beta = (float)(rz_new / st->rz[par]);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = z[i] + beta * p[i];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    st->rz[par ^ 1] = rz_new;
+    st->rr = rr;
+    if (rr <= st->tol2 || st->it + 1 >= st->max_it || !(rr == rr)) st->done = 1;
+  }
+}
+
+__global__ void k_axpy64(int n, const float *__restrict__ dx, double *__restrict__ x) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] += (double)dx[i];
+}
+
+__global__ void k_scale_copy(int n, double a, const double *__restrict__ x, double *__restrict__ y) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) y[i] = a * x[i];
+}
+
+__global__ void k_axpy_to(int n, const double *__restrict__ x, double a, const double *__restrict__ d,
+                          double *__restrict__ y) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) y[i] = x[i] + a * d[i];
+}
+
+__global__ void k_f64_to_f32(int64_t n, const double *__restrict__ a, float *__restrict__ b) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+// ================================================================ host ======
+struct PcgOperator {
+  // block layout (plan)
+  bartels_mesh_plan plan = nullptr;
+  const float *values = nullptr;
+  const unsigned char *pinned = nullptr;
+  // generic CSR
+  int n = 0;
+  const int *rp = nullptr, *ci = nullptr;
+};
+
+struct PcgWork {
+  float *x, *r, *z, *p, *ap, *minv;
+  double *r64, *part_a, *part_b, *part_c;
+  PcgState *st;
+  int nparts_spmv, nparts_vec;
+};
+
+static int grid_vec(bartels_ctx ctx, int64_t n) {
+  int64_t g = (n + 255) / 256;
+  int64_t cap = (int64_t)ctx->num_sms * kVecBlocksPerSM;
+  return (int)std::max<int64_t>(1, std::min(g, cap));
+}
+static int grid_spmv(bartels_ctx ctx, int64_t rows) {
+  int64_t g = (rows + 7) / 8;  // 8 warps per 256-thread block
+  int64_t cap = (int64_t)ctx->num_sms * kSpmvBlocksPerSM;
+  return (int)std::max<int64_t>(1, std::min(g, cap));
+}
+
+struct GraphCache {
+  cudaGraphExec_t exec = nullptr;
+  const void *key[8] = {};
+  int iters = 0;
+};
+
+static int pcg_enqueue_iters(bartels_ctx ctx, const PcgOperator &op, const PcgWork &w, int n, int nb, int iters) {
+  const bool blk = op.plan != nullptr;
+  const int gs = blk ? grid_spmv(ctx, op.plan->nV) : grid_spmv(ctx, n);
+  const int gv = grid_vec(ctx, nb);
+  const int gd = grid_vec(ctx, n);
+  for (int i = 0; i < iters; ++i) {
+    BT_LAUNCH(ctx, k_pcg_tick, 1, 1, 0, w.st);
+    if (blk) {
+      BT_LAUNCH(ctx, k_spmv_blk<true>, gs, 256, 0, op.plan->nV, op.plan->brp, op.plan->bcol, op.values, w.p, w.ap,
+                op.pinned, w.part_a, w.st);
+    } else {
+      BT_LAUNCH(ctx, k_spmv_csr<true>, gs, 256, 0, n, op.rp, op.ci, op.values, w.p, w.ap, w.part_a, w.st);
+    }
+    BT_LAUNCH(ctx, k_pcg_update, gv, 256, 0, nb, n, gs, w.part_a, w.minv, w.p, w.ap, w.x, w.r, w.z, w.part_b,
+              w.part_c, w.st);
+    BT_LAUNCH(ctx, k_pcg_dir, gd, 256, 0, n, gv, w.part_b, w.part_c, w.z, w.p, w.st);
+  }
+  return BARTELS_OK;
+}
+
+// Run a full PCG solve of A x = b (FP64 in/out, device pointers) with FP64
+// residual refinement. x must be initialised (normally 0).
+static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double *b, double *x, DevBuf &wbuf,
+                     const bartels_pcg_params &prm, bartels_pcg_report *rep) {
+  const int nb = (n + 2) / 3;
+  const bool blk = op.plan != nullptr;
+  const int gs = blk ? grid_spmv(ctx, op.plan->nV) : grid_spmv(ctx, n);
+  const int gv = grid_vec(ctx, nb);
+  const int nparts = std::max(gs, gv);
+  // workspace layout
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off += (bytes + 255) & ~size_t(255);
+    return o;
+  };
+  const size_t o_x = take(4ull * n), o_r = take(4ull * n), o_z = take(4ull * n), o_p = take(4ull * n),
+               o_ap = take(4ull * n), o_minv = take(36ull * nb), o_r64 = take(8ull * n), o_pa = take(8ull * nparts),
+               o_pb = take(8ull * nparts), o_pc = take(8ull * nparts), o_st = take(sizeof(PcgState));
+  BT_CHECK(wbuf.ensure(off));
+  char *base = wbuf.as<char>();
+  PcgWork w;
+  w.x = (float *)(base + o_x);
+  w.r = (float *)(base + o_r);
+  w.z = (float *)(base + o_z);
+  w.p = (float *)(base + o_p);
+  w.ap = (float *)(base + o_ap);
+  w.minv = (float *)(base + o_minv);
+  w.r64 = (double *)(base + o_r64);
+  w.part_a = (double *)(base + o_pa);
+  w.part_b = (double *)(base + o_pb);
+  w.part_c = (double *)(base + o_pc);
+  w.st = (PcgState *)(base + o_st);
+  w.nparts_spmv = gs;
+  w.nparts_vec = gv;
+  // preconditioner
+  if (blk) {
+    BT_LAUNCH(ctx, k_minv_blk, grid_vec(ctx, op.plan->nV), 256, 0, op.plan->nV, op.plan->brp, op.plan->diag_pos,
+              op.values, op.pinned, w.minv);
+  } else {
+    BT_LAUNCH(ctx, k_minv_csr, grid_vec(ctx, nb), 256, 0, nb, n, op.rp, op.ci, op.values, w.minv);
+  }
+  // ||b||
+  BT_CHECK(dot(ctx, b, b, n, (double *)&w.st->rr0));
+  double bb = 0.0;
+  BT_CUDA(cudaMemcpyAsync(&bb, &w.st->rr0, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  BT_CUDA(cudaStreamSynchronize(ctx->stream));
+  const double bnorm = std::sqrt(bb);
+  rep->iterations = 0;
+  rep->refinements = 0;
+  rep->converged = 0;
+  rep->rel_residual = 0.0;
+  if (!(bnorm > 0.0)) {
+    BT_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, ctx->stream));
+    rep->converged = std::isfinite(bnorm) ? 1 : 0;
+    return rep->converged ? BARTELS_OK : fail(BARTELS_E_NONFINITE, "non-finite right-hand side");
+  }
+  const double target = prm.rel_tol * bnorm;
+  // CUDA graph of a fixed number of PCG iterations (kernels no-op once done)
+  const int chunk = 16;
+  cudaGraphExec_t exec = nullptr;
+  {
+    cudaGraph_t graph;
+    const int64_t launches_before = ctx->launches;
+    BT_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    int s = pcg_enqueue_iters(ctx, op, w, n, nb, chunk);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+    ctx->launches = launches_before;  // counted per graph launch below
+    if (s != BARTELS_OK) return s;
+    if (e != cudaSuccess) return fail(BARTELS_E_DEVICE, std::string("graph capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(BARTELS_E_DEVICE, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  }
+  int status = BARTELS_OK;
+  double rel = 0.0;
+  PcgState hs;
+  for (int pass = 0; pass <= prm.max_refinements; ++pass) {
+    // r64 = b - A x (FP64)
+    if (blk) {
+      BT_LAUNCH(ctx, k_resid_blk64, gs, 256, 0, op.plan->nV, op.plan->brp, op.plan->bcol, op.values, x, b, w.r64,
+                op.pinned, w.part_a);
+    } else {
+      BT_LAUNCH(ctx, k_resid_csr64, gs, 256, 0, n, op.rp, op.ci, op.values, x, b, w.r64, w.part_a);
+    }
+    BT_CHECK(reduce_sum(ctx, w.part_a, gs, &w.st->rr));
+    double rr = 0.0;
+    BT_CUDA(cudaMemcpyAsync(&rr, &w.st->rr, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    BT_CUDA(cudaStreamSynchronize(ctx->stream));
+    rel = std::sqrt(rr) / bnorm;
+    rep->rel_residual = rel;
+    if (!std::isfinite(rel)) {
+      status = fail(BARTELS_E_NONFINITE, "PCG residual is not finite");
+      break;
+    }
+    if (std::sqrt(rr) <= target) {
+      rep->converged = 1;
+      break;
+    }
+    if (pass == prm.max_refinements || rep->iterations >= prm.max_iters) {
+      status = fail(BARTELS_E_NOT_CONVERGED, "PCG did not reach the residual target");
+      break;
+    }
+    rep->refinements = pass + 1;
+    // inner FP32 PCG on r64
+    BT_LAUNCH(ctx, k_pcg_init, gv, 256, 0, nb, n, w.r64, w.minv, w.x, w.r, w.z, w.p, w.part_b, w.part_c);
+    const double abs2 = (0.5 * target) * (0.5 * target);
+    BT_LAUNCH(ctx, k_pcg_setup_state, 1, 1024, 0, gv, w.part_b, w.part_c, prm.inner_rel_tol * prm.inner_rel_tol,
+              abs2, prm.max_iters - rep->iterations, w.st);
+    for (;;) {
+      BT_CUDA(cudaGraphLaunch(exec, ctx->stream));
+      ctx->launches += 4 * chunk;
+      BT_CUDA(cudaMemcpyAsync(&hs, w.st, sizeof(PcgState), cudaMemcpyDeviceToHost, ctx->stream));
+      BT_CUDA(cudaStreamSynchronize(ctx->stream));
+      if (hs.done) break;
+    }
+    rep->iterations += hs.it + 1;
+    BT_LAUNCH(ctx, k_axpy64, grid_vec(ctx, n), 256, 0, n, w.x, x);
+  }
+  cudaGraphExecDestroy(exec);
+  return status;
+}
+
+// ============================================================ Newton =======
+struct NewtonWork {
+  double *g, *d, *xt, *scal;
+  float4 *u;
+  float *values;
+};
+
+static int newton_work(bartels_mesh_plan plan, NewtonWork &w) {
+  const size_t n = 3 * (size_t)plan->nV;
+  BT_CHECK(plan->w_vec.ensure(sizeof(double) * (3 * n + 16)));
+  BT_CHECK(plan->w_u.ensure(sizeof(float4) * (size_t)plan->nV));
+  BT_CHECK(plan->w_values.ensure(sizeof(float) * 9 * (size_t)plan->nnzb));
+  double *b = plan->w_vec.as<double>();
+  w.g = b;
+  w.d = b + n;
+  w.xt = b + 2 * n;
+  w.scal = b + 3 * n;
+  w.u = plan->w_u.as<float4>();
+  w.values = plan->w_values.as<float>();
+  return BARTELS_OK;
+}
+
+static ObjectiveDev objective_of(bartels_mesh_plan plan, const bartels_newton_params &p) {
+  ObjectiveDev o;
+  o.mass_coeff = p.mass_coeff;
+  o.scale = p.scale;
+  o.force_scale = p.force_scale;
+  o.q_base = plan->q_base;
+  o.x_hat = plan->x_hat;
+  o.f_ext = plan->f_ext;
+  o.pinned = plan->pinned;
+  return o;
+}
+
+static double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+static int read_scalar(bartels_ctx ctx, const double *d, double *h) {
+  BT_CUDA(cudaMemcpyAsync(ctx->host_scalars, d, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  BT_CUDA(cudaStreamSynchronize(ctx->stream));
+  *h = ctx->host_scalars[0];
+  return BARTELS_OK;
+}
+
+int newton_iterate(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params &p, double *x,
+                   double g0_norm, int *done, bartels_newton_report *rep) {
+  NewtonWork w;
+  BT_CHECK(newton_work(plan, w));
+  const int n = 3 * plan->nV;
+  const ObjectiveDev obj = objective_of(plan, p);
+  double t0 = now_s();
+  // gradient and convergence test (include/optimization_gradient_based.h:80-84)
+  BT_CHECK(gradient(ctx, plan, p.model, obj, x, w.g));
+  BT_CHECK(dot(ctx, w.g, w.g, n, w.scal));
+  double gg;
+  BT_CHECK(read_scalar(ctx, w.scal, &gg));
+  double t1 = now_s();
+  rep->t_gradient += t1 - t0;
+  const double gnorm = std::sqrt(gg);
+  rep->grad_norm = gnorm;
+  if (!std::isfinite(gnorm)) return fail(BARTELS_E_NONFINITE, "gradient is not finite (inverted element?)");
+  const bool conv = p.relative ? (gnorm <= p.gradient_tol * g0_norm) : (gg < p.gradient_tol * p.gradient_tol);
+  if (conv) {
+    *done = 1;
+    return BARTELS_OK;
+  }
+  *done = 0;
+  // Hessian H = mass_coeff M + scale^2 K (fused assembly, FP32)
+  BT_CHECK(launch_prep_u(ctx, plan, x, plan->q_base, p.scale, plan->dphi_matches_rest, w.u));
+  BT_CHECK(launch_hess(ctx, plan, p.model, p.psd_mode, w.u, plan->dphi_matches_rest ? 1 : 0,
+                       (float)(p.scale * p.scale), (float)p.mass_coeff, (float)p.psd_tol, p.dq2_flags, w.values));
+  BT_CUDA(cudaStreamSynchronize(ctx->stream));
+  double t2 = now_s();
+  rep->t_hessian += t2 - t1;
+  // search direction d = -H^-1 g (src/search_direction_newton_sparse.cpp:12-24)
+  BT_LAUNCH(ctx, k_scale_copy, grid_vec(ctx, n), 256, 0, n, -1.0, w.g, w.xt);
+  BT_CUDA(cudaMemsetAsync(w.d, 0, sizeof(double) * n, ctx->stream));
+  PcgOperator op;
+  op.plan = plan;
+  op.values = w.values;
+  op.pinned = plan->pinned;
+  bartels_pcg_report pr;
+  int s = pcg_solve(ctx, op, n, w.xt, w.d, plan->w_pcg, p.pcg, &pr);
+  rep->pcg_iterations += pr.iterations;
+  double t3 = now_s();
+  rep->t_pcg += t3 - t2;
+  if (s != BARTELS_OK && s != BARTELS_E_NOT_CONVERGED) return s;
+  // line search (src/linesearch_backtracking_bisection.cpp:17-30)
+  double gd, f0;
+  BT_CHECK(dot(ctx, w.g, w.d, n, w.scal));
+  BT_CHECK(read_scalar(ctx, w.scal, &gd));
+  BT_CHECK(energy(ctx, plan, p.model, obj, x, w.scal));
+  BT_CHECK(read_scalar(ctx, w.scal, &f0));
+  double alpha = p.ls_alpha;
+  int it = 0;
+  for (;;) {
+    BT_LAUNCH(ctx, k_axpy_to, grid_vec(ctx, n), 256, 0, n, x, alpha, w.d, w.xt);
+    double ft;
+    BT_CHECK(energy(ctx, plan, p.model, obj, w.xt, w.scal));
+    BT_CHECK(read_scalar(ctx, w.scal, &ft));
+    if (!(ft > f0 + p.ls_c * gd && it < p.max_iterations_ls)) {
+      if (!(ft > f0 + p.ls_c * gd)) rep->energy = ft;
+      break;
+    }
+    alpha *= p.ls_p;
+    it++;
+  }
+  if (it == p.max_iterations_ls) rep->ls_failures++;
+  BT_CUDA(cudaMemcpyAsync(x, w.xt, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+  rep->ls_iterations += it;
+  BT_CUDA(cudaStreamSynchronize(ctx->stream));
+  rep->t_linesearch += now_s() - t3;
+  rep->iterations += 1;
+  return BARTELS_OK;
+}
+
+int newton_solve(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params &p, double *x,
+                 bartels_newton_report *rep) {
+  const double t0 = now_s();
+  NewtonWork w;
+  BT_CHECK(newton_work(plan, w));
+  const int n = 3 * plan->nV;
+  const ObjectiveDev obj = objective_of(plan, p);
+  // reference gradient norm for the relative test
+  BT_CHECK(gradient(ctx, plan, p.model, obj, x, w.g));
+  BT_CHECK(dot(ctx, w.g, w.g, n, w.scal));
+  double gg;
+  BT_CHECK(read_scalar(ctx, w.scal, &gg));
+  rep->grad_norm0 = std::sqrt(gg);
+  rep->status = BARTELS_MAX_ITERATIONS_REACHED;
+  int count = 0;
+  do {
+    int done = 0;
+    BT_CHECK(newton_iterate(ctx, plan, p, x, rep->grad_norm0, &done, rep));
+    if (done) {
+      rep->status = BARTELS_CONVERGED;
+      break;
+    }
+    count++;
+  } while (count <= p.max_iterations);
+  double f;
+  BT_CHECK(energy(ctx, plan, p.model, obj, x, w.scal));
+  BT_CHECK(read_scalar(ctx, w.scal, &f));
+  rep->energy = f;
+  rep->seconds = now_s() - t0;
+  return BARTELS_OK;
+}
+
+__global__ void k_advance_ie(int n, double dt, const double *__restrict__ v, double *__restrict__ q_base,
+                             double *__restrict__ x_hat) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    q_base[i] += dt * v[i];
+    x_hat[i] = v[i];
+  }
+}
+
+int advance_implicit_euler(bartels_ctx ctx, bartels_mesh_plan plan, double dt, const double *v) {
+  const int n = 3 * plan->nV;
+  if (!plan->q_base) {
+    BT_CUDA(cudaMalloc(&plan->q_base, sizeof(double) * n));
+    BT_CUDA(cudaMemsetAsync(plan->q_base, 0, sizeof(double) * n, ctx->stream));
+  }
+  if (!plan->x_hat) BT_CUDA(cudaMalloc(&plan->x_hat, sizeof(double) * n));
+  BT_LAUNCH(ctx, k_advance_ie, grid_vec(ctx, n), 256, 0, n, dt, v, plan->q_base, plan->x_hat);
+  return BARTELS_OK;
+}
+
+int plan_spmv(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const float *x, float *y) {
+  BT_LAUNCH(ctx, k_spmv_blk<false>, grid_spmv(ctx, plan->nV), 256, 0, plan->nV, plan->brp, plan->bcol, values, x, y,
+            plan->pinned, (double *)nullptr, (const PcgState *)nullptr);
+  return BARTELS_OK;
+}
+
+// generic CSR solve for the drop-in search direction
+int csr_search_direction(bartels_ctx ctx, int n, const int *rp, const int *ci, const double *vals, const double *g,
+                         double *d, const bartels_pcg_params &prm, bartels_pcg_report *rep) {
+  const int64_t nnz = (n > 0) ? rp[n] : 0;
+  size_t bytes_rp = sizeof(int) * (n + 1), bytes_ci = sizeof(int) * nnz, bytes_v64 = sizeof(double) * nnz;
+  BT_CHECK(ctx->stage_a.ensure(bytes_rp + bytes_ci + 512));
+  BT_CHECK(ctx->stage_b.ensure(bytes_v64 + sizeof(float) * nnz + 512));
+  BT_CHECK(ctx->stage_c.ensure(sizeof(double) * 2 * (size_t)n + 512));
+  int *drp = ctx->stage_a.as<int>();
+  int *dci = drp + ((n + 1 + 63) & ~63);
+  double *dv64 = ctx->stage_b.as<double>();
+  float *dv32 = reinterpret_cast<float *>(dv64 + ((nnz + 63) & ~63ll));
+  double *db = ctx->stage_c.as<double>();
+  double *dx = db + ((n + 63) & ~63);
+  BT_CUDA(cudaMemcpyAsync(drp, rp, bytes_rp, cudaMemcpyHostToDevice, ctx->stream));
+  BT_CUDA(cudaMemcpyAsync(dci, ci, bytes_ci, cudaMemcpyHostToDevice, ctx->stream));
+  BT_CUDA(cudaMemcpyAsync(dv64, vals, bytes_v64, cudaMemcpyHostToDevice, ctx->stream));
+  BT_CUDA(cudaMemcpyAsync(dx, g, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+  BT_LAUNCH(ctx, k_f64_to_f32, grid_vec(ctx, nnz), 256, 0, nnz, dv64, dv32);
+  BT_LAUNCH(ctx, k_scale_copy, grid_vec(ctx, n), 256, 0, n, -1.0, dx, db);
+  BT_CUDA(cudaMemsetAsync(dx, 0, sizeof(double) * n, ctx->stream));
+  PcgOperator op;
+  op.n = n;
+  op.rp = drp;
+  op.ci = dci;
+  op.values = dv32;
+  int s = pcg_solve(ctx, op, n, db, dx, ctx->stage_d, prm, rep);
+  BT_CUDA(cudaMemcpyAsync(d, dx, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+  BT_CUDA(cudaStreamSynchronize(ctx->stream));
+  return s;
+}
+
+}  // namespace bartels

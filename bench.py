@@ -1,0 +1,313 @@
+"""Newton iterations per second on the n=96 Neo-Hookean Kuhn cube (5,308,416 tets).
+
+Workload (one "step" = one Newton iteration): implicit Euler in velocity form
+(dt = 0.01) from rest under gravity, z = 0 face pinned, Neo-Hookean E = 2e6 Pa,
+nu = 0.45, rho = 1000, Hessians PSD-projected (simple_psd_fix, tol 1e-6), each
+Newton system solved by block-Jacobi PCG to 1e-8 relative residual (FP32 PCG,
+FP64 residual refinement), Newton to 1e-8 relative gradient norm; when a time
+step converges the next one starts. Synthetic, seeded inputs (no dataset).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line. Under torchrun (N > 1) every rank runs an independent
+replica on its own GPU (the path does not shard: replicas only) and rank 0
+reports the max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Newton iters/s (5.3M-tet NH): learned-PCG vs Jacobi-PCG, same GB300, 1e-8 res"
+UNIT = "Newton iters/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=6)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=96)
+    ap.add_argument("--model", default="neohookean")
+    ap.add_argument("--no-psd", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ setup ---
+def build_problem(n, model, seed=0):
+    from bartels_gb300.meshes import kuhn_cube, material_params
+    V, E = kuhn_cube(n)
+    rho, young, nu, dt = 1000.0, 2e6, 0.45, 0.01
+    params = material_params(model, len(E), young, nu)
+    pinned = np.zeros(len(V), np.uint8)
+    pinned[np.abs(V[:, 2] - V[:, 2].min()) <= 1e-9] = 1
+    return dict(V=V, E=E, rho=rho, dt=dt, params=params, pinned=pinned,
+                gravity=np.array([0.0, 0.0, -9.81]))
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = max(mx, float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------ GPU arm ---------
+def run_gpu(args, rank, world):
+    import torch
+    import bartels_gb300 as bg
+    from bartels_gb300 import _lib
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    L = bg.lib()
+    ctx = bg.Context(dev)
+    stream = torch.cuda.ExternalStream(int(L.bartels_ctx_stream(ctx.handle)), device=f"cuda:{dev}")
+    pb = build_problem(args.n, args.model)
+    V, E = pb["V"], pb["E"]
+    nV, nT = len(V), len(E)
+    t0 = time.time()
+    plan = bg.MeshPlan(V, E, ctx)
+    t_plan = time.time() - t0
+    density = np.full(nT, pb["rho"])
+    plan.set_element_data(params=pb["params"], density=density)
+    f_g = plan.const_ext_force(None, pb["rho"] * pb["gravity"])
+    qt = V.ravel().copy()
+    vt = np.zeros(3 * nV)
+    plan.set_problem(q_base=qt, x_hat=vt, f_ext=f_g, pinned=pb["pinned"])
+    psd = _lib.PSD_NONE if args.no_psd else _lib.PSD_SIMPLE_FIX
+    prm = bg.newton_params(model=args.model, psd_mode=psd, psd_tol=1e-6, gradient_tol=1e-8, relative=1,
+                           mass_coeff=1.0, scale=pb["dt"], force_scale=pb["dt"], max_iterations=100)
+    x = torch.zeros(3 * nV, dtype=torch.float64, device=f"cuda:{dev}")
+    xp = C.c_void_p(x.data_ptr())
+    state = {"g0": -1.0, "steps": 0}
+    rep = _lib.NewtonReport()
+
+    def newton_step():
+        """Run until one Newton iteration (Hessian + PCG + line search) completed."""
+        while True:
+            done = C.c_int()
+            _lib.check(L.bartels_newton_iterate_d(ctx.handle, plan.handle, C.byref(prm), xp, state["g0"],
+                                                  C.byref(done), C.byref(rep)), "newton_iterate")
+            if state["g0"] < 0:
+                state["g0"] = rep.grad_norm
+            if done.value:
+                # converged time step: q_t += dt v, v_t = v; next step starts from v
+                _lib.check(L.bartels_newton_advance_implicit_euler_d(ctx.handle, plan.handle, pb["dt"], xp),
+                           "advance")
+                state["g0"] = -1.0
+                state["steps"] += 1
+                continue
+            return
+
+    for _ in range(args.warmup):
+        newton_step()
+    ctx.synchronize()
+    rep_before = (rep.iterations, rep.pcg_iterations, rep.ls_iterations)
+    launches0 = ctx.kernel_launches
+    if world > 1:
+        torch.distributed.barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(dev) as clk:
+        ctx.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            newton_step()
+        ev1.record(stream)
+        ctx.synchronize()
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    launches = ctx.kernel_launches - launches0
+    if world > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device=f"cuda:{dev}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    pcg_its = rep.pcg_iterations - rep_before[1]
+    newton_its = rep.iterations - rep_before[0]
+
+    # --- roofline of the dominant kernel (PCG SpMV) and the dq2 assembly, live
+    n_dof = 3 * nV
+    xs = torch.randn(n_dof, dtype=torch.float32, device=f"cuda:{dev}")
+    ys = torch.empty_like(xs)
+    nnz = plan.nnz
+    nnzb = nnz // 9
+
+    def time_launch(fn, reps):
+        for _ in range(2):
+            fn()
+        ctx.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            fn()
+        b.record(stream)
+        ctx.synchronize()
+        return a.elapsed_time(b) / reps * 1e-3
+
+    spmv_s = time_launch(lambda: _lib.check(L.bartels_plan_spmv_d(ctx.handle, plan.handle, None,
+                                                                  C.c_void_p(xs.data_ptr()),
+                                                                  C.c_void_p(ys.data_ptr())), "spmv"), 30)
+    spmv_bytes = 4 * nnz + 4 * nnzb + 4 * (nV + 1) + 12 * nV + 12 * nV
+    qd = torch.from_numpy(V.ravel().copy()).to(f"cuda:{dev}")
+    model_id = bg.api.MODELS[args.model]
+    hess_s = time_launch(lambda: _lib.check(L.bartels_plan_hessian_d(ctx.handle, plan.handle, model_id, psd, 1e-6, 0,
+                                                                     1.0, 0.0, C.c_void_p(qd.data_ptr()), None),
+                                            "hess"), 5)
+    # compulsory bytes of the fused dq2 stage: per-tet record (64 B) + vertex input
+    # (16 B) + CSR values written (4 B each) + incidence map (8 B per incidence)
+    hess_bytes = 64 * nT + 16 * nV + 4 * nnz + 8 * 4 * nT
+    peak, peak_kind = peaks()
+    spmv_gbs = spmv_bytes / spmv_s / 1e9
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "spmv_traffic.json")) as f:
+            tj = json.load(f)
+        if tj.get("n") == args.n:
+            traffic = tj["dram_bytes_per_launch"]
+    except Exception:
+        pass
+
+    # --- end to end through the host-buffer public API (one implicit-Euler step per e2e step)
+    e2e = None
+    if rank == 0 and args.e2e_steps > 0:
+        plan.set_problem(q_base=qt, x_hat=vt, f_ext=f_g, pinned=pb["pinned"])
+        v_host = np.zeros(3 * nV)
+        its = 0
+        t = 0.0
+        h2d = d2h = 0
+        for _ in range(args.e2e_steps):
+            t1 = time.perf_counter()
+            v_out, r = plan.newton_solve(v_host, prm)
+            t += time.perf_counter() - t1
+            its += r.iterations
+            h2d += v_host.nbytes
+            d2h += v_out.nbytes
+        e2e = {"value": its / t if t > 0 else None, "unit": UNIT,
+               "h2d_bytes_per_step": h2d // args.e2e_steps, "d2h_bytes_per_step": d2h // args.e2e_steps,
+               "newton_iterations": its, "seconds": t}
+
+    out = {
+        "metric": METRIC, "value": newton_its * world / (ms * 1e-3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / max(newton_its, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic (seeded Kuhn cube, gravity)",
+        "config": {"workload": f"implicit-Euler Newton, Neo-Hookean Kuhn cube n={args.n} "
+                               f"({nV} vertices, {nT} tets), dt=0.01, z=0 pinned, PSD "
+                               f"{'off' if args.no_psd else 'simple_psd_fix 1e-6'}, block-Jacobi PCG 1e-8, "
+                               "Newton 1e-8 relative", "preconditioner": "block-Jacobi",
+                   "learned_pcg": "not built", "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (CSR values %.0f MB)" % (4 * nnz / 1e6)},
+        "newton_iterations": newton_its, "pcg_iterations": pcg_its,
+        "pcg_iters_per_newton": pcg_its / max(newton_its, 1),
+        "roofline": {"bound": "hbm", "achieved": spmv_gbs, "peak": peak, "unit": "GB/s",
+                     "frac": spmv_gbs / peak, "traffic": traffic, "kernel": "k_spmv_blk (PCG SpMV, FP32 BCSR3)",
+                     "bytes_per_launch": spmv_bytes, "us_per_launch": spmv_s * 1e6, "peak_source": peak_kind},
+        "kernels": {"dq2_fused_assembly": {"us_per_launch": hess_s * 1e6, "compulsory_bytes": hess_bytes,
+                                           "achieved_gbs": hess_bytes / hess_s / 1e9,
+                                           "frac": hess_bytes / hess_s / 1e9 / peak}},
+        "clocks": clk.summary(), "gpu_launches": int(launches), "e2e": e2e,
+        "setup_s": {"plan": t_plan}, "time_steps_completed": state["steps"],
+        "stage_seconds": {"gradient": rep.t_gradient, "hessian": rep.t_hessian, "pcg": rep.t_pcg,
+                          "linesearch": rep.t_linesearch},
+    }
+    return out
+
+
+# --------------------------------------------------------- reference arm ---
+def run_reference(args):
+    return {"impl": "reference", "metric": METRIC, "unit": UNIT, "higher_is_better": True,
+            "unavailable": "CPU reference arm not wired yet"}
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)))
+        return
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    out = run_gpu(args, rank, world)
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,297 @@
+/* bartels_gpu.h -- C ABI of the GB300 (sm_103a) implementation of the
+ * tet-mesh hyperelastic path of dilevin/Bartels.
+ *
+ * Plain C: pointers and sizes only, no C++ or torch types. Every function
+ * returns an int status (BARTELS_OK = 0). Nothing calls exit(); a failed call
+ * leaves its outputs unspecified and bartels_last_error() describes it.
+ *
+ * Conventions (the reference's, see the Bartels sources cited per function):
+ *   V       nV x 3 double, column-major (all x, then y, then z)
+ *   E       nT x 4 int, column-major, 0-based
+ *   q, g    3 nV double, interleaved [x0 y0 z0 x1 ...]
+ *   dphidX  nT x 12 double, column-major; row t = column-major flatten of the
+ *           4x3 matrix of shape-function gradients of tet t
+ *   volume  nT double
+ *   params  nT x 2 double, column-major; Neo-Hookean (C, D) = (mu/2, lambda/2),
+ *           StVK and corotational (lambda, mu)
+ *   sparse  CSR of the symmetric 3nV x 3nV matrix. Its pattern is the full 3x3
+ *           block pattern of the mesh graph (every vertex pair sharing a tet, the
+ *           vertex itself included), which is exactly the pattern that the
+ *           reference's sim::assemble produces (explicit zeros kept). Because the
+ *           pattern is symmetric the CSR arrays are also the reference's CSC.
+ *
+ * Host-pointer entry points copy inputs to the GPU, compute on the context's
+ * stream and copy results back before returning. The *_d variants take device
+ * pointers and only enqueue work on the context's stream.
+ */
+#ifndef BARTELS_GPU_H
+#define BARTELS_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status --- */
+enum {
+  BARTELS_OK = 0,
+  BARTELS_E_INVALID_ARG = 1,
+  BARTELS_E_NONFINITE = 2,     /* an element produced NaN/Inf (e.g. J <= 0 for Neo-Hookean) */
+  BARTELS_E_NOT_CONVERGED = 3, /* PCG or Newton hit its iteration cap */
+  BARTELS_E_DEVICE = 4,        /* CUDA error */
+  BARTELS_E_TIMEOUT = 5,
+  BARTELS_E_UNSUPPORTED = 6,   /* mesh outside the kernels' limits (e.g. > 255 neighbours) */
+  BARTELS_E_NO_DEVICE = 7
+};
+
+/* Exit status of line search / Newton, include/BartelsTypes.h:6-9. */
+enum { BARTELS_CONVERGED = 0, BARTELS_MAX_ITERATIONS_REACHED = 1 };
+
+/* Material laws. NEOHOOKEAN is src/psi_neohookean_F.cpp:31 (C (I1-3-2 ln J) +
+ * D (J-1)^2). NEOHOOKEAN_ISOCHORIC is the reference's earlier law kept as
+ * commented-out code in src/psi_neohookean_F.cpp:8-14 (C (J^-2/3 I1 - 3) +
+ * D (J-1)^2); data/matrices/H_neohookean_coarser_bunny.txt was made with it. */
+enum {
+  BARTELS_NEOHOOKEAN = 0,
+  BARTELS_STVK = 1,
+  BARTELS_COROTATIONAL = 2,
+  BARTELS_NEOHOOKEAN_ISOCHORIC = 3
+};
+
+/* Element-matrix callback replacement (src/linear_tetmesh_neohookean_dq2.cpp:22):
+ * a host functor cannot run on the GPU, so the one callback the reference uses,
+ * simple_psd_fix (src/simple_psd_fix.cpp:5-21), is selected by flag. */
+enum { BARTELS_PSD_NONE = 0, BARTELS_PSD_SIMPLE_FIX = 1 };
+
+/* Flags for the dq2 entry points. */
+enum {
+  /* corotational only: use the exact Hessian instead of the reference's layout.
+   * The reference (src/d2psi_stretch_dF2.cpp:37-45) fills d2psi/dF2 in row-major
+   * F order while B is column-major, so its matrix is the Hessian at F^T; that
+   * is the default here, for drop-in parity. */
+  BARTELS_DQ2_COROT_EXACT = 1
+};
+
+typedef struct bartels_ctx_s *bartels_ctx;
+typedef struct bartels_mesh_plan_s *bartels_mesh_plan;
+
+const char *bartels_status_string(int status);
+/* Text of the last error raised on the calling thread ("" if none). */
+const char *bartels_last_error(void);
+
+/* ---------------------------------------------------------------- context -- */
+/* One context per host thread: a device, a stream, workspace and a pinned
+ * staging area. All work is ordered on the context's stream. */
+int bartels_ctx_create(int device, bartels_ctx *out);
+int bartels_ctx_destroy(bartels_ctx ctx);
+int bartels_ctx_synchronize(bartels_ctx ctx);
+/* The context's cudaStream_t, as void*. */
+void *bartels_ctx_stream(bartels_ctx ctx);
+/* Number of kernels this library enqueued on ctx since creation. */
+int64_t bartels_ctx_kernel_launches(bartels_ctx ctx);
+
+/* ------------------------------------------------------------- kinematics -- */
+/* linear_tetmesh_dphi_dX, src/linear_tetmesh_dphi_dX.cpp:5-18 (per tet:
+ * src/linear_tet_dphi_dX.cpp:10-16). dphidX: nT x 12 column-major. */
+int bartels_tetmesh_dphi_dX(bartels_ctx ctx, int nV, const double *V, int nT, const int *E, double *dphidX);
+/* Signed tet volumes det[X1-X0, X2-X0, X3-X0]/6 (the reference's callers use
+ * igl::volume, tests/test_constitutive_model.cpp:28). */
+int bartels_tetmesh_volume(bartels_ctx ctx, int nV, const double *V, int nT, const int *E, double *vol);
+
+/* ------------------------------------------------------------------ plan --- */
+/* A mesh plan is built once from (V, E): rest data, per-tet records, the
+ * vertex->tet incidence lists in tet order, the block CSR pattern and the
+ * element->CSR scatter positions. Plans are immutable after creation apart from
+ * the element data set with bartels_plan_set_element_data. */
+int bartels_plan_create(bartels_ctx ctx, int nV, const double *V, int nT, const int *E, bartels_mesh_plan *out);
+int bartels_plan_destroy(bartels_mesh_plan plan);
+/* Upload per-tet element data (host pointers; any may be NULL to keep the
+ * plan's current values). Defaults after plan creation: dphidX and volume
+ * computed from V, params = 0, density = 0. */
+int bartels_plan_set_element_data(bartels_mesh_plan plan, const double *dphidX, const double *vol,
+                                  const double *params, const double *density);
+/* Scalar CSR size of the 3nV x 3nV pattern. */
+int bartels_plan_csr_size(bartels_mesh_plan plan, int *n, int64_t *nnz);
+/* Host copy of the CSR pattern: row_ptr (n+1), col_idx (nnz). */
+int bartels_plan_csr_pattern(bartels_mesh_plan plan, int *row_ptr, int *col_idx);
+
+/* ------------------------------------------------------ energy / gradient -- */
+/* linear_tetmesh_{neohookean,stvk,corotational}_q, e.g.
+ * src/linear_tetmesh_neohookean_q.cpp:10-24: sum over tets of psi(F) vol.
+ * dphidX/vol/params may be NULL to use the plan's element data; otherwise they
+ * are uploaded first (as bartels_plan_set_element_data). FP64 element math,
+ * deterministic FP64 reduction. */
+int bartels_tetmesh_q(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q, const double *dphidX,
+                      const double *vol, const double *params, double *energy);
+/* linear_tetmesh_{model}_dq, e.g. src/linear_tetmesh_neohookean_dq.cpp:5-22:
+ * assembled gradient g (3 nV). FP64 element math, per-vertex sums in tet order. */
+int bartels_tetmesh_dq(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q, const double *dphidX,
+                       const double *vol, const double *params, double *g);
+/* linear_tetmesh_{model}_dq2, e.g. src/linear_tetmesh_neohookean_dq2.cpp:8-28:
+ * assembled Hessian values in the plan's CSR order (nnz doubles). FP32 element
+ * math; each entry summed over its tets in tet order (the order in which the
+ * reference's setFromTriplets sums duplicates). psd_mode/psd_tol replace the
+ * element callback; flags: BARTELS_DQ2_*. */
+int bartels_tetmesh_dq2(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q, const double *dphidX,
+                        const double *vol, const double *params, int psd_mode, double psd_tol, int flags,
+                        double *csr_values);
+
+/* Named drop-ins (same as the generic calls with the model fixed). */
+int bartels_tetmesh_neohookean_q(bartels_ctx, bartels_mesh_plan, const double *q, const double *dphidX,
+                                 const double *vol, const double *params, double *energy);
+int bartels_tetmesh_neohookean_dq(bartels_ctx, bartels_mesh_plan, const double *q, const double *dphidX,
+                                  const double *vol, const double *params, double *g);
+int bartels_tetmesh_neohookean_dq2(bartels_ctx, bartels_mesh_plan, const double *q, const double *dphidX,
+                                   const double *vol, const double *params, int psd_mode, double psd_tol,
+                                   double *csr_values);
+int bartels_tetmesh_stvk_q(bartels_ctx, bartels_mesh_plan, const double *q, const double *dphidX,
+                           const double *vol, const double *params, double *energy);
+int bartels_tetmesh_stvk_dq(bartels_ctx, bartels_mesh_plan, const double *q, const double *dphidX,
+                            const double *vol, const double *params, double *g);
+int bartels_tetmesh_stvk_dq2(bartels_ctx, bartels_mesh_plan, const double *q, const double *dphidX,
+                             const double *vol, const double *params, int psd_mode, double psd_tol,
+                             double *csr_values);
+int bartels_tetmesh_corotational_q(bartels_ctx, bartels_mesh_plan, const double *q, const double *dphidX,
+                                   const double *vol, const double *params, double *energy);
+int bartels_tetmesh_corotational_dq(bartels_ctx, bartels_mesh_plan, const double *q, const double *dphidX,
+                                    const double *vol, const double *params, double *g);
+int bartels_tetmesh_corotational_dq2(bartels_ctx, bartels_mesh_plan, const double *q, const double *dphidX,
+                                     const double *vol, const double *params, int psd_mode, double psd_tol,
+                                     double *csr_values);
+
+/* --------------------------------------------------- mass, loads, bounds --- */
+/* linear_tetmesh_mass_matrix, src/linear_tetmesh_mass_matrix.cpp:7-24 (per tet
+ * src/linear_tet_mass_matrix.cpp:12-42): values in the plan's CSR order. */
+int bartels_tetmesh_mass_matrix(bartels_ctx ctx, bartels_mesh_plan plan, const double *density, const double *vol,
+                                double *csr_values);
+/* linear_tetmesh_const_ext_force, src/linear_tetmesh_const_ext_force.cpp:5-18:
+ * f_v = sum over tets of v of vol/4 * traction. */
+int bartels_tetmesh_const_ext_force(bartels_ctx ctx, bartels_mesh_plan plan, const double *vol,
+                                    const double traction[3], double *f);
+/* fixed_point_constraint_matrix, src/fixed_point_constraint_matrix.cpp:7-38.
+ * fixed (sorted ascending, as the reference requires). Rows = dim*(nV-nfix),
+ * cols = dim*nV, one 1 per row: row_ptr (rows+1), col_idx (rows), values all 1.
+ * Host-side (integer bookkeeping only). Pass row_ptr = NULL to query rows. */
+int bartels_fixed_point_constraint_matrix(int nV, int dim, const int *fixed, int nfix, int *rows, int *row_ptr,
+                                          int *col_idx, double *values);
+/* find_min_vertices, src/find_min_vertices.cpp:5-21: indices of vertices whose
+ * coordinate dim is within tol of the minimum. Returns count in *count. */
+int bartels_find_min_vertices(int nV, const double *V, int dim, double tol, int *indices, int *count);
+
+/* ------------------------------------------------------------ linear solve -- */
+typedef struct {
+  double rel_tol;       /* relative residual target ||b - A x|| / ||b|| (default 1e-8) */
+  int max_iters;        /* total PCG iterations cap (default 20000) */
+  double inner_rel_tol; /* FP32 inner PCG tolerance per refinement pass (default 1e-4) */
+  int max_refinements;  /* FP64 residual refinement passes (default 8) */
+} bartels_pcg_params;
+
+typedef struct {
+  int iterations;      /* total PCG iterations */
+  int refinements;     /* FP64 refinement passes used */
+  double rel_residual; /* final ||b - A x|| / ||b|| in FP64 */
+  int converged;
+} bartels_pcg_report;
+
+void bartels_pcg_default_params(bartels_pcg_params *p);
+
+/* search_direction_newton_sparse, src/search_direction_newton_sparse.cpp:5-26:
+ * d = -H^{-1} g for an SPD H given as CSR (host arrays, nnz values double).
+ * Replaces the reference's Eigen::SparseLU with block-Jacobi PCG (FP32 with
+ * FP64 residual refinement). n must be a multiple of 3 for the 3x3 block
+ * preconditioner (falls back to scalar Jacobi otherwise). Returns
+ * BARTELS_E_NOT_CONVERGED where the reference's solver.info() != Success. */
+int bartels_search_direction_newton_sparse(bartels_ctx ctx, int n, const int *row_ptr, const int *col_idx,
+                                           const double *values, const double *g, double *d,
+                                           const bartels_pcg_params *params, bartels_pcg_report *report);
+
+/* ------------------------------------------------------------- line search -- */
+/* linesearch_backtracking_bisection, src/linesearch_backtracking_bisection.cpp:5-31,
+ * for a host objective: while f(x + alpha d) > f(x) + c g.d and it < max_it:
+ * alpha *= p. Then x += alpha d. *status = BARTELS_CONVERGED or
+ * BARTELS_MAX_ITERATIONS_REACHED, exactly as the reference. The vector update
+ * and dot product run on the host arrays given (this entry point exists for
+ * callers with their own host objective; the GPU Newton solver below runs its
+ * line search on the device). */
+typedef double (*bartels_objective_fn)(const double *x, int n, void *user);
+int bartels_linesearch_backtracking_bisection(int n, double *x, const double *d, bartels_objective_fn f,
+                                              void *user, const double *g, int max_iterations, double alpha,
+                                              double c, double p, int *status, double *alpha_out);
+
+/* ------------------------------------------------------------------ Newton -- */
+/* Objective minimised by bartels_newton_solve over the unknown x (3 nV):
+ *   q(x)  = q_base + scale * x
+ *   f(x)  = mass_coeff * (1/2 x^T M x - x^T M x_hat) + Psi(q(x)) - force_scale * x^T f_ext
+ * restricted to the free vertices (pinned vertices keep x = 0).
+ * Quasi-static (config: Newton under gravity): mass_coeff 0, scale 1, q_base 0.
+ * Implicit Euler in velocity form (matlab/examples/implicit_integration.m:69-83):
+ *   x = v, q_base = q_t, scale = dt, x_hat = v_t, force_scale = dt, mass_coeff 1.
+ * M is the consistent mass matrix of the plan's density. */
+typedef struct {
+  int model;
+  int psd_mode;          /* BARTELS_PSD_* for the Hessian */
+  double psd_tol;
+  int dq2_flags;
+  double mass_coeff;
+  double scale;
+  double force_scale;
+  /* Newton (include/optimization_gradient_based.h:51-56 defaults) */
+  double gradient_tol;   /* absolute tol (reference) when relative == 0, else relative */
+  int relative;          /* 1: stop when ||g|| <= gradient_tol * ||g_0|| */
+  int max_iterations;    /* reference: loop runs while iteration_count <= max_iterations */
+  int max_iterations_ls;
+  double ls_alpha, ls_c, ls_p;
+  bartels_pcg_params pcg;
+} bartels_newton_params;
+
+typedef struct {
+  int status;            /* BARTELS_CONVERGED / BARTELS_MAX_ITERATIONS_REACHED */
+  int iterations;        /* Newton iterations taken */
+  int pcg_iterations;    /* total PCG iterations */
+  int ls_iterations;     /* total line-search backtracks */
+  int ls_failures;       /* line searches that hit max_iterations_ls */
+  double grad_norm0, grad_norm;
+  double energy;
+  double seconds;        /* wall time of the solve (device-synchronised) */
+  double t_gradient, t_hessian, t_pcg, t_linesearch; /* seconds per stage, summed */
+} bartels_newton_report;
+
+void bartels_newton_default_params(bartels_newton_params *p);
+
+/* Problem data for a Newton solve on a plan (host pointers; may be NULL):
+ * q_base (3nV), x_hat (3nV), f_ext (3nV), pinned (nV bytes, 1 = vertex fixed). */
+int bartels_newton_set_problem(bartels_mesh_plan plan, const double *q_base, const double *x_hat,
+                               const double *f_ext, const unsigned char *pinned);
+/* Solve from x (host, 3nV, in/out). Host buffers, copies counted in the time. */
+int bartels_newton_solve(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params *params,
+                         double *x, bartels_newton_report *report);
+/* Device-resident variant: x_d is a device pointer (3nV doubles). */
+int bartels_newton_solve_d(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params *params,
+                           double *x_d, bartels_newton_report *report);
+/* One Newton iteration (gradient, Hessian, PCG, line search) on device x_d;
+ * *done = 1 when the gradient test passed before the step. Used by benchmarks
+ * that time individual iterations. g0_norm: reference gradient norm for the
+ * relative test (<= 0 to compute it now). */
+int bartels_newton_iterate_d(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params *params,
+                             double *x_d, double g0_norm, int *done, bartels_newton_report *report);
+
+/* ------------------------------------------------- device-pointer variants -- */
+/* Hessian H = coeff_M M + coeff_K K(q) of the plan's element data into FP32
+ * values_d (9*nnzb floats, the plan's CSR order), q_d = 3nV positions on the
+ * device. values_d == NULL writes the plan's internal Hessian buffer (the one
+ * bartels_plan_spmv_d and the Newton solver use). Enqueued on ctx's stream. */
+int bartels_plan_hessian_d(bartels_ctx ctx, bartels_mesh_plan plan, int model, int psd_mode, double psd_tol,
+                           int flags, double coeff_K, double coeff_M, const double *q_d, float *values_d);
+/* y_d = H x_d (FP32, 3nV) with H in the plan's CSR order (values_d == NULL: the
+ * plan's internal Hessian buffer). Rows of pinned vertices give 0. */
+int bartels_plan_spmv_d(bartels_ctx ctx, bartels_mesh_plan plan, const float *values_d, const float *x_d,
+                        float *y_d);
+/* Implicit-Euler bookkeeping after a converged step in velocity form:
+ * q_base += dt * v, x_hat = v (device v_d, 3nV). */
+int bartels_newton_advance_implicit_euler_d(bartels_ctx ctx, bartels_mesh_plan plan, double dt, const double *v_d);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BARTELS_GPU_H */

@@ -1,0 +1,151 @@
+"""The element math the CUDA kernels use (bartels_gb300/csrc/devmath.cuh),
+compiled for the host, against the FP64 oracle: block laws assembled into the
+12x12 element Hessian, PSD projection (fast and slow paths), energies,
+stresses and the 3x3 SVD, in FP64 (tight) and FP32 (kernel precision)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import devmath
+
+D = C.POINTER(C.c_double)
+Fp = C.POINTER(C.c_float)
+MODEL_ID = {"neohookean": 0, "stvk": 1, "corotational": 2, "neohookean_isochoric": 3}
+PARAMS = {"neohookean": np.array([3.5e5, 1.2e6]), "neohookean_isochoric": np.array([3.5e5, 1.2e6]),
+          "stvk": np.array([2.4e6, 7e5]), "corotational": np.array([2.4e6, 7e5])}
+
+
+def dp(a):
+    return a.ctypes.data_as(D)
+
+
+def fp(a):
+    return a.ctypes.data_as(Fp)
+
+
+def random_tet(rng, amp):
+    X = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1.0]]) * 0.1 + 0.02 * rng.standard_normal((4, 3))
+    x = X @ (np.eye(3) + amp * rng.standard_normal((3, 3))).T + 0.001 * rng.standard_normal((4, 3))
+    return X, x
+
+
+def oracle_element(oracle, model, X, x, p, psd_tol, exact):
+    E = np.array([[0, 1, 2, 3]], np.int32)
+    dphi = oracle.dphi_dX(X, E)
+    vol = oracle.volume(X, E)
+    K = oracle.tetmesh_dq2_elements(model, E, x.ravel(), dphi, vol, p[None, :], psd_tol=psd_tol,
+                                    corot_layout_reference=not exact)[0]
+    return K, dphi[0], vol[0]
+
+
+def lib_element(model, x, dphi12, vol, p, psd_tol, exact, dtype):
+    L = devmath()
+    dphi9 = np.array([dphi12[a + 4 * d] for a in (1, 2, 3) for d in range(3)])
+    F = np.zeros(9)
+    xs = [np.ascontiguousarray(x[a]) for a in range(4)]
+    L.dm_def_grad_d(*[dp(v) for v in xs], dp(dphi9), 0, dp(F))
+    pv = vol * p
+    if dtype == np.float64:
+        out = np.zeros(144)
+        slow = L.dm_element_hessian_d(MODEL_ID[model], dp(F), dp(pv), dp(dphi9), int(exact), int(psd_tol is not None),
+                                      C.c_double(psd_tol or 0.0), dp(out))
+    else:
+        F32, pv32, d32 = (np.ascontiguousarray(a, np.float32) for a in (F, pv, dphi9))
+        out = np.zeros(144, np.float32)
+        slow = L.dm_element_hessian_f(MODEL_ID[model], fp(F32), fp(pv32), fp(d32), int(exact),
+                                      int(psd_tol is not None), C.c_float(psd_tol or 0.0), fp(out))
+    return out.reshape(12, 12).astype(np.float64), slow
+
+
+@pytest.mark.parametrize("model", list(MODEL_ID))
+@pytest.mark.parametrize("exact", [False, True])
+def test_element_hessian_fp64(oracle, model, exact):
+    if exact and model != "corotational":
+        pytest.skip("flag only affects the corotational law")
+    rng = np.random.default_rng(11)
+    for _ in range(20):
+        X, x = random_tet(rng, 0.2)
+        K_ref, dphi, vol = oracle_element(oracle, model, X, x, PARAMS[model], None, exact)
+        K, _ = lib_element(model, x, dphi, vol, PARAMS[model], None, exact, np.float64)
+        assert np.linalg.norm(K - K_ref) <= 1e-10 * np.linalg.norm(K_ref)
+
+
+@pytest.mark.parametrize("model", list(MODEL_ID))
+def test_element_hessian_psd_fp64(oracle, model):
+    rng = np.random.default_rng(12)
+    slow_seen = fast_seen = 0
+    for k in range(40):
+        X, x = random_tet(rng, 0.6 if k % 2 else 0.05)
+        for tol in (1e-6, 1e-3):
+            K_ref, dphi, vol = oracle_element(oracle, model, X, x, PARAMS[model], tol, False)
+            K, slow = lib_element(model, x, dphi, vol, PARAMS[model], tol, False, np.float64)
+            slow_seen += slow
+            fast_seen += 1 - slow
+            assert np.linalg.norm(K - K_ref) <= 1e-9 * np.linalg.norm(K_ref)
+    assert fast_seen > 0
+
+
+def test_psd_slow_path_is_exercised(oracle):
+    """Strongly compressed Neo-Hookean and StVK elements are indefinite."""
+    rng = np.random.default_rng(13)
+    seen = 0
+    for _ in range(40):
+        X, x = random_tet(rng, 0.0)
+        x = X @ np.diag([0.5, 1.2, 0.6]) + 0.02 * rng.standard_normal((4, 3))
+        for model in ("stvk", "neohookean"):
+            K_ref, dphi, vol = oracle_element(oracle, model, X, x, PARAMS[model], 1e-6, False)
+            K, slow = lib_element(model, x, dphi, vol, PARAMS[model], 1e-6, False, np.float64)
+            seen += slow
+            assert np.linalg.norm(K - K_ref) <= 1e-9 * np.linalg.norm(K_ref)
+    assert seen > 0
+
+
+@pytest.mark.parametrize("model", list(MODEL_ID))
+def test_element_hessian_fp32(oracle, model):
+    rng = np.random.default_rng(14)
+    for _ in range(20):
+        X, x = random_tet(rng, 0.2)
+        for tol in (None, 1e-6):
+            K_ref, dphi, vol = oracle_element(oracle, model, X, x, PARAMS[model], tol, False)
+            K, _ = lib_element(model, x, dphi, vol, PARAMS[model], tol, False, np.float32)
+            assert np.linalg.norm(K - K_ref) <= 2e-5 * np.linalg.norm(K_ref)
+
+
+@pytest.mark.parametrize("model", list(MODEL_ID))
+def test_energy_and_stress_fp64(oracle, model):
+    L = devmath()
+    rng = np.random.default_rng(15)
+    p = PARAMS[model]
+    for _ in range(30):
+        F = np.eye(3) + 0.2 * rng.standard_normal((3, 3))
+        if model.startswith("neo") and np.linalg.det(F) <= 0:
+            continue
+        fv = np.ascontiguousarray(F.ravel(order="F"))
+        e = L.dm_psi_d(MODEL_ID[model], dp(fv), dp(p))
+        e_ref = oracle.psi(model, F, p)
+        assert abs(e - e_ref) <= 1e-11 * max(abs(e_ref), 1.0)
+        P = np.zeros(9)
+        L.dm_pk1_d(MODEL_ID[model], dp(fv), dp(p), dp(P))
+        P_ref = oracle.dpsi(model, F, p)
+        assert np.linalg.norm(P - P_ref) <= 1e-11 * np.linalg.norm(P_ref)
+
+
+def test_svd3_float_and_double(oracle):
+    L = devmath()
+    rng = np.random.default_rng(16)
+    for k in range(100):
+        F = rng.standard_normal((3, 3)) if k % 3 == 0 else np.eye(3) + 0.3 * rng.standard_normal((3, 3))
+        U0, S0, V0 = oracle.svd3(F)
+        fv = np.ascontiguousarray(F.ravel(order="F"))
+        U, S, V = np.zeros(9), np.zeros(3), np.zeros(9)
+        L.dm_svd3_d(dp(fv), dp(U), dp(S), dp(V))
+        assert np.allclose(S, S0, rtol=1e-12, atol=1e-13)
+        Um, Vm = U.reshape(3, 3, order="F"), V.reshape(3, 3, order="F")
+        assert np.linalg.norm(Um @ np.diag(S) @ Vm.T - F) <= 1e-12 * np.linalg.norm(F)
+        f32 = fv.astype(np.float32)
+        U32, S32, V32 = np.zeros(9, np.float32), np.zeros(3, np.float32), np.zeros(9, np.float32)
+        L.dm_svd3_f(fp(f32), fp(U32), fp(S32), fp(V32))
+        assert np.allclose(S32, S0, rtol=2e-5, atol=2e-6 * np.abs(S0).max())
+        Um, Vm = U32.reshape(3, 3, order="F").astype(float), V32.reshape(3, 3, order="F").astype(float)
+        assert np.linalg.norm(Um @ np.diag(S32.astype(float)) @ Vm.T - F) <= 1e-5 * np.linalg.norm(F)
