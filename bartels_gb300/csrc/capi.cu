@@ -1,6 +1,7 @@
 // extern "C" entry points (include/bartels_gpu.h).
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -90,6 +91,10 @@ int bartels_ctx_create(int device, bartels_ctx *out) {
   BT_CUDA(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
   BT_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
   BT_CUDA(cudaMallocHost(&ctx->host_scalars, 64 * sizeof(double)));
+  if (const char *e = std::getenv("BARTELS_SPMV_LANES")) {
+    const int g = std::atoi(e);
+    if (g == 4 || g == 8 || g == 16) ctx->spmv_lanes = g;
+  }
   *out = ctx;
   return BARTELS_OK;
 }

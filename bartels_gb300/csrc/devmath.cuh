@@ -482,38 +482,51 @@ BT_HD void pk1_model(int model, const T *F, const T *pv, T *P) {
 // Fast test: min eig M >= tol  <=>  S - tol (G^-1 (x) I) is PSD, G = Phi^T Phi.
 // ----------------------------------------------------------------------------
 
-// 9x9 symmetric S from a block law: S[(k + 3 i) + 9 (l + 3 j)] = block(e_i, e_j)[k][l]
+// packed lower-triangular index of a symmetric 9x9 (i >= j)
+BT_HD constexpr int p9(int i, int j) { return i >= j ? i * (i + 1) / 2 + j : j * (j + 1) / 2 + i; }
+
+// 9x9 symmetric S from a block law, packed: S[(k + 3 i), (l + 3 j)] = block(e_i, e_j)[k][l]
 template <class Law, class T>
-BT_HD void law_matrix9(const Law &law, T *S) {
+BT_HD void law_matrix9p(const Law &law, T *S) {
+#pragma unroll
   for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) {
+#pragma unroll
+    for (int j = 0; j <= i; ++j) {
       T ei[3] = {T(0), T(0), T(0)}, ej[3] = {T(0), T(0), T(0)};
       ei[i] = T(1);
       ej[j] = T(1);
       T K[9];
       law.block(ei, ej, K);
+#pragma unroll
       for (int k = 0; k < 3; ++k)
-        for (int l = 0; l < 3; ++l) S[(k + 3 * i) + 9 * (l + 3 * j)] = K[3 * k + l];
+#pragma unroll
+        for (int l = 0; l < 3; ++l)
+          if ((k + 3 * i) >= (l + 3 * j)) S[p9(k + 3 * i, l + 3 * j)] = K[3 * k + l];
     }
 }
 
-// Cholesky test of the symmetric 9x9 A (overwritten); true if all pivots > 0.
+// Cholesky test of a packed symmetric 9x9 (overwritten); true if all pivots > 0.
 template <class T>
-BT_HD bool chol9_ok(T *A) {
+BT_HD bool chol9p_ok(T *A) {
+  bool ok = true;
+#pragma unroll
   for (int j = 0; j < 9; ++j) {
-    T d = A[j + 9 * j];
-    for (int k = 0; k < j; ++k) d -= A[j + 9 * k] * A[j + 9 * k];
-    if (!(d > T(0))) return false;
-    T s = bt_sqrt(d);
-    A[j + 9 * j] = s;
-    T inv = T(1) / s;
+    T d = A[p9(j, j)];
+#pragma unroll
+    for (int k = 0; k < j; ++k) d -= A[p9(j, k)] * A[p9(j, k)];
+    ok = ok && (d > T(0));
+    const T s = bt_sqrt(d > T(0) ? d : T(1));
+    A[p9(j, j)] = s;
+    const T inv = T(1) / s;
+#pragma unroll
     for (int i = j + 1; i < 9; ++i) {
-      T v = A[i + 9 * j];
-      for (int k = 0; k < j; ++k) v -= A[i + 9 * k] * A[j + 9 * k];
-      A[i + 9 * j] = v * inv;
+      T v = A[p9(i, j)];
+#pragma unroll
+      for (int k = 0; k < j; ++k) v -= A[p9(i, k)] * A[p9(j, k)];
+      A[p9(i, j)] = v * inv;
     }
   }
-  return true;
+  return ok;
 }
 
 // inverse of a symmetric 3x3 (column-major)
@@ -523,142 +536,193 @@ BT_HD void inv3(T *R, const T *A) {
   cof3(G, A);
   T J = A[0] * G[0] + A[1] * G[1] + A[2] * G[2];
   T inv = T(1) / J;
+#pragma unroll
   for (int i = 0; i < 3; ++i)
+#pragma unroll
     for (int j = 0; j < 3; ++j) R[i + 3 * j] = G[j + 3 * i] * inv;
 }
 
 // phi: 4 gradients (phi[a][d]). G = Phi^T Phi.
 template <class T>
 BT_HD void gram3(T *G, const T (*phi)[3]) {
+#pragma unroll
   for (int i = 0; i < 3; ++i)
+#pragma unroll
     for (int j = 0; j < 3; ++j) {
       T s = T(0);
+#pragma unroll
       for (int a = 0; a < 4; ++a) s += phi[a][i] * phi[a][j];
       G[i + 3 * j] = s;
     }
 }
 
-// fast-path test on the element law: true when K needs no eigenvalue change
-// beyond the translation modes (all non-null eigenvalues >= tol).
+// fast-path test on the element law: true when every non-translational
+// eigenvalue of the element matrix is >= tol (nothing to project).
 template <class Law, class T>
 BT_HD bool psd_fast_ok(const Law &law, const T (*phi)[3], T tol) {
-  T S[81], G[9], Gi[9];
-  law_matrix9(law, S);
+  T S[45], G[9], Gi[9];
+  law_matrix9p(law, S);
   gram3(G, phi);
   inv3(Gi, G);
+#pragma unroll
   for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j)
-      for (int k = 0; k < 3; ++k) S[(k + 3 * i) + 9 * (k + 3 * j)] -= tol * Gi[i + 3 * j];
-  return chol9_ok(S);
+#pragma unroll
+    for (int j = 0; j <= i; ++j)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) S[p9(k + 3 * i, k + 3 * j)] -= tol * Gi[i + 3 * j];
+  return chol9p_ok(S);
 }
 
-// Cyclic Jacobi eigen-decomposition of a symmetric n x n A (column-major,
-// overwritten by a near-diagonal matrix), W = eigenvectors.
-template <int N, class T>
-BT_HD void jacobi_eig(T *A, T *W, int sweeps) {
-  for (int i = 0; i < N * N; ++i) W[i] = (i % (N + 1) == 0) ? T(1) : T(0);
-  for (int s = 0; s < sweeps; ++s) {
-    T off = T(0), tot = T(0);
-    for (int i = 0; i < N; ++i)
-      for (int j = 0; j < N; ++j) {
-        T v = A[i + N * j] * A[i + N * j];
-        tot += v;
-        if (i != j) off += v;
-      }
-    if (off <= (sizeof(T) == 4 ? T(1e-13) : T(1e-30)) * tot) break;
-    for (int p = 0; p < N - 1; ++p)
-      for (int q = p + 1; q < N; ++q) {
-        T apq = A[p + N * q];
-        if (apq == T(0)) continue;
-        T theta = (A[q + N * q] - A[p + N * p]) / (T(2) * apq);
-        T t = (theta >= T(0) ? T(1) : T(-1)) / (bt_abs(theta) + bt_sqrt(theta * theta + T(1)));
-        T c = T(1) / bt_sqrt(t * t + T(1)), sn = t * c;
-        for (int k = 0; k < N; ++k) {
-          T akp = A[k + N * p], akq = A[k + N * q];
-          A[k + N * p] = c * akp - sn * akq;
-          A[k + N * q] = sn * akp + c * akq;
-        }
-        for (int k = 0; k < N; ++k) {
-          T apk = A[p + N * k], aqk = A[q + N * k];
-          A[p + N * k] = c * apk - sn * aqk;
-          A[q + N * k] = sn * apk + c * aqk;
-        }
-        for (int k = 0; k < N; ++k) {
-          T wkp = W[k + N * p], wkq = W[k + N * q];
-          W[k + N * p] = c * wkp - sn * wkq;
-          W[k + N * q] = sn * wkp + c * wkq;
-        }
-      }
-  }
-}
-
-// Slow path: the 4 projected blocks K_ab (b = 0..3) of row a (out[b][k*3+l]),
-// without the tol/4 translation term.
-template <class Law, class T>
-BT_HD_NOINLINE void psd_row_slow(const Law &law, const T (*phi)[3], T tol, int a, T (*out)[9]) {
-  T S[81];
-  law_matrix9(law, S);
-  // thin QR of Phi (4x3) by modified Gram-Schmidt on its columns
-  T Q[4][3], Rm[9];
+// thin QR of Phi (4x3) by modified Gram-Schmidt on its columns: Phi = Q R
+template <class T>
+BT_HD void qr_phi(const T (*phi)[3], T (*Q)[3], T *Rm) {
+#pragma unroll
   for (int j = 0; j < 3; ++j) {
     T v[4];
+#pragma unroll
     for (int r = 0; r < 4; ++r) v[r] = phi[r][j];
-    for (int i = 0; i < j; ++i) {
-      T d = T(0);
-      for (int r = 0; r < 4; ++r) d += Q[r][i] * v[r];
-      Rm[i + 3 * j] = d;
-      for (int r = 0; r < 4; ++r) v[r] -= d * Q[r][i];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      if (i < j) {
+        T d = T(0);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) d += Q[r][i] * v[r];
+        Rm[i + 3 * j] = d;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) v[r] -= d * Q[r][i];
+      } else if (i > j) {
+        Rm[i + 3 * j] = T(0);
+      }
     }
     T nrm = T(0);
+#pragma unroll
     for (int r = 0; r < 4; ++r) nrm += v[r] * v[r];
     nrm = bt_sqrt(nrm);
     Rm[j + 3 * j] = nrm;
-    for (int i = j + 1; i < 3; ++i) Rm[i + 3 * j] = T(0);
-    T inv = nrm > T(0) ? T(1) / nrm : T(0);
+    const T inv = nrm > T(0) ? T(1) / nrm : T(0);
+#pragma unroll
     for (int r = 0; r < 4; ++r) Q[r][j] = v[r] * inv;
   }
-  // M[(k + 3c), (l + 3d)] = sum_{i,j} R[c][i] R[d][j] S[(k + 3i), (l + 3j)]
-  T Tm[81], M[81];
-  for (int col = 0; col < 9; ++col)
-    for (int k = 0; k < 3; ++k)
-      for (int c = 0; c < 3; ++c) {
-        T s = T(0);
-        for (int i = 0; i < 3; ++i) s += Rm[c + 3 * i] * S[(k + 3 * i) + 9 * col];
-        Tm[(k + 3 * c) + 9 * col] = s;
-      }
-  for (int row = 0; row < 9; ++row)
-    for (int l = 0; l < 3; ++l)
-      for (int d = 0; d < 3; ++d) {
-        T s = T(0);
-        for (int j = 0; j < 3; ++j) s += Rm[d + 3 * j] * Tm[row + 9 * (l + 3 * j)];
-        M[row + 9 * (l + 3 * d)] = s;
-      }
-  for (int i = 0; i < 9; ++i)
-    for (int j = i + 1; j < 9; ++j) {
-      T s = T(0.5) * (M[i + 9 * j] + M[j + 9 * i]);
-      M[i + 9 * j] = s;
-      M[j + 9 * i] = s;
+}
+
+// Cyclic Jacobi on a packed symmetric 9x9 (overwritten: eigenvalues on the
+// diagonal), W = eigenvectors (column-major 9x9). Rotation indices are
+// compile-time so A and W stay in registers.
+template <class T>
+BT_HD void jacobi9p(T *A, T *W, int sweeps) {
+#pragma unroll
+  for (int i = 0; i < 81; ++i) W[i] = (i % 10 == 0) ? T(1) : T(0);
+  for (int s = 0; s < sweeps; ++s) {
+    T off = T(0), dia = T(0);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      dia += A[p9(i, i)] * A[p9(i, i)];
+#pragma unroll
+      for (int j = 0; j < i; ++j) off += A[p9(i, j)] * A[p9(i, j)];
     }
+    if (off <= (sizeof(T) == 4 ? T(1e-14) : T(1e-32)) * dia) break;
+#pragma unroll
+    for (int p = 0; p < 8; ++p)
+#pragma unroll
+      for (int q = p + 1; q < 9; ++q) {
+        const T apq = A[p9(p, q)];
+        if (apq != T(0)) {
+          const T theta = (A[p9(q, q)] - A[p9(p, p)]) / (T(2) * apq);
+          const T t = (theta >= T(0) ? T(1) : T(-1)) / (bt_abs(theta) + bt_sqrt(theta * theta + T(1)));
+          const T c = T(1) / bt_sqrt(t * t + T(1)), sn = t * c;
+          A[p9(p, p)] -= t * apq;
+          A[p9(q, q)] += t * apq;
+          A[p9(p, q)] = T(0);
+#pragma unroll
+          for (int k = 0; k < 9; ++k) {
+            if (k != p && k != q) {
+              const T akp = A[p9(k, p)], akq = A[p9(k, q)];
+              A[p9(k, p)] = c * akp - sn * akq;
+              A[p9(k, q)] = sn * akp + c * akq;
+            }
+          }
+#pragma unroll
+          for (int k = 0; k < 9; ++k) {
+            const T wkp = W[k + 9 * p], wkq = W[k + 9 * q];
+            W[k + 9 * p] = c * wkp - sn * wkq;
+            W[k + 9 * q] = sn * wkp + c * wkq;
+          }
+        }
+      }
+  }
+}
+
+// Slow path, step 1 (once per element): N = W max(L, tol) W^T (packed, 45)
+// with M = (R (x) I) S (R^T (x) I) = W L W^T.
+template <class Law, class T>
+BT_HD_NOINLINE void psd_eig_N(const Law &law, const T (*phi)[3], T tol, T *N) {
+  T M[45];
+  {
+    T S[45], Q[4][3], Rm[9];
+    law_matrix9p(law, S);
+    qr_phi(phi, Q, Rm);
+    // M[(k + 3c), (l + 3d)] = sum_{i,j} R[c][i] R[d][j] S[(k + 3i), (l + 3j)]  (R upper triangular)
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int d = 0; d <= c; ++d)
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+          for (int l = 0; l < 3; ++l) {
+            if ((k + 3 * c) < (l + 3 * d)) continue;
+            T acc = T(0);
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+              for (int j = 0; j < 3; ++j)
+                if (i >= c && j >= d) acc += Rm[c + 3 * i] * Rm[d + 3 * j] * S[p9(k + 3 * i, l + 3 * j)];
+            M[p9(k + 3 * c, l + 3 * d)] = acc;
+          }
+  }
   T W[81];
-  jacobi_eig<9>(M, W, sizeof(T) == 4 ? 12 : 30);
+  jacobi9p(M, W, sizeof(T) == 4 ? 10 : 30);
   T lam[9];
-  for (int i = 0; i < 9; ++i) lam[i] = M[i + 9 * i] < tol ? tol : M[i + 9 * i];
-  // N = W diag(lam) W^T
-  T N[81];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) lam[i] = M[p9(i, i)] < tol ? tol : M[p9(i, i)];
+#pragma unroll
   for (int i = 0; i < 9; ++i)
-    for (int j = 0; j < 9; ++j) {
-      T s = T(0);
-      for (int k = 0; k < 9; ++k) s += W[i + 9 * k] * lam[k] * W[j + 9 * k];
-      N[i + 9 * j] = s;
+#pragma unroll
+    for (int j = 0; j <= i; ++j) {
+      T acc = T(0);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) acc += W[i + 9 * k] * lam[k] * W[j + 9 * k];
+      N[p9(i, j)] = acc;
     }
+}
+
+// Slow path, step 2 (per incidence): blocks K_ab (b = 0..3) of row a from the
+// projected N (packed), without the tol/4 translation term.
+template <class T>
+BT_HD void psd_blocks_from_N(const T *N, const T (*phi)[3], int a, T (*out)[9]) {
+  T Q[4][3], Rm[9];
+  qr_phi(phi, Q, Rm);
+#pragma unroll
   for (int b = 0; b < 4; ++b)
+#pragma unroll
     for (int k = 0; k < 3; ++k)
+#pragma unroll
       for (int l = 0; l < 3; ++l) {
-        T s = T(0);
+        T acc = T(0);
+#pragma unroll
         for (int c = 0; c < 3; ++c)
-          for (int d = 0; d < 3; ++d) s += Q[a][c] * Q[b][d] * N[(k + 3 * c) + 9 * (l + 3 * d)];
-        out[b][3 * k + l] = s;
+#pragma unroll
+          for (int d = 0; d < 3; ++d) acc += Q[a][c] * Q[b][d] * N[p9(k + 3 * c, l + 3 * d)];
+        out[b][3 * k + l] = acc;
       }
+}
+
+// Both steps (used by host tests and by callers without a pre-pass)
+template <class Law, class T>
+BT_HD void psd_row_slow(const Law &law, const T (*phi)[3], T tol, int a, T (*out)[9]) {
+  T N[45];
+  psd_eig_N(law, phi, tol, N);
+  psd_blocks_from_N(N, phi, a, out);
 }
 
 }  // namespace bartels

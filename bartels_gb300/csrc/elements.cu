@@ -291,36 +291,64 @@ __global__ void k_grad_gather(int nV, const int *__restrict__ inc_ptr, const int
 // precomputed in inc_pos. Every entry is therefore summed over its tets in tet
 // order, as the reference's setFromTriplets does. The chunk's values are then
 // written out with coalesced stores.
-template <int MODEL, bool PSD>
-__device__ __forceinline__ void hess_slab(const TetRec32 &r, const float (*phi)[3], const float4 *__restrict__ u,
-                                          int add_identity, float tol, int corot_exact, int a, float (*K)[9]) {
+template <int MODEL>
+__device__ __forceinline__ void elem_F(const TetRec32 &r, const float4 *__restrict__ u, int add_identity, float *F) {
   const float4 x0 = __ldg(u + r.idx.x), x1 = __ldg(u + r.idx.y), x2 = __ldg(u + r.idx.z), x3 = __ldg(u + r.idx.w);
   const float p0[3] = {x0.x, x0.y, x0.z}, p1[3] = {x1.x, x1.y, x1.z}, p2[3] = {x2.x, x2.y, x2.z},
               p3[3] = {x3.x, x3.y, x3.z};
-  float F[9];
   def_grad(F, p0, p1, p2, p3, r.dphi, add_identity != 0);
-  auto run = [&](const auto &law) {
-    bool slow = false;
-    if (PSD) slow = !psd_fast_ok(law, phi, tol);
-    if (slow) {
-      psd_row_slow(law, phi, tol, a, K);
-    } else {
-#pragma unroll
-      for (int b = 0; b < 4; ++b) law.block(phi[a], phi[b], K[b]);
-    }
-  };
-  if (MODEL == MODEL_NH) run(LawNH<float>(F, r.pv));
-  else if (MODEL == MODEL_NH_ISO) run(LawNHIso<float>(F, r.pv));
-  else if (MODEL == MODEL_STVK) run(LawStVK<float>(F, r.pv));
-  else run(LawCorot<float>(F, r.pv, corot_exact != 0));
 }
 
+template <int MODEL, class Fn>
+__device__ __forceinline__ void with_law(const float *F, const float *pv, int corot_exact, Fn &&fn) {
+  if constexpr (MODEL == MODEL_NH) fn(LawNH<float>(F, pv));
+  else if constexpr (MODEL == MODEL_NH_ISO) fn(LawNHIso<float>(F, pv));
+  else if constexpr (MODEL == MODEL_STVK) fn(LawStVK<float>(F, pv));
+  else fn(LawCorot<float>(F, pv, corot_exact != 0));
+}
+
+// PSD pre-pass, one thread per tet: decide whether simple_psd_fix changes the
+// element matrix beyond its translation modes; if so store the projected 9x9
+// N (packed, 45 floats) and flag the tet.
+template <int MODEL>
+__global__ void __launch_bounds__(128)
+k_psd_prepass(int nT, const TetRec32 *__restrict__ rec, const float4 *__restrict__ u, int add_identity, float tol,
+              int corot_exact, unsigned char *__restrict__ slow, float *__restrict__ Nbuf) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nT; t += gridDim.x * blockDim.x) {
+    TetRec32 r;
+    load_rec32(rec, t, r);
+    float phi[4][3];
+    phi4(r.dphi, phi);
+    float F[9];
+    elem_F<MODEL>(r, u, add_identity, F);
+    unsigned char flag = 0;
+    with_law<MODEL>(F, r.pv, corot_exact, [&](const auto &law) {
+      if (!psd_fast_ok(law, phi, tol)) {
+        flag = 1;
+        float N[45];
+        psd_eig_N(law, phi, tol, N);
+        float *o = Nbuf + 45ll * t;
+#pragma unroll
+        for (int i = 0; i < 45; ++i) o[i] = N[i];
+      }
+    });
+    slow[t] = flag;
+  }
+}
+
+// One CTA per chunk of consecutive vertices, one thread per vertex. The thread
+// walks its incidences in tet order, evaluates the 3x12 slab (row block a) of
+// the element Hessian B^T d2psi B vol (PSD-projected if asked, from the
+// pre-pass), and adds the four 3x3 blocks into its CSR rows staged in shared
+// memory at the positions precomputed in inc_pos. Every entry is therefore
+// summed over its tets in tet order, as the reference's setFromTriplets does.
+// The chunk's values are then written out with coalesced stores.
 template <int MODEL, bool PSD>
 __global__ void __launch_bounds__(kChunkMaxVerts)
 k_hess(const int *__restrict__ chunk_v, const int *__restrict__ brp, const int *__restrict__ inc_ptr,
        const int *__restrict__ inc_tet, const uint32_t *__restrict__ inc_pos, const TetRec32 *__restrict__ rec,
        const float4 *__restrict__ u, int add_identity, float cK, float cM, float tol, int corot_exact,
-       float *__restrict__ values) {
+       const unsigned char *__restrict__ slow, const float *__restrict__ Nbuf, float *__restrict__ values) {
   extern __shared__ float sbuf[];
   const int v0 = chunk_v[blockIdx.x], v1 = chunk_v[blockIdx.x + 1];
   const int b0 = brp[v0];
@@ -342,13 +370,28 @@ k_hess(const int *__restrict__ chunk_v, const int *__restrict__ brp, const int *
       float phi[4][3];
       phi4(r.dphi, phi);
       float K[4][9];
-      if (MODEL >= 0) {
-        hess_slab<MODEL, PSD>(r, phi, u, add_identity, tol, corot_exact, a, K);
+      if constexpr (MODEL >= 0) {
+        bool from_n = false;
+        if constexpr (PSD) from_n = __ldg(slow + t) != 0;
+        if (from_n) {
+          float N[45];
+          const float *src = Nbuf + 45ll * t;
+#pragma unroll
+          for (int i = 0; i < 45; ++i) N[i] = __ldg(src + i);
+          psd_blocks_from_N(N, phi, a, K);
+        } else {
+          float F[9];
+          elem_F<MODEL>(r, u, add_identity, F);
+          with_law<MODEL>(F, r.pv, corot_exact, [&](const auto &law) {
+#pragma unroll
+            for (int b = 0; b < 4; ++b) law.block(phi[a], phi[b], K[b]);
+          });
+        }
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
 #pragma unroll
           for (int i = 0; i < 9; ++i) K[b][i] *= cK;
-          if (PSD) {
+          if constexpr (PSD) {
             K[b][0] += cK * 0.25f * tol;
             K[b][4] += cK * 0.25f * tol;
             K[b][8] += cK * 0.25f * tol;
@@ -552,8 +595,18 @@ static int launch_hess_t(bartels_ctx ctx, bartels_mesh_plan plan, const float4 *
     BT_CUDA(cudaFuncSetAttribute(k_hess<MODEL, PSD>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     attr_set = true;
   }
+  unsigned char *slow = nullptr;
+  float *nbuf = nullptr;
+  if constexpr (PSD && MODEL >= 0) {
+    const size_t nT = (size_t)plan->nT;
+    BT_CHECK(plan->w_psd.ensure(nT * (45 * sizeof(float) + 1) + 256));
+    nbuf = plan->w_psd.as<float>();
+    slow = reinterpret_cast<unsigned char *>(nbuf + 45 * nT);
+    BT_LAUNCH(ctx, k_psd_prepass<MODEL>, grid_for(ctx, plan->nT, 128), 128, 0, plan->nT, plan->rec32, u,
+              add_identity, tol, corot_exact, slow, nbuf);
+  }
   BT_LAUNCH(ctx, (k_hess<MODEL, PSD>), plan->nchunks, kChunkMaxVerts, smem, plan->chunk_v, plan->brp, plan->inc_ptr,
-            plan->inc_tet, plan->inc_pos, plan->rec32, u, add_identity, cK, cM, tol, corot_exact, values);
+            plan->inc_tet, plan->inc_pos, plan->rec32, u, add_identity, cK, cM, tol, corot_exact, slow, nbuf, values);
   return BARTELS_OK;
 }
 

@@ -85,6 +85,9 @@ struct bartels_ctx_s {
   int num_sms = 0;
   cudaStream_t stream = nullptr;
   int64_t launches = 0;
+  // lanes per vertex row in the block-layout SpMV (4, 8 or 16; tuned per GPU,
+  // overridable with BARTELS_SPMV_LANES)
+  int spmv_lanes = 8;
   // pinned host staging for small read-backs
   double *host_scalars = nullptr;
   // device scratch for reductions
@@ -128,7 +131,7 @@ struct bartels_mesh_plan_s {
   // true when dphidX is the rest shape's own (F = I + sum (u_a - u_0) phi_a^T)
   bool dphi_matches_rest = true;
   // solver workspace
-  bartels::DevBuf w_values, w_minv, w_vec, w_grad_e, w_energy, w_u, w_pcg;
+  bartels::DevBuf w_values, w_minv, w_vec, w_grad_e, w_energy, w_u, w_pcg, w_psd;
 };
 
 namespace bartels {

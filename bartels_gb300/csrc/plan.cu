@@ -253,6 +253,7 @@ void plan_free(bartels_mesh_plan plan) {
   plan->w_energy.release();
   plan->w_u.release();
   plan->w_pcg.release();
+  plan->w_psd.release();
 }
 
 }  // namespace bartels

@@ -24,18 +24,20 @@ int launch_prep_u(bartels_ctx ctx, bartels_mesh_plan plan, const double *x, cons
 int launch_hess(bartels_ctx ctx, bartels_mesh_plan plan, int model, int psd_mode, const float4 *u, int add_identity,
                 float cK, float cM, float tol, int flags, float *values);
 
-constexpr int kVecBlocksPerSM = 4;
+constexpr int kVecBlocksPerSM = 8;
 constexpr int kSpmvBlocksPerSM = 8;
 
+// Device-side PCG scalars. Reductions finish in the last block of the kernel
+// that produces them (fixed summation order), so consumers read scalars.
 struct PcgState {
-  double rz[2];
-  double rr0;
-  double rr;
-  double tol2;
-  int it;
+  double rz, rz_prev;   // r.z of the current and previous iterate
+  double rr;            // r.r of the current iterate
+  double pap;           // p.Ap of the current direction
+  double rr0, tol2;
+  int it;               // iterations completed in the current inner solve
   int done;
   int max_it;
-  int pad;
+  unsigned int count;   // blocks finished (last-block reductions)
 };
 
 // ------------------------------------------------------------- reductions ---
@@ -79,47 +81,6 @@ __device__ __forceinline__ double cta_sum_array(const double *__restrict__ a, in
 }
 
 // ------------------------------------------------------------------ SpMV ---
-// Block layout: one warp per vertex row. Lanes walk the (block, component)
-// pairs of the row; each lane reads the three scalar rows at that column.
-template <bool DOT>
-__global__ void __launch_bounds__(256)
-k_spmv_blk(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, const float *__restrict__ val,
-           const float *__restrict__ x, float *__restrict__ y, const unsigned char *__restrict__ pinned,
-           double *__restrict__ partial, const PcgState *__restrict__ st) {
-  if (st && st->done) return;
-  const int lane = threadIdx.x & 31;
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  double acc = 0.0;
-  for (int v = warp; v < nV; v += nwarps) {
-    const int rb = brp[v];
-    const int rs = 3 * (brp[v + 1] - rb);
-    const float *r0 = val + 9ll * rb;
-    float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-    for (int e = lane; e < rs; e += 32) {
-      const int j = e / 3, l = e - 3 * j;
-      const float xv = __ldg(x + 3 * __ldg(bcol + rb + j) + l);
-      s0 += __ldg(r0 + e) * xv;
-      s1 += __ldg(r0 + rs + e) * xv;
-      s2 += __ldg(r0 + 2 * rs + e) * xv;
-    }
-    s0 = warp_sumf(s0);
-    s1 = warp_sumf(s1);
-    s2 = warp_sumf(s2);
-    if (pinned && pinned[v]) s0 = s1 = s2 = 0.f;
-    if (lane == 0) {
-      y[3 * v] = s0;
-      y[3 * v + 1] = s1;
-      y[3 * v + 2] = s2;
-      if (DOT) acc += (double)(x[3 * v] * s0 + x[3 * v + 1] * s1 + x[3 * v + 2] * s2);
-    }
-  }
-  if (DOT) {
-    double s = cta_sum(acc);
-    if (threadIdx.x == 0) partial[blockIdx.x] = s;
-  }
-}
-
 // FP64 residual r = b - A x (block layout), partial sums of r.r
 __global__ void __launch_bounds__(256)
 k_resid_blk64(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, const float *__restrict__ val,
@@ -209,20 +170,27 @@ k_resid_csr64(int n, const int *__restrict__ rp, const int *__restrict__ ci, con
 // inverse of each 3x3 diagonal block (FP64 inversion, FP32 storage). Blocks
 // that are pinned get 0; singular or indefinite blocks fall back to the
 // inverse diagonal.
-__device__ void store_inv3(const double *A, float *out) {
+// 6 floats per block: m00 m11 m22 m01 m02 m12 of the symmetric inverse
+__device__ void store_inv3(const double *A0, float *out) {
+  double A[9];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) A[i + 3 * j] = 0.5 * (A0[i + 3 * j] + A0[j + 3 * i]);
   double G[9];
   cof3(G, A);
   double det = A[0] * G[0] + A[1] * G[1] + A[2] * G[2];
-  bool ok = det > 0.0 && isfinite(det);
-  for (int i = 0; i < 9; ++i) out[i] = 0.f;
-  if (ok) {
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) out[3 * i + j] = (float)(G[j + 3 * i] / det);  // row-major inverse
+  if (det > 0.0 && isfinite(det)) {
+    out[0] = (float)(G[0] / det);
+    out[1] = (float)(G[4] / det);
+    out[2] = (float)(G[8] / det);
+    out[3] = (float)(G[3] / det);
+    out[4] = (float)(G[6] / det);
+    out[5] = (float)(G[7] / det);
   } else {
     for (int i = 0; i < 3; ++i) {
       double d = A[i + 3 * i];
-      out[4 * i] = (d != 0.0 && isfinite(d)) ? (float)(1.0 / d) : 1.f;
+      out[i] = (d != 0.0 && isfinite(d)) ? (float)(1.0 / d) : 1.f;
     }
+    out[3] = out[4] = out[5] = 0.f;
   }
 }
 
@@ -235,13 +203,13 @@ __global__ void k_minv_blk(int nV, const int *__restrict__ brp, const int *__res
     double A[9];
     for (int k = 0; k < 3; ++k)
       for (int l = 0; l < 3; ++l) A[k + 3 * l] = r0[k * rs + 3 * j + l];
-    float out[9];
+    float out[6];
     if (pinned && pinned[v]) {
-      for (int i = 0; i < 9; ++i) out[i] = 0.f;
+      for (int i = 0; i < 6; ++i) out[i] = 0.f;
     } else {
       store_inv3(A, out);
     }
-    for (int i = 0; i < 9; ++i) minv[9ll * v + i] = out[i];
+    for (int i = 0; i < 6; ++i) minv[6ll * v + i] = out[i];
   }
 }
 
@@ -260,24 +228,48 @@ __global__ void k_minv_csr(int nb, int n, const int *__restrict__ rp, const int 
         if (c >= 0 && c < 3) A[k + 3 * c] += val[e];
       }
     }
-    float out[9];
+    float out[6];
     store_inv3(A, out);
-    for (int i = 0; i < 9; ++i) minv[9ll * v + i] = out[i];
+    for (int i = 0; i < 6; ++i) minv[6ll * v + i] = out[i];
   }
 }
 
 // ------------------------------------------------------------ PCG vectors ---
 __device__ __forceinline__ void apply_minv(const float *__restrict__ minv, int v, const float *r, float *z) {
-  const float *m = minv + 9ll * v;
-  z[0] = m[0] * r[0] + m[1] * r[1] + m[2] * r[2];
-  z[1] = m[3] * r[0] + m[4] * r[1] + m[5] * r[2];
-  z[2] = m[6] * r[0] + m[7] * r[1] + m[8] * r[2];
+  const float *m = minv + 6ll * v;
+  const float m00 = m[0], m11 = m[1], m22 = m[2], m01 = m[3], m02 = m[4], m12 = m[5];
+  z[0] = m00 * r[0] + m01 * r[1] + m02 * r[2];
+  z[1] = m01 * r[0] + m11 * r[1] + m12 * r[2];
+  z[2] = m02 * r[0] + m12 * r[1] + m22 * r[2];
 }
 
-// start of an inner solve: x = 0, r = (float) r64, z = M^-1 r, p = z
+// Last-block completion: returns true in every thread of the block that
+// finished last (after all partials are visible).
+__device__ __forceinline__ bool last_block(unsigned int *count) {
+  __shared__ bool am_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned int prev = atomicAdd(count, 1u);
+    am_last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  return am_last;
+}
+
+// deterministic sum of n partials (fixed order), valid in thread 0
+__device__ __forceinline__ double sum_partials(const double *a, int n) {
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) acc += __ldcg(a + i);
+  return cta_sum(acc);
+}
+
+// start of an inner solve: x = 0, r = (float) r64, z = M^-1 r, p = 0
 __global__ void k_pcg_init(int nb, int n, const double *__restrict__ r64, const float *__restrict__ minv,
                            float *__restrict__ x, float *__restrict__ r, float *__restrict__ z,
-                           float *__restrict__ p, double *__restrict__ part_rz, double *__restrict__ part_rr) {
+                           float *__restrict__ p0, float *__restrict__ p1, double *__restrict__ part_a,
+                           double *__restrict__ part_b, PcgState *__restrict__ st, double inner_rel2, double abs_tol2,
+                           int max_it) {
   double arz = 0.0, arr = 0.0;
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nb; v += gridDim.x * blockDim.x) {
     float rv[3], zv[3];
@@ -289,62 +281,193 @@ __global__ void k_pcg_init(int nb, int n, const double *__restrict__ r64, const 
         x[i] = 0.f;
         r[i] = rv[k];
         z[i] = zv[k];
-        p[i] = zv[k];
+        p0[i] = 0.f;
+        p1[i] = 0.f;
         arz += (double)rv[k] * zv[k];
         arr += (double)rv[k] * rv[k];
       }
     }
   }
   double s = cta_sum(arz);
-  if (threadIdx.x == 0) part_rz[blockIdx.x] = s;
+  if (threadIdx.x == 0) part_a[blockIdx.x] = s;
   s = cta_sum(arr);
-  if (threadIdx.x == 0) part_rr[blockIdx.x] = s;
-}
-
-__global__ void k_pcg_setup_state(int nparts, const double *__restrict__ part_rz, const double *__restrict__ part_rr,
-                                  double inner_rel2, double abs_tol2, int max_it, PcgState *__restrict__ st) {
-  const double rz = cta_sum_array(part_rz, nparts);
-  const double rr = cta_sum_array(part_rr, nparts);
-  if (threadIdx.x == 0) {
-    st->rz[0] = rz;
-    st->rz[1] = rz;
-    st->rr0 = rr;
-    st->rr = rr;
-    st->tol2 = fmax(inner_rel2 * rr, abs_tol2);
-    st->it = -1;
-    st->max_it = max_it;
-    st->done = (rr <= st->tol2 || max_it <= 0) ? 1 : 0;
+  if (threadIdx.x == 0) part_b[blockIdx.x] = s;
+  if (last_block(&st->count)) {
+    const double rz = sum_partials(part_a, gridDim.x);
+    const double rr = sum_partials(part_b, gridDim.x);
+    if (threadIdx.x == 0) {
+      st->rz = rz;
+      st->rz_prev = rz;
+      st->rr = rr;
+      st->rr0 = rr;
+      st->pap = 0.0;
+      st->tol2 = fmax(inner_rel2 * rr, abs_tol2);
+      st->it = 0;
+      st->max_it = max_it;
+      st->done = (rr <= st->tol2 || max_it <= 0 || !(rr == rr)) ? 1 : 0;
+      st->count = 0;
+    }
   }
 }
 
-// iteration counter (one thread) -- runs before the SpMV of each iteration
-__global__ void k_pcg_tick(PcgState *__restrict__ st) {
-  if (!st->done) st->it += 1;
+// One vertex row of the block-layout SpMV: G lanes walk the row's (block,
+// component) pairs and read the three scalar rows at that column with
+// streaming loads; xval(c) supplies the vector entry at scalar column c.
+// Returns the three row sums in every lane of the group.
+template <int G, class XV>
+__device__ __forceinline__ void spmv_row_blk(int v, int sl, const int *__restrict__ brp, const int *__restrict__ bcol,
+                                             const float *__restrict__ val, XV &&xval, float &s0, float &s1,
+                                             float &s2) {
+  const int rb = __ldg(brp + v);
+  const int rs = 3 * (__ldg(brp + v + 1) - rb);
+  const float *r0 = val + 9ll * rb;
+  s0 = s1 = s2 = 0.f;
+  for (int e = sl; e < rs; e += G) {
+    const int j = e / 3, l = e - 3 * j;
+    const float xv = xval(3 * __ldg(bcol + rb + j) + l);
+    s0 += __ldcs(r0 + e) * xv;
+    s1 += __ldcs(r0 + rs + e) * xv;
+    s2 += __ldcs(r0 + 2 * rs + e) * xv;
+  }
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) {
+    s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+  }
 }
 
-// alpha = rz / pAp; x += alpha p; r -= alpha Ap; z = M^-1 r; partial r.z, r.r
-__global__ void k_pcg_update(int nb, int n, int nparts, const double *__restrict__ part_pap,
-                             const float *__restrict__ minv, const float *__restrict__ p, const float *__restrict__ ap,
-                             float *__restrict__ x, float *__restrict__ r, float *__restrict__ z,
-                             double *__restrict__ part_rz, double *__restrict__ part_rr,
-                             const PcgState *__restrict__ st) {
+// y = A x with the PCG's row mapping (rows of pinned vertices give 0)
+template <int G>
+__global__ void __launch_bounds__(256)
+k_spmv_blk_g(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, const float *__restrict__ val,
+             const float *__restrict__ x, float *__restrict__ y, const unsigned char *__restrict__ pinned) {
+  const int sl = (threadIdx.x & 31) % G;
+  const int group = (blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const int ngroups = (gridDim.x * blockDim.x) / G;
+  for (int v = group; v < nV; v += ngroups) {
+    float s0, s1, s2;
+    spmv_row_blk<G>(v, sl, brp, bcol, val, [&](int c) { return __ldg(x + c); }, s0, s1, s2);
+    if (sl == 0) {
+      if (pinned && pinned[v]) s0 = s1 = s2 = 0.f;
+      y[3 * v] = s0;
+      y[3 * v + 1] = s1;
+      y[3 * v + 2] = s2;
+    }
+  }
+}
+
+// Direction + SpMV, block layout: p = z + beta p_old (computed on the fly for
+// every column read, written by the row owner), ap = A p, partials of p.Ap.
+template <int G>
+__global__ void __launch_bounds__(256)
+k_pcg_spmv_blk(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, const float *__restrict__ val,
+               const float *__restrict__ z, float *__restrict__ pa, float *__restrict__ pb, float *__restrict__ ap,
+               const unsigned char *__restrict__ pinned, double *__restrict__ part, PcgState *__restrict__ st) {
   if (st->done) return;
-  const double pap = cta_sum_array(part_pap, nparts);
-  const float alpha = (float)(st->rz[st->it & 1] / pap);
+  const int it = st->it;
+  const float beta = it == 0 ? 0.f : (float)(st->rz / st->rz_prev);
+  // iteration it reads p_{it-1} from (it odd ? pa : pb) and writes p_it to the other
+  const float *p_old = (it & 1) ? pa : pb;
+  float *p_new = (it & 1) ? pb : pa;
+  const int sl = (threadIdx.x & 31) % G;
+  const int group = (blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const int ngroups = (gridDim.x * blockDim.x) / G;
+  double acc = 0.0;
+  for (int v = group; v < nV; v += ngroups) {
+    float s0, s1, s2;
+    spmv_row_blk<G>(v, sl, brp, bcol, val, [&](int c) { return __ldcg(z + c) + beta * __ldcg(p_old + c); }, s0, s1,
+                    s2);
+    if (sl == 0) {
+      float pv[3];
+      for (int k = 0; k < 3; ++k) pv[k] = __ldcg(z + 3 * v + k) + beta * __ldcg(p_old + 3 * v + k);
+      if (pinned && pinned[v]) s0 = s1 = s2 = 0.f;
+      p_new[3 * v] = pv[0];
+      p_new[3 * v + 1] = pv[1];
+      p_new[3 * v + 2] = pv[2];
+      ap[3 * v] = s0;
+      ap[3 * v + 1] = s1;
+      ap[3 * v + 2] = s2;
+      acc += (double)(pv[0] * s0 + pv[1] * s1 + pv[2] * s2);
+    }
+  }
+  double s = cta_sum(acc);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+  if (last_block(&st->count)) {
+    const double pap = sum_partials(part, gridDim.x);
+    if (threadIdx.x == 0) {
+      st->pap = pap;
+      st->count = 0;
+    }
+  }
+}
+
+// Direction + SpMV for a generic scalar CSR (one warp per row).
+__global__ void __launch_bounds__(256)
+k_pcg_spmv_csr(int n, const int *__restrict__ rp, const int *__restrict__ ci, const float *__restrict__ val,
+               const float *__restrict__ z, float *__restrict__ pa, float *__restrict__ pb, float *__restrict__ ap,
+               double *__restrict__ part, PcgState *__restrict__ st) {
+  if (st->done) return;
+  const int it = st->it;
+  const float beta = it == 0 ? 0.f : (float)(st->rz / st->rz_prev);
+  const float *p_old = (it & 1) ? pa : pb;
+  float *p_new = (it & 1) ? pb : pa;
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  double acc = 0.0;
+  for (int i = warp; i < n; i += nwarps) {
+    float s = 0.f;
+    for (int k = rp[i] + lane; k < rp[i + 1]; k += 32) {
+      const int c = ci[k];
+      s += val[k] * (__ldcg(z + c) + beta * __ldcg(p_old + c));
+    }
+    s = warp_sumf(s);
+    if (lane == 0) {
+      const float pv = __ldcg(z + i) + beta * __ldcg(p_old + i);
+      p_new[i] = pv;
+      ap[i] = s;
+      acc += (double)(pv * s);
+    }
+  }
+  double s = cta_sum(acc);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+  if (last_block(&st->count)) {
+    const double pap = sum_partials(part, gridDim.x);
+    if (threadIdx.x == 0) {
+      st->pap = pap;
+      st->count = 0;
+    }
+  }
+}
+
+// alpha = rz / pAp; x += alpha p; r -= alpha Ap; z = M^-1 r; r.z and r.r;
+// convergence test and iteration count in the last block.
+__global__ void __launch_bounds__(256)
+k_pcg_update(int nb, int n, const float *__restrict__ minv, const float *__restrict__ pa,
+             const float *__restrict__ pb, const float *__restrict__ ap, float *__restrict__ x,
+             float *__restrict__ r, float *__restrict__ z, double *__restrict__ part_a, double *__restrict__ part_b,
+             PcgState *__restrict__ st) {
+  if (st->done) return;
+  const int it = st->it;
+  const float *p = (it & 1) ? pb : pa;
+  const float alpha = (float)(st->rz / st->pap);
   double arz = 0.0, arr = 0.0;
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nb; v += gridDim.x * blockDim.x) {
     float rv[3], zv[3];
+#pragma unroll
     for (int k = 0; k < 3; ++k) {
       const int i = 3 * v + k;
       if (i < n) {
-        x[i] += alpha * p[i];
-        rv[k] = r[i] - alpha * ap[i];
+        x[i] += alpha * __ldcg(p + i);
+        rv[k] = r[i] - alpha * __ldcg(ap + i);
         r[i] = rv[k];
       } else {
         rv[k] = 0.f;
       }
     }
     apply_minv(minv, v, rv, zv);
+#pragma unroll
     for (int k = 0; k < 3; ++k) {
       const int i = 3 * v + k;
       if (i < n) {
@@ -355,24 +478,20 @@ __global__ void k_pcg_update(int nb, int n, int nparts, const double *__restrict
     }
   }
   double s = cta_sum(arz);
-  if (threadIdx.x == 0) part_rz[blockIdx.x] = s;
+  if (threadIdx.x == 0) part_a[blockIdx.x] = s;
   s = cta_sum(arr);
-  if (threadIdx.x == 0) part_rr[blockIdx.x] = s;
-}
-
-// beta = rz_new / rz; p = z + beta p; convergence test
-__global__ void k_pcg_dir(int n, int nparts, const double *__restrict__ part_rz, const double *__restrict__ part_rr,
-                          const float *__restrict__ z, float *__restrict__ p, PcgState *__restrict__ st) {
-  if (st->done) return;
-  const double rz_new = cta_sum_array(part_rz, nparts);
-  const double rr = cta_sum_array(part_rr, nparts);
-  const int par = st->it & 1;
-  const float beta = (float)(rz_new / st->rz[par]);
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = z[i] + beta * p[i];
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    st->rz[par ^ 1] = rz_new;
-    st->rr = rr;
-    if (rr <= st->tol2 || st->it + 1 >= st->max_it || !(rr == rr)) st->done = 1;
+  if (threadIdx.x == 0) part_b[blockIdx.x] = s;
+  if (last_block(&st->count)) {
+    const double rz = sum_partials(part_a, gridDim.x);
+    const double rr = sum_partials(part_b, gridDim.x);
+    if (threadIdx.x == 0) {
+      st->rz_prev = st->rz;
+      st->rz = rz;
+      st->rr = rr;
+      st->it = it + 1;
+      if (rr <= st->tol2 || it + 1 >= st->max_it || !(rr == rr)) st->done = 1;
+      st->count = 0;
+    }
   }
 }
 
@@ -406,10 +525,9 @@ struct PcgOperator {
 };
 
 struct PcgWork {
-  float *x, *r, *z, *p, *ap, *minv;
-  double *r64, *part_a, *part_b, *part_c;
+  float *x, *r, *z, *pa, *pb, *ap, *minv;
+  double *r64, *part_a, *part_b;
   PcgState *st;
-  int nparts_spmv, nparts_vec;
 };
 
 static int grid_vec(bartels_ctx ctx, int64_t n) {
@@ -423,28 +541,24 @@ static int grid_spmv(bartels_ctx ctx, int64_t rows) {
   return (int)std::max<int64_t>(1, std::min(g, cap));
 }
 
-struct GraphCache {
-  cudaGraphExec_t exec = nullptr;
-  const void *key[8] = {};
-  int iters = 0;
-};
 
 static int pcg_enqueue_iters(bartels_ctx ctx, const PcgOperator &op, const PcgWork &w, int n, int nb, int iters) {
   const bool blk = op.plan != nullptr;
-  const int gs = blk ? grid_spmv(ctx, op.plan->nV) : grid_spmv(ctx, n);
+  const int gs = blk ? grid_spmv(ctx, (int64_t)op.plan->nV * ctx->spmv_lanes / 32 + 1) : grid_spmv(ctx, n);
   const int gv = grid_vec(ctx, nb);
-  const int gd = grid_vec(ctx, n);
   for (int i = 0; i < iters; ++i) {
-    BT_LAUNCH(ctx, k_pcg_tick, 1, 1, 0, w.st);
     if (blk) {
-      BT_LAUNCH(ctx, k_spmv_blk<true>, gs, 256, 0, op.plan->nV, op.plan->brp, op.plan->bcol, op.values, w.p, w.ap,
-                op.pinned, w.part_a, w.st);
+#define BT_K1(G)                                                                                                \
+  BT_LAUNCH(ctx, k_pcg_spmv_blk<G>, gs, 256, 0, op.plan->nV, op.plan->brp, op.plan->bcol, op.values, w.z, w.pa, \
+            w.pb, w.ap, op.pinned, w.part_a, w.st)
+      if (ctx->spmv_lanes == 4) BT_K1(4);
+      else if (ctx->spmv_lanes == 16) BT_K1(16);
+      else BT_K1(8);
+#undef BT_K1
     } else {
-      BT_LAUNCH(ctx, k_spmv_csr<true>, gs, 256, 0, n, op.rp, op.ci, op.values, w.p, w.ap, w.part_a, w.st);
+      BT_LAUNCH(ctx, k_pcg_spmv_csr, gs, 256, 0, n, op.rp, op.ci, op.values, w.z, w.pa, w.pb, w.ap, w.part_a, w.st);
     }
-    BT_LAUNCH(ctx, k_pcg_update, gv, 256, 0, nb, n, gs, w.part_a, w.minv, w.p, w.ap, w.x, w.r, w.z, w.part_b,
-              w.part_c, w.st);
-    BT_LAUNCH(ctx, k_pcg_dir, gd, 256, 0, n, gv, w.part_b, w.part_c, w.z, w.p, w.st);
+    BT_LAUNCH(ctx, k_pcg_update, gv, 256, 0, nb, n, w.minv, w.pa, w.pb, w.ap, w.x, w.r, w.z, w.part_a, w.part_b, w.st);
   }
   return BARTELS_OK;
 }
@@ -457,7 +571,7 @@ static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double
   const bool blk = op.plan != nullptr;
   const int gs = blk ? grid_spmv(ctx, op.plan->nV) : grid_spmv(ctx, n);
   const int gv = grid_vec(ctx, nb);
-  const int nparts = std::max(gs, gv);
+  const int nparts = std::max(std::max(gs, gv), 1024);
   // workspace layout
   size_t off = 0;
   auto take = [&](size_t bytes) {
@@ -465,25 +579,24 @@ static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double
     off += (bytes + 255) & ~size_t(255);
     return o;
   };
-  const size_t o_x = take(4ull * n), o_r = take(4ull * n), o_z = take(4ull * n), o_p = take(4ull * n),
-               o_ap = take(4ull * n), o_minv = take(36ull * nb), o_r64 = take(8ull * n), o_pa = take(8ull * nparts),
-               o_pb = take(8ull * nparts), o_pc = take(8ull * nparts), o_st = take(sizeof(PcgState));
+  const size_t o_x = take(4ull * n), o_r = take(4ull * n), o_z = take(4ull * n), o_pa = take(4ull * n),
+               o_pb = take(4ull * n), o_ap = take(4ull * n), o_minv = take(24ull * nb), o_r64 = take(8ull * n),
+               o_pa8 = take(8ull * nparts), o_pb8 = take(8ull * nparts), o_st = take(sizeof(PcgState));
   BT_CHECK(wbuf.ensure(off));
   char *base = wbuf.as<char>();
   PcgWork w;
   w.x = (float *)(base + o_x);
   w.r = (float *)(base + o_r);
   w.z = (float *)(base + o_z);
-  w.p = (float *)(base + o_p);
+  w.pa = (float *)(base + o_pa);
+  w.pb = (float *)(base + o_pb);
   w.ap = (float *)(base + o_ap);
   w.minv = (float *)(base + o_minv);
   w.r64 = (double *)(base + o_r64);
-  w.part_a = (double *)(base + o_pa);
-  w.part_b = (double *)(base + o_pb);
-  w.part_c = (double *)(base + o_pc);
+  w.part_a = (double *)(base + o_pa8);
+  w.part_b = (double *)(base + o_pb8);
   w.st = (PcgState *)(base + o_st);
-  w.nparts_spmv = gs;
-  w.nparts_vec = gv;
+  BT_CUDA(cudaMemsetAsync(w.st, 0, sizeof(PcgState), ctx->stream));
   // preconditioner
   if (blk) {
     BT_LAUNCH(ctx, k_minv_blk, grid_vec(ctx, op.plan->nV), 256, 0, op.plan->nV, op.plan->brp, op.plan->diag_pos,
@@ -554,18 +667,17 @@ static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double
     }
     rep->refinements = pass + 1;
     // inner FP32 PCG on r64
-    BT_LAUNCH(ctx, k_pcg_init, gv, 256, 0, nb, n, w.r64, w.minv, w.x, w.r, w.z, w.p, w.part_b, w.part_c);
     const double abs2 = (0.5 * target) * (0.5 * target);
-    BT_LAUNCH(ctx, k_pcg_setup_state, 1, 1024, 0, gv, w.part_b, w.part_c, prm.inner_rel_tol * prm.inner_rel_tol,
-              abs2, prm.max_iters - rep->iterations, w.st);
+    BT_LAUNCH(ctx, k_pcg_init, gv, 256, 0, nb, n, w.r64, w.minv, w.x, w.r, w.z, w.pa, w.pb, w.part_a, w.part_b, w.st,
+              prm.inner_rel_tol * prm.inner_rel_tol, abs2, prm.max_iters - rep->iterations);
     for (;;) {
       BT_CUDA(cudaGraphLaunch(exec, ctx->stream));
-      ctx->launches += 4 * chunk;
+      ctx->launches += 2 * chunk;
       BT_CUDA(cudaMemcpyAsync(&hs, w.st, sizeof(PcgState), cudaMemcpyDeviceToHost, ctx->stream));
       BT_CUDA(cudaStreamSynchronize(ctx->stream));
       if (hs.done) break;
     }
-    rep->iterations += hs.it + 1;
+    rep->iterations += hs.it;
     BT_LAUNCH(ctx, k_axpy64, grid_vec(ctx, n), 256, 0, n, w.x, x);
   }
   cudaGraphExecDestroy(exec);
@@ -741,8 +853,13 @@ int advance_implicit_euler(bartels_ctx ctx, bartels_mesh_plan plan, double dt, c
 }
 
 int plan_spmv(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const float *x, float *y) {
-  BT_LAUNCH(ctx, k_spmv_blk<false>, grid_spmv(ctx, plan->nV), 256, 0, plan->nV, plan->brp, plan->bcol, values, x, y,
-            plan->pinned, (double *)nullptr, (const PcgState *)nullptr);
+  const int g = grid_spmv(ctx, (int64_t)plan->nV * ctx->spmv_lanes / 32 + 1);
+  if (ctx->spmv_lanes == 4)
+    BT_LAUNCH(ctx, k_spmv_blk_g<4>, g, 256, 0, plan->nV, plan->brp, plan->bcol, values, x, y, plan->pinned);
+  else if (ctx->spmv_lanes == 16)
+    BT_LAUNCH(ctx, k_spmv_blk_g<16>, g, 256, 0, plan->nV, plan->brp, plan->bcol, values, x, y, plan->pinned);
+  else
+    BT_LAUNCH(ctx, k_spmv_blk_g<8>, g, 256, 0, plan->nV, plan->brp, plan->bcol, values, x, y, plan->pinned);
   return BARTELS_OK;
 }
 

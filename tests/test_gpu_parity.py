@@ -240,3 +240,43 @@ def test_kernel_launch_counter():
     V, E = kuhn_cube(2)
     bg.linear_tetmesh_dphi_dX(V, E)
     assert ctx.kernel_launches > before
+
+
+def test_device_hessian_and_spmv(oracle):
+    """bartels_plan_hessian_d + bartels_plan_spmv_d (the PCG's SpMV row loop)."""
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+    from bartels_gb300 import _lib
+    V, E, q = noisy_cube(4, amp=0.1, seed=10)
+    params = material_params("neohookean", len(E), 2e6, 0.45)
+    plan = bg.MeshPlan(V, E)
+    plan.set_element_data(params=params, density=np.full(len(E), 1000.0))
+    dphi, vol = oracle.dphi_dX(V, E), oracle.volume(V, E)
+    K = oracle.tetmesh_dq2("neohookean", len(V), E, q, dphi, vol, params, psd_tol=1e-6)
+    M = oracle.mass_matrix(len(V), E, np.full(len(E), 1000.0), vol)
+    H = (M + 1e-4 * K).tocsr()
+    L = bg.lib()
+    qd = torch.from_numpy(q).cuda()
+    x = torch.randn(3 * len(V), dtype=torch.float32, device="cuda")
+    y = torch.empty_like(x)
+    torch.cuda.synchronize()
+    for lanes in (4, 8, 16):
+        ctx = bg.Context(0)
+        ctx_lanes = lanes
+        import os
+        os.environ["BARTELS_SPMV_LANES"] = str(ctx_lanes)
+        ctx2 = bg.Context(0)
+        plan2 = bg.MeshPlan(V, E, ctx2)
+        plan2.set_element_data(params=params, density=np.full(len(E), 1000.0))
+        _lib.check(L.bartels_plan_hessian_d(ctx2.handle, plan2.handle, _lib.NEOHOOKEAN, _lib.PSD_SIMPLE_FIX, 1e-6, 0,
+                                            1e-4, 1.0, C.c_void_p(qd.data_ptr()), None), "hessian_d")
+        _lib.check(L.bartels_plan_spmv_d(ctx2.handle, plan2.handle, None, C.c_void_p(x.data_ptr()),
+                                         C.c_void_p(y.data_ptr())), "spmv_d")
+        ctx2.synchronize()
+        ref = H @ x.cpu().double().numpy()
+        got = y.cpu().double().numpy()
+        assert np.linalg.norm(got - ref) <= 1e-5 * np.linalg.norm(ref), lanes
+        plan2.close()
+        ctx2.close()
+        ctx.close()
+    os.environ.pop("BARTELS_SPMV_LANES", None)
