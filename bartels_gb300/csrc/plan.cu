@@ -31,10 +31,10 @@ const char *last_error_cstr() { return g_last_error.c_str(); }
 
 int DevBuf::ensure(size_t n) {
   if (n <= bytes) return BARTELS_OK;
+  const size_t want = std::max(n, bytes + bytes / 2);
   if (p) cudaFree(p);
   p = nullptr;
   bytes = 0;
-  size_t want = std::max(n, bytes + bytes / 2);
   cudaError_t e = cudaMalloc(&p, want);
   if (e != cudaSuccess) {
     p = nullptr;

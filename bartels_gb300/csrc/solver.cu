@@ -146,15 +146,15 @@ k_spmv_csr(int n, const int *__restrict__ rp, const int *__restrict__ ci, const 
 
 __global__ void __launch_bounds__(256)
 k_resid_csr64(int n, const int *__restrict__ rp, const int *__restrict__ ci, const float *__restrict__ val,
-              const double *__restrict__ x, const double *__restrict__ b, double *__restrict__ r,
-              double *__restrict__ partial) {
+              const double *__restrict__ val64, const double *__restrict__ x, const double *__restrict__ b,
+              double *__restrict__ r, double *__restrict__ partial) {
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   double acc = 0.0;
   for (int i = warp; i < n; i += nwarps) {
     double s = 0.0;
-    for (int k = rp[i] + lane; k < rp[i + 1]; k += 32) s += (double)val[k] * x[ci[k]];
+    for (int k = rp[i] + lane; k < rp[i + 1]; k += 32) s += (val64 ? val64[k] : (double)val[k]) * x[ci[k]];
     s = warp_sum(s);
     if (lane == 0) {
       double q = b[i] - s;
@@ -310,18 +310,18 @@ __global__ void k_pcg_init(int nb, int n, const double *__restrict__ r64, const 
   }
 }
 
-// One vertex row of the block-layout SpMV: G lanes walk the row's (block,
-// component) pairs and read the three scalar rows at that column with
-// streaming loads; xval(c) supplies the vector entry at scalar column c.
-// Returns the three row sums in every lane of the group.
+// One vertex row of the block-layout SpMV, split in two so that no shuffle
+// runs in a divergent region: spmv_row_acc (G lanes of a group walk the row's
+// (block, component) pairs and read the three scalar rows at that column with
+// streaming loads; xval(c) supplies the vector entry at scalar column c) runs
+// only for an active group, group_reduce runs in every lane of the warp.
 template <int G, class XV>
-__device__ __forceinline__ void spmv_row_blk(int v, int sl, const int *__restrict__ brp, const int *__restrict__ bcol,
+__device__ __forceinline__ void spmv_row_acc(int v, int sl, const int *__restrict__ brp, const int *__restrict__ bcol,
                                              const float *__restrict__ val, XV &&xval, float &s0, float &s1,
                                              float &s2) {
   const int rb = __ldg(brp + v);
   const int rs = 3 * (__ldg(brp + v + 1) - rb);
   const float *r0 = val + 9ll * rb;
-  s0 = s1 = s2 = 0.f;
   for (int e = sl; e < rs; e += G) {
     const int j = e / 3, l = e - 3 * j;
     const float xv = xval(3 * __ldg(bcol + rb + j) + l);
@@ -329,6 +329,10 @@ __device__ __forceinline__ void spmv_row_blk(int v, int sl, const int *__restric
     s1 += __ldcs(r0 + rs + e) * xv;
     s2 += __ldcs(r0 + 2 * rs + e) * xv;
   }
+}
+
+template <int G>
+__device__ __forceinline__ void group_reduce(float &s0, float &s1, float &s2) {
 #pragma unroll
   for (int o = G / 2; o > 0; o >>= 1) {
     s0 += __shfl_xor_sync(0xffffffffu, s0, o);
@@ -337,24 +341,33 @@ __device__ __forceinline__ void spmv_row_blk(int v, int sl, const int *__restric
   }
 }
 
+// Warp-uniform walk over vertex rows: each warp takes 32/G consecutive rows
+// per step, group g of the warp row vb + g (inactive past nV).
+#define BT_ROW_LOOP_BEGIN(G)                                                      \
+  const int lane_ = threadIdx.x & 31, sl = lane_ % (G), gw_ = lane_ / (G);       \
+  const int warp_ = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;                \
+  const int nwarps_ = (gridDim.x * blockDim.x) >> 5;                             \
+  for (int vb_ = warp_ * (32 / (G)); vb_ < nV; vb_ += nwarps_ * (32 / (G))) {    \
+    const int v = vb_ + gw_;                                                      \
+    const bool active = v < nV;
+#define BT_ROW_LOOP_END }
+
 // y = A x with the PCG's row mapping (rows of pinned vertices give 0)
 template <int G>
 __global__ void __launch_bounds__(256)
 k_spmv_blk_g(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, const float *__restrict__ val,
              const float *__restrict__ x, float *__restrict__ y, const unsigned char *__restrict__ pinned) {
-  const int sl = (threadIdx.x & 31) % G;
-  const int group = (blockIdx.x * blockDim.x + threadIdx.x) / G;
-  const int ngroups = (gridDim.x * blockDim.x) / G;
-  for (int v = group; v < nV; v += ngroups) {
-    float s0, s1, s2;
-    spmv_row_blk<G>(v, sl, brp, bcol, val, [&](int c) { return __ldg(x + c); }, s0, s1, s2);
-    if (sl == 0) {
-      if (pinned && pinned[v]) s0 = s1 = s2 = 0.f;
-      y[3 * v] = s0;
-      y[3 * v + 1] = s1;
-      y[3 * v + 2] = s2;
-    }
+  BT_ROW_LOOP_BEGIN(G)
+  float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+  if (active) spmv_row_acc<G>(v, sl, brp, bcol, val, [&](int c) { return __ldg(x + c); }, s0, s1, s2);
+  group_reduce<G>(s0, s1, s2);
+  if (active && sl == 0) {
+    if (pinned && pinned[v]) s0 = s1 = s2 = 0.f;
+    y[3 * v] = s0;
+    y[3 * v + 1] = s1;
+    y[3 * v + 2] = s2;
   }
+  BT_ROW_LOOP_END
 }
 
 // Direction + SpMV, block layout: p = z + beta p_old (computed on the fly for
@@ -370,27 +383,26 @@ k_pcg_spmv_blk(int nV, const int *__restrict__ brp, const int *__restrict__ bcol
   // iteration it reads p_{it-1} from (it odd ? pa : pb) and writes p_it to the other
   const float *p_old = (it & 1) ? pa : pb;
   float *p_new = (it & 1) ? pb : pa;
-  const int sl = (threadIdx.x & 31) % G;
-  const int group = (blockIdx.x * blockDim.x + threadIdx.x) / G;
-  const int ngroups = (gridDim.x * blockDim.x) / G;
   double acc = 0.0;
-  for (int v = group; v < nV; v += ngroups) {
-    float s0, s1, s2;
-    spmv_row_blk<G>(v, sl, brp, bcol, val, [&](int c) { return __ldcg(z + c) + beta * __ldcg(p_old + c); }, s0, s1,
+  BT_ROW_LOOP_BEGIN(G)
+  float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+  if (active)
+    spmv_row_acc<G>(v, sl, brp, bcol, val, [&](int c) { return __ldcg(z + c) + beta * __ldcg(p_old + c); }, s0, s1,
                     s2);
-    if (sl == 0) {
-      float pv[3];
-      for (int k = 0; k < 3; ++k) pv[k] = __ldcg(z + 3 * v + k) + beta * __ldcg(p_old + 3 * v + k);
-      if (pinned && pinned[v]) s0 = s1 = s2 = 0.f;
-      p_new[3 * v] = pv[0];
-      p_new[3 * v + 1] = pv[1];
-      p_new[3 * v + 2] = pv[2];
-      ap[3 * v] = s0;
-      ap[3 * v + 1] = s1;
-      ap[3 * v + 2] = s2;
-      acc += (double)(pv[0] * s0 + pv[1] * s1 + pv[2] * s2);
-    }
+  group_reduce<G>(s0, s1, s2);
+  if (active && sl == 0) {
+    float pv[3];
+    for (int k = 0; k < 3; ++k) pv[k] = __ldcg(z + 3 * v + k) + beta * __ldcg(p_old + 3 * v + k);
+    if (pinned && pinned[v]) s0 = s1 = s2 = 0.f;
+    p_new[3 * v] = pv[0];
+    p_new[3 * v + 1] = pv[1];
+    p_new[3 * v + 2] = pv[2];
+    ap[3 * v] = s0;
+    ap[3 * v + 1] = s1;
+    ap[3 * v + 2] = s2;
+    acc += (double)(pv[0] * s0 + pv[1] * s1 + pv[2] * s2);
   }
+  BT_ROW_LOOP_END
   double s = cta_sum(acc);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
   if (last_block(&st->count)) {
@@ -522,6 +534,7 @@ struct PcgOperator {
   // generic CSR
   int n = 0;
   const int *rp = nullptr, *ci = nullptr;
+  const double *values64 = nullptr;  // exact values for the FP64 refinement residual
 };
 
 struct PcgWork {
@@ -645,7 +658,7 @@ static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double
       BT_LAUNCH(ctx, k_resid_blk64, gs, 256, 0, op.plan->nV, op.plan->brp, op.plan->bcol, op.values, x, b, w.r64,
                 op.pinned, w.part_a);
     } else {
-      BT_LAUNCH(ctx, k_resid_csr64, gs, 256, 0, n, op.rp, op.ci, op.values, x, b, w.r64, w.part_a);
+      BT_LAUNCH(ctx, k_resid_csr64, gs, 256, 0, n, op.rp, op.ci, op.values, op.values64, x, b, w.r64, w.part_a);
     }
     BT_CHECK(reduce_sum(ctx, w.part_a, gs, &w.st->rr));
     double rr = 0.0;
@@ -889,6 +902,7 @@ int csr_search_direction(bartels_ctx ctx, int n, const int *rp, const int *ci, c
   op.rp = drp;
   op.ci = dci;
   op.values = dv32;
+  op.values64 = dv64;
   int s = pcg_solve(ctx, op, n, db, dx, ctx->stage_d, prm, rep);
   BT_CUDA(cudaMemcpyAsync(d, dx, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
   BT_CUDA(cudaStreamSynchronize(ctx->stream));

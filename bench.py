@@ -123,6 +123,23 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+# ------------------------------------------------------------- replicas -------
+def reduce_max_ms(ms, world, device="cpu"):
+    """Max over ranks of the timed region (ms); identity for one process."""
+    if world <= 1:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(newton_its_per_rank, world, ms):
+    """Whole-job Newton iterations per second: every replica runs the same
+    number of iterations; the job takes as long as the slowest replica."""
+    return newton_its_per_rank * world / (ms * 1e-3)
+
+
 # ------------------------------------------------------------ GPU arm ---------
 def run_gpu(args, rank, world):
     import torch
@@ -189,10 +206,7 @@ def run_gpu(args, rank, world):
         torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
     launches = ctx.kernel_launches - launches0
-    if world > 1:
-        t = torch.tensor([ms], dtype=torch.float64, device=f"cuda:{dev}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = reduce_max_ms(ms, world, f"cuda:{dev}")
     pcg_its = rep.pcg_iterations - rep_before[1]
     newton_its = rep.iterations - rep_before[0]
 
@@ -257,8 +271,17 @@ def run_gpu(args, rank, world):
                "h2d_bytes_per_step": h2d // args.e2e_steps, "d2h_bytes_per_step": d2h // args.e2e_steps,
                "newton_iterations": its, "seconds": t}
 
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        counts = {"pcg_per_newton": pcg_its / max(newton_its, 1),
+                  "ls_per_newton": (rep.ls_iterations - rep_before[2]) / max(newton_its, 1)}
+        est, parts, threads, _ = cpu_newton_sample(pb, args, counts)
+        cpu = {"value": 1.0 / est[0], "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": cpu_sample_text(counts, args.n).replace("from the GPU run of the same workload", "from this run"),
+               "components": parts}
+
     out = {
-        "metric": METRIC, "value": newton_its * world / (ms * 1e-3), "unit": UNIT, "n_gpus": world,
+        "metric": METRIC, "value": replica_value(newton_its, world, ms), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / max(newton_its, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded Kuhn cube, gravity)",
@@ -276,7 +299,7 @@ def run_gpu(args, rank, world):
         "kernels": {"dq2_fused_assembly": {"us_per_launch": hess_s * 1e6, "compulsory_bytes": hess_bytes,
                                            "achieved_gbs": hess_bytes / hess_s / 1e9,
                                            "frac": hess_bytes / hess_s / 1e9 / peak}},
-        "clocks": clk.summary(), "gpu_launches": int(launches), "e2e": e2e,
+        "clocks": clk.summary(), "gpu_launches": int(launches), "e2e": e2e, "cpu_baseline": cpu,
         "setup_s": {"plan": t_plan}, "time_steps_completed": state["steps"],
         "stage_seconds": {"gradient": rep.t_gradient, "hessian": rep.t_hessian, "pcg": rep.t_pcg,
                           "linesearch": rep.t_linesearch},
@@ -284,10 +307,79 @@ def run_gpu(args, rank, world):
     return out
 
 
-# --------------------------------------------------------- reference arm ---
+# --------------------------------------------------------- CPU baseline ----
+def cpu_newton_sample(pb, args, counts, reps=1):
+    """Time the FP64 OpenMP CPU restatement (oracle/oracle_baseline.cpp) of one
+    Newton iteration of this workload on the host cores, by components:
+    gradient and energy over all tets, the PSD-projected Hessian assembly over a
+    1/16 slice of the tets (scaled x16), and 20 block-Jacobi PCG iterations on
+    the full 3nV system (scaled to the PCG iteration count per Newton
+    iteration). Returns the estimated seconds per Newton iteration."""
+    from oracle import oracle as o
+    from oracle.baseline import CpuNewton
+    V, E = pb["V"], pb["E"]
+    nV, nT = len(V), len(E)
+    t0 = time.perf_counter()
+    cb = CpuNewton(V, E)
+    t_setup = time.perf_counter() - t0
+    vol = o.volume(V, E)
+    f_g = o.const_ext_force(nV, E, vol, pb["rho"] * pb["gravity"])
+    cb.set(args.model, pb["params"], np.full(nT, pb["rho"]), V.ravel(), np.zeros(3 * nV), f_g, pb["pinned"], 1.0,
+           pb["dt"], pb["dt"], None if args.no_psd else 1e-6)
+    x = np.zeros(3 * nV)
+    slice_t = max(1, nT // 16)
+    est = []
+    parts = {}
+    for _ in range(reps):
+        t = time.perf_counter(); g = cb.gradient(x); t_g = time.perf_counter() - t
+        t = time.perf_counter(); cb.energy(x); t_e = time.perf_counter() - t
+        t = time.perf_counter(); cb.hessian_range(x, 0, slice_t, True); t_h = (time.perf_counter() - t) * nT / slice_t
+        d = np.zeros(3 * nV)
+        t = time.perf_counter(); it, _ = cb.pcg(-g, d, 1e-30, 20); t_p = (time.perf_counter() - t) / max(it, 1)
+        n_pcg, n_ls = counts["pcg_per_newton"], counts["ls_per_newton"]
+        est.append(t_g + t_h + n_pcg * t_p + (1.0 + n_ls) * t_e)
+        parts = {"gradient_s": t_g, "hessian_s": t_h, "pcg_iter_s": t_p, "energy_s": t_e}
+    cb.close()
+    return est, parts, cb.threads, t_setup
+
+
+def cpu_sample_text(counts, n=96):
+    return (f"one Newton iteration of the n={n} workload, FP64 OpenMP restatement: gradient + energy over all "
+            "tets, PSD Hessian assembly over 1/16 of the tets x16, 20 block-Jacobi PCG iterations on the full "
+            f"system x {counts['pcg_per_newton']:.0f} PCG iterations per Newton (count from the GPU run of the "
+            "same workload)")
+
+
+def load_counts(args):
+    try:
+        with open(os.path.join(ROOT, "profiles", "newton_counts.json")) as f:
+            c = json.load(f)
+        if c.get("n") == args.n and c.get("model") == args.model:
+            return c
+    except Exception:
+        pass
+    return {"pcg_per_newton": 1000.0, "ls_per_newton": 0.0, "source": "default"}
+
+
 def run_reference(args):
-    return {"impl": "reference", "metric": METRIC, "unit": UNIT, "higher_is_better": True,
-            "unavailable": "CPU reference arm not wired yet"}
+    """--impl reference: the reference's CPU path (its FP64 restatement; the
+    reference itself needs Eigen/libigl, absent here) on the host cores."""
+    pb = build_problem(args.n, args.model)
+    counts = load_counts(args)
+    cpu_newton_sample(pb, args, counts, reps=max(args.warmup, 0) and 1)
+    est, parts, threads, t_setup = cpu_newton_sample(pb, args, counts, reps=max(args.steps, 1))
+    total = sum(est)
+    value = len(est) / total
+    return {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * total / len(est), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Kuhn cube, gravity)",
+            "config": {"workload": f"implicit-Euler Newton, Neo-Hookean Kuhn cube n={args.n}, dt=0.01, z=0 pinned, "
+                                   "PSD simple_psd_fix 1e-6, block-Jacobi PCG 1e-8", "parallelism": "OpenMP host"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": cpu_sample_text(counts, args.n), "components": parts,
+                             "counts_source": counts.get("source", "profiles/newton_counts.json")},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "setup_s": t_setup}
 
 
 def main():

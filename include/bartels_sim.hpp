@@ -1,0 +1,244 @@
+// bartels_sim.hpp -- header-only C++ layer with the reference's names and
+// argument order (namespace sim, include/linear_tetmesh_*.h of Bartels) over
+// the C ABI in bartels_gpu.h.
+//
+// Matrix arguments are any column-major dense type exposing data(), rows(),
+// cols() (and resize(r, c) for outputs): Eigen::MatrixXd / MatrixXi /
+// VectorXd work as-is, as do the small sim::Dense<T> types below. Sparse
+// outputs are sim::SparseMatrix (compressed arrays; the pattern is symmetric,
+// so outer_ptr/inner_idx read as CSR or CSC) and can be wrapped with
+// Eigen::Map<Eigen::SparseMatrix<double>>.
+//
+// A mesh plan is cached per (V, E) data pointer pair and size, so repeated
+// calls on the same mesh reuse the pattern; element data is uploaded per call
+// as in the reference. Errors throw sim::Error (the reference asserts or
+// exits).
+#pragma once
+
+#include <cstdint>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <tuple>
+#include <type_traits>
+#include <vector>
+
+#include "bartels_gpu.h"
+
+namespace sim {
+
+struct Error : std::runtime_error {
+  int status;
+  Error(int s, const std::string &where)
+      : std::runtime_error(where + ": " + bartels_status_string(s) + " (" + bartels_last_error() + ")"), status(s) {}
+};
+
+inline void check(int s, const char *where) {
+  if (s != BARTELS_OK) throw Error(s, where);
+}
+
+enum SolverExitStatus { CONVERGED = BARTELS_CONVERGED, MAX_ITERATIONS_REACHED = BARTELS_MAX_ITERATIONS_REACHED };
+
+// Minimal column-major dense matrix for callers without Eigen.
+template <class T>
+struct Dense {
+  std::vector<T> v;
+  int r = 0, c = 0;
+  Dense() = default;
+  Dense(int rows, int cols) : v((size_t)rows * cols), r(rows), c(cols) {}
+  T *data() { return v.data(); }
+  const T *data() const { return v.data(); }
+  int rows() const { return r; }
+  int cols() const { return c; }
+  void resize(int rows, int cols) {
+    r = rows;
+    c = cols;
+    v.assign((size_t)rows * cols, T(0));
+  }
+  T &operator()(int i, int j) { return v[i + (size_t)r * j]; }
+  const T &operator()(int i, int j) const { return v[i + (size_t)r * j]; }
+  T &operator()(int i) { return v[i]; }
+};
+using MatrixXd = Dense<double>;
+using MatrixXi = Dense<int>;
+using VectorXd = Dense<double>;
+
+struct SparseMatrix {
+  int n_rows = 0, n_cols = 0;
+  std::vector<int> outer_ptr, inner_idx;
+  std::vector<double> values;
+  int rows() const { return n_rows; }
+  int cols() const { return n_cols; }
+  int64_t nonZeros() const { return (int64_t)values.size(); }
+};
+
+// One context for the process (the C ABI allows one per host thread).
+inline bartels_ctx context() {
+  static bartels_ctx ctx = [] {
+    bartels_ctx c = nullptr;
+    check(bartels_ctx_create(0, &c), "bartels_ctx_create");
+    return c;
+  }();
+  return ctx;
+}
+
+namespace detail {
+template <class MV, class ME>
+bartels_mesh_plan plan_for(const MV &V, const ME &E) {
+  static std::map<std::tuple<const void *, const void *, int, int>, bartels_mesh_plan> cache;
+  auto key = std::make_tuple((const void *)V.data(), (const void *)E.data(), (int)V.rows(), (int)E.rows());
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  bartels_mesh_plan p = nullptr;
+  check(bartels_plan_create(context(), (int)V.rows(), V.data(), (int)E.rows(), E.data(), &p), "bartels_plan_create");
+  cache[key] = p;
+  return p;
+}
+template <class Out>
+void copy_pattern(SparseMatrix &S, bartels_mesh_plan p, int n, int64_t nnz) {
+  S.n_rows = S.n_cols = n;
+  S.outer_ptr.resize(n + 1);
+  S.inner_idx.resize(nnz);
+  check(bartels_plan_csr_pattern(p, S.outer_ptr.data(), S.inner_idx.data()), "bartels_plan_csr_pattern");
+}
+}  // namespace detail
+
+// element-matrix callback replacements (src/linear_tetmesh_neohookean_dq2.cpp:22)
+struct default_callback_t {};
+struct simple_psd_fix_t {
+  double tol = 1e-6;  // include/simple_psd_fix.h:11
+};
+inline simple_psd_fix_t simple_psd_fix(double tol = 1e-6) { return simple_psd_fix_t{tol}; }
+
+// linear_tetmesh_dphi_dX, include/linear_tetmesh_dphi_dX.h
+template <class MR, class MV, class ME>
+void linear_tetmesh_dphi_dX(MR &dX, const MV &V, const ME &E) {
+  dX.resize((int)E.rows(), 12);
+  check(bartels_tetmesh_dphi_dX(context(), (int)V.rows(), V.data(), (int)E.rows(), E.data(), dX.data()),
+        "bartels_tetmesh_dphi_dX");
+}
+
+#define BARTELS_SIM_MODEL(name, id)                                                                                \
+  template <class MV, class ME, class MQ, class MD, class MVol, class MP>                                          \
+  double linear_tetmesh_##name##_q(const MV &V, const ME &E, const MQ &q, const MD &dphidX, const MVol &volume,   \
+                                   const MP &params) {                                                             \
+    double e = 0;                                                                                                  \
+    check(bartels_tetmesh_q(context(), detail::plan_for(V, E), id, q.data(), dphidX.data(), volume.data(),         \
+                            params.data(), &e),                                                                    \
+          "linear_tetmesh_" #name "_q");                                                                           \
+    return e;                                                                                                      \
+  }                                                                                                                \
+  template <class MG, class MV, class ME, class MQ, class MD, class MVol, class MP>                                \
+  void linear_tetmesh_##name##_dq(MG &g, const MV &V, const ME &E, const MQ &q, const MD &dphidX,                  \
+                                  const MVol &volume, const MP &params) {                                          \
+    g.resize(3 * (int)V.rows(), 1);                                                                                \
+    check(bartels_tetmesh_dq(context(), detail::plan_for(V, E), id, q.data(), dphidX.data(), volume.data(),        \
+                             params.data(), g.data()),                                                             \
+          "linear_tetmesh_" #name "_dq");                                                                          \
+  }                                                                                                                \
+  template <class MV, class ME, class MQ, class MD, class MVol, class MP, class CB = default_callback_t>            \
+  void linear_tetmesh_##name##_dq2(SparseMatrix &H, const MV &V, const ME &E, const MQ &q, const MD &dphidX,       \
+                                   const MVol &volume, const MP &params, const CB &cb = CB()) {                    \
+    bartels_mesh_plan p = detail::plan_for(V, E);                                                                  \
+    int n = 0;                                                                                                     \
+    int64_t nnz = 0;                                                                                               \
+    check(bartels_plan_csr_size(p, &n, &nnz), "bartels_plan_csr_size");                                            \
+    detail::copy_pattern<SparseMatrix>(H, p, n, nnz);                                                              \
+    H.values.resize(nnz);                                                                                          \
+    int psd = BARTELS_PSD_NONE;                                                                                    \
+    double tol = 0.0;                                                                                              \
+    if constexpr (std::is_same<CB, simple_psd_fix_t>::value) {                                                     \
+      psd = BARTELS_PSD_SIMPLE_FIX;                                                                                \
+      tol = cb.tol;                                                                                                \
+    }                                                                                                              \
+    check(bartels_tetmesh_dq2(context(), p, id, q.data(), dphidX.data(), volume.data(), params.data(), psd, tol, 0, \
+                              H.values.data()),                                                                    \
+          "linear_tetmesh_" #name "_dq2");                                                                         \
+  }
+
+BARTELS_SIM_MODEL(neohookean, BARTELS_NEOHOOKEAN)
+BARTELS_SIM_MODEL(stvk, BARTELS_STVK)
+BARTELS_SIM_MODEL(corotational, BARTELS_COROTATIONAL)
+#undef BARTELS_SIM_MODEL
+
+// linear_tetmesh_mass_matrix, include/linear_tetmesh_mass_matrix.h
+template <class MV, class ME, class MD, class MVol>
+void linear_tetmesh_mass_matrix(SparseMatrix &M, const MV &V, const ME &E, const MD &density, const MVol &volume) {
+  bartels_mesh_plan p = detail::plan_for(V, E);
+  int n = 0;
+  int64_t nnz = 0;
+  check(bartels_plan_csr_size(p, &n, &nnz), "bartels_plan_csr_size");
+  detail::copy_pattern<SparseMatrix>(M, p, n, nnz);
+  M.values.resize(nnz);
+  check(bartels_tetmesh_mass_matrix(context(), p, density.data(), volume.data(), M.values.data()),
+        "linear_tetmesh_mass_matrix");
+}
+
+// linear_tetmesh_const_ext_force, include/linear_tetmesh_const_ext_force.h
+template <class MF, class MV, class ME, class MVol, class MT>
+void linear_tetmesh_const_ext_force(MF &f, const MV &V, const ME &E, const MVol &volume, const MT &traction) {
+  f.resize(3 * (int)V.rows(), 1);
+  check(bartels_tetmesh_const_ext_force(context(), detail::plan_for(V, E), volume.data(), traction.data(), f.data()),
+        "linear_tetmesh_const_ext_force");
+}
+
+// fixed_point_constraint_matrix, include/fixed_point_constraint_matrix.h
+template <class MV, class MI>
+void fixed_point_constraint_matrix(SparseMatrix &P, const MV &V, const MI &fixed_indices) {
+  int rows = 0;
+  const int nfix = (int)(fixed_indices.rows() * fixed_indices.cols());
+  check(bartels_fixed_point_constraint_matrix((int)V.rows(), (int)V.cols(), fixed_indices.data(), nfix, &rows,
+                                              nullptr, nullptr, nullptr),
+        "fixed_point_constraint_matrix");
+  P.n_rows = rows;
+  P.n_cols = (int)(V.rows() * V.cols());
+  P.outer_ptr.resize(rows + 1);
+  P.inner_idx.resize(rows);
+  P.values.resize(rows);
+  check(bartels_fixed_point_constraint_matrix((int)V.rows(), (int)V.cols(), fixed_indices.data(), nfix, &rows,
+                                              P.outer_ptr.data(), P.inner_idx.data(), P.values.data()),
+        "fixed_point_constraint_matrix");
+}
+
+// search_direction_newton_sparse, include/search_direction_newton_sparse.h:8-12.
+// The solver argument selects PCG parameters (the reference's SparseLU is
+// replaced by GPU PCG); returns false where solver.info() != Success.
+struct PCGSolver {
+  bartels_pcg_params params;
+  bartels_pcg_report report{};
+  PCGSolver() { bartels_pcg_default_params(&params); }
+};
+template <class MD, class MG>
+bool search_direction_newton_sparse(MD &d, const MG &g, const SparseMatrix &H, PCGSolver &solver) {
+  d.resize((int)g.rows(), 1);
+  const int s = bartels_search_direction_newton_sparse(context(), H.rows(), H.outer_ptr.data(), H.inner_idx.data(),
+                                                       H.values.data(), g.data(), d.data(), &solver.params,
+                                                       &solver.report);
+  if (s == BARTELS_E_NOT_CONVERGED) return false;
+  check(s, "search_direction_newton_sparse");
+  return true;
+}
+
+// linesearch_backtracking_bisection, include/linesearch_backtracking_bisection.h:23-33
+template <class MX, class Objective>
+SolverExitStatus linesearch_backtracking_bisection(MX &x, const MX &d, const Objective &f, const MX &g,
+                                                   unsigned int max_iterations, double alpha, double c, double p) {
+  struct Thunk {
+    const Objective *f;
+    int rows, cols;
+    static double call(const double *xp, int n, void *u) {
+      auto *t = static_cast<Thunk *>(u);
+      MX tmp;
+      tmp.resize(t->rows, t->cols);
+      for (int i = 0; i < n; ++i) tmp.data()[i] = xp[i];
+      return (*t->f)(tmp);
+    }
+  } th{&f, (int)x.rows(), (int)x.cols()};
+  int status = 0;
+  check(bartels_linesearch_backtracking_bisection((int)(x.rows() * x.cols()), x.data(), d.data(), &Thunk::call, &th,
+                                                  g.data(), (int)max_iterations, alpha, c, p, &status, nullptr),
+        "linesearch_backtracking_bisection");
+  return status == BARTELS_CONVERGED ? CONVERGED : MAX_ITERATIONS_REACHED;
+}
+
+}  // namespace sim

@@ -633,7 +633,16 @@ inline void element_dq2(int model, double *K /*12x12 col-major*/, const double *
 // (reference: Eigen::SelfAdjointEigenSolver, reading the lower triangle), every
 // eigenvalue below tol set to tol, A = Q diag Q^T. Cyclic Jacobi here.
 inline void psd_fix(double *A, int n, double tol) {
-  std::vector<double> M(n * n), Q(n * n, 0.0);
+  double Mbuf[144], Qbuf[144];
+  std::vector<double> Mv, Qv;
+  double *M = Mbuf, *Q = Qbuf;
+  if (n > 12) {
+    Mv.resize(n * n);
+    Qv.resize(n * n);
+    M = Mv.data();
+    Q = Qv.data();
+  }
+  for (int i = 0; i < n * n; ++i) Q[i] = 0.0;
   for (int i = 0; i < n; ++i)
     for (int j = 0; j < n; ++j) M[i + n * j] = (i >= j) ? A[i + n * j] : A[j + n * i];
   for (int i = 0; i < n; ++i) Q[i + n * i] = 1.0;
@@ -669,7 +678,9 @@ inline void psd_fix(double *A, int n, double tol) {
         }
       }
   }
-  std::vector<double> lam(n);
+  std::vector<double> lamv(n > 144 ? n : 0);
+  double lamb[144];
+  double *lam = n > 144 ? lamv.data() : lamb;
   for (int i = 0; i < n; ++i) lam[i] = std::max(M[i + n * i], tol);
   for (int i = 0; i < n; ++i)
     for (int j = 0; j < n; ++j) {

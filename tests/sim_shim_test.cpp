@@ -1,0 +1,134 @@
+// C++ caller of the sim:: layer (include/bartels_sim.hpp) written the way a
+// user of the reference's headers would: builds a 2x2x2 Kuhn cube, evaluates
+// q / dq / dq2 (with simple_psd_fix), mass, force, the constraint matrix, a
+// search direction and a line search, and checks them against each other.
+// Prints "sim shim ok" and returns 0 on success.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+
+#include "bartels_sim.hpp"
+
+#define REQUIRE(c)                                                   \
+  do {                                                               \
+    if (!(c)) {                                                      \
+      std::fprintf(stderr, "check failed: %s (line %d)\n", #c, __LINE__); \
+      return 1;                                                      \
+    }                                                                \
+  } while (0)
+
+int main() {
+  const int n = 2, m = n + 1;
+  sim::MatrixXd V(m * m * m, 3);
+  for (int k = 0; k < m; ++k)
+    for (int j = 0; j < m; ++j)
+      for (int i = 0; i < m; ++i) {
+        const int v = i + m * (j + m * k);
+        V(v, 0) = i * 0.5;
+        V(v, 1) = j * 0.5;
+        V(v, 2) = k * 0.5;
+      }
+  // 6 Kuhn tets per cell along the (0,0,0)-(1,1,1) diagonal, positively oriented
+  const int perms[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+  const int sgn[6] = {1, -1, -1, 1, 1, -1};
+  const int step[3] = {1, m, m * m};
+  sim::MatrixXi E(6 * n * n * n, 4);
+  int t = 0;
+  for (int k = 0; k < n; ++k)
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i)
+        for (int p = 0; p < 6; ++p) {
+          const int p0 = i + m * (j + m * k), p1 = p0 + step[perms[p][0]], p2 = p1 + step[perms[p][1]],
+                    p3 = p2 + step[perms[p][2]];
+          E(t, 0) = p0;
+          E(t, 1) = sgn[p] > 0 ? p1 : p2;
+          E(t, 2) = sgn[p] > 0 ? p2 : p1;
+          E(t, 3) = p3;
+          ++t;
+        }
+  const int nV = V.rows(), nT = E.rows();
+  sim::MatrixXd dphidX;
+  sim::linear_tetmesh_dphi_dX(dphidX, V, E);
+  REQUIRE(dphidX.rows() == nT && dphidX.cols() == 12);
+  sim::VectorXd vol(nT, 1), density(nT, 1);
+  for (int e = 0; e < nT; ++e) {
+    vol(e) = 0.125 / 6.0;
+    density(e) = 1000.0;
+  }
+  const double Y = 2e6, nu = 0.45, lam = Y * nu / ((1 + nu) * (1 - 2 * nu)), mu = Y / (2 * (1 + nu));
+  sim::MatrixXd params(nT, 2);
+  for (int e = 0; e < nT; ++e) {
+    params(e, 0) = 0.5 * mu;
+    params(e, 1) = 0.5 * lam;
+  }
+  sim::VectorXd q(3 * nV, 1);
+  for (int v = 0; v < nV; ++v)
+    for (int d = 0; d < 3; ++d) q(3 * v + d) = V(v, d) * (d == 2 ? 0.97 : 1.01) + 0.003 * std::sin(7.0 * v + d);
+
+  const double e0 = sim::linear_tetmesh_neohookean_q(V, E, q, dphidX, vol, params);
+  sim::VectorXd g;
+  sim::linear_tetmesh_neohookean_dq(g, V, E, q, dphidX, vol, params);
+  REQUIRE(std::isfinite(e0) && e0 > 0);
+  // gradient against centred differences of the energy (src/finite_differences.cpp:42-80)
+  for (int i = 0; i < 3 * nV; i += 7) {
+    const double h = 1e-6;
+    sim::VectorXd qp = q, qm = q;
+    qp(i) += h;
+    qm(i) -= h;
+    const double fd = (sim::linear_tetmesh_neohookean_q(V, E, qp, dphidX, vol, params) -
+                       sim::linear_tetmesh_neohookean_q(V, E, qm, dphidX, vol, params)) /
+                      (2 * h);
+    REQUIRE(std::fabs(fd - g(i)) <= 1e-4 * (std::fabs(g(i)) + 1.0));
+  }
+  sim::SparseMatrix H;
+  sim::linear_tetmesh_neohookean_dq2(H, V, E, q, dphidX, vol, params, sim::simple_psd_fix(1e-6));
+  REQUIRE(H.rows() == 3 * nV && H.nonZeros() == H.outer_ptr.back());
+  sim::SparseMatrix M;
+  sim::linear_tetmesh_mass_matrix(M, V, E, density, vol);
+  double msum = 0;
+  for (double v : M.values) msum += v;
+  REQUIRE(std::fabs(msum - 3 * 1000.0) < 1e-9);  // 3 x total mass
+  sim::VectorXd f;
+  sim::VectorXd traction(3, 1);
+  traction(2) = -9810.0;
+  sim::linear_tetmesh_const_ext_force(f, V, E, vol, traction);
+  double fz = 0;
+  for (int v = 0; v < nV; ++v) fz += f(3 * v + 2);
+  REQUIRE(std::fabs(fz + 9810.0) < 1e-8);
+  sim::MatrixXi fixed(m * m, 1);
+  for (int i = 0; i < m * m; ++i) fixed(i) = i;  // the z = 0 face
+  sim::SparseMatrix P;
+  sim::fixed_point_constraint_matrix(P, V, fixed);
+  REQUIRE(P.rows() == 3 * (nV - m * m) && P.cols() == 3 * nV);
+  // search direction on H + M (SPD), residual check
+  sim::SparseMatrix A = H;
+  for (size_t k = 0; k < A.values.size(); ++k) A.values[k] += M.values[k];
+  sim::PCGSolver solver;
+  sim::VectorXd d;
+  REQUIRE(sim::search_direction_newton_sparse(d, g, A, solver));
+  double rr = 0, gg = 0;
+  for (int i = 0; i < A.rows(); ++i) {
+    double s = 0;
+    for (int k = A.outer_ptr[i]; k < A.outer_ptr[i + 1]; ++k) s += A.values[k] * d(A.inner_idx[k]);
+    rr += (s + g(i)) * (s + g(i));
+    gg += g(i) * g(i);
+  }
+  REQUIRE(std::sqrt(rr) <= 2e-8 * std::sqrt(gg));
+  // line search along -g on a quadratic
+  auto quad = [&](const sim::VectorXd &x) {
+    double s = 0;
+    for (int i = 0; i < x.rows(); ++i) s += 0.5 * x.data()[i] * x.data()[i];
+    return s;
+  };
+  sim::VectorXd x(4, 1), gx(4, 1), dx(4, 1);
+  for (int i = 0; i < 4; ++i) {
+    x(i) = 1.0 + i;
+    gx(i) = x(i);
+    dx(i) = -3.0 * x(i);
+  }
+  REQUIRE(sim::linesearch_backtracking_bisection(x, dx, quad, gx, 100, 1.0, 1e-4, 0.5) == sim::CONVERGED);
+  REQUIRE(std::fabs(x(0) - (1.0 - 1.5)) < 1e-12);
+  std::printf("sim shim ok: energy %.6e, nnz %lld, pcg iterations %d\n", e0, (long long)H.nonZeros(),
+              solver.report.iterations);
+  return 0;
+}

@@ -106,3 +106,20 @@ def test_kuhn_cube_counts_and_pattern(oracle, n):
     assert np.allclose(vol, 1.0 / (6 * n ** 3), rtol=1e-12)
     M = oracle.mass_matrix(len(V), E, np.ones(len(E)), vol)
     assert M.nnz == c["nnz"]
+
+
+def build_sim_shim_test():
+    """g++ build of tests/sim_shim_test.cpp against include/bartels_sim.hpp and the library."""
+    import subprocess
+    out_dir = os.path.join(ROOT, "tests", "_build")
+    os.makedirs(out_dir, exist_ok=True)
+    exe = os.path.join(out_dir, "sim_shim_test")
+    libdir = os.path.join(ROOT, "bartels_gb300", "lib")
+    subprocess.check_call(["g++", "-std=c++17", "-O1", os.path.join(ROOT, "tests", "sim_shim_test.cpp"), "-I",
+                           os.path.join(ROOT, "include"), "-L", libdir, "-lbartels_gpu", f"-Wl,-rpath,{libdir}",
+                           "-o", exe])
+    return exe
+
+
+def test_sim_shim_compiles():
+    assert os.path.exists(build_sim_shim_test())

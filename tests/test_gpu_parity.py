@@ -280,3 +280,12 @@ def test_device_hessian_and_spmv(oracle):
         ctx2.close()
         ctx.close()
     os.environ.pop("BARTELS_SPMV_LANES", None)
+
+
+def test_sim_shim_cpp_program():
+    """The C++ sim:: layer (include/bartels_sim.hpp) driven like the reference's headers."""
+    import subprocess
+    from test_capi import build_sim_shim_test
+    r = subprocess.run([build_sim_shim_test()], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "sim shim ok" in r.stdout
