@@ -10,8 +10,11 @@ calls exit()).
 """
 from __future__ import annotations
 
+import atexit
 import ctypes as C
 import hashlib
+import sys
+import weakref
 from collections import OrderedDict
 
 import numpy as np
@@ -41,15 +44,19 @@ def _colmajor(a, dtype):
 
 
 class Context:
-    """A device, a stream and workspace (bartels_ctx)."""
+    """A device, a stream and workspace (bartels_ctx). Plans created on a
+    context are destroyed before it (the C ABI requires that order)."""
 
     _default = None
+    _live: "weakref.WeakSet[Context]" = weakref.WeakSet()
 
     def __init__(self, device: int = 0):
         h = C.c_void_p()
         check(lib().bartels_ctx_create(device, C.byref(h)), "bartels_ctx_create")
         self.handle = h
         self.device = device
+        self._plans: "weakref.WeakSet[MeshPlan]" = weakref.WeakSet()
+        Context._live.add(self)
 
     @classmethod
     def default(cls) -> "Context":
@@ -66,14 +73,29 @@ class Context:
 
     def close(self):
         if self.handle:
+            for p in list(self._plans):
+                p.close()
             lib().bartels_ctx_destroy(self.handle)
             self.handle = None
 
     def __del__(self):
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:
             pass
+
+
+@atexit.register
+def _close_all():
+    """Destroy plans, then contexts, before the interpreter tears down."""
+    for p in list(_plans.values()):
+        p.close()
+    _plans.clear()
+    for c in list(Context._live):
+        c.close()
+    Context._default = None
 
 
 class MeshPlan:
@@ -92,6 +114,7 @@ class MeshPlan:
         check(lib().bartels_plan_create(self.ctx.handle, self.nV, _dptr(vcm), self.nT, _iptr(ecm), C.byref(h)),
               "bartels_plan_create")
         self.handle = h
+        self.ctx._plans.add(self)
         n = C.c_int()
         nnz = C.c_int64()
         check(lib().bartels_plan_csr_size(h, C.byref(n), C.byref(nnz)), "bartels_plan_csr_size")
@@ -198,11 +221,13 @@ class MeshPlan:
         return xa, rep
 
     def close(self):
-        if getattr(self, "handle", None):
+        if getattr(self, "handle", None) and getattr(self.ctx, "handle", None):
             lib().bartels_plan_destroy(self.handle)
-            self.handle = None
+        self.handle = None
 
     def __del__(self):
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:

@@ -84,6 +84,7 @@ const char *bartels_last_error(void);
 /* One context per host thread: a device, a stream, workspace and a pinned
  * staging area. All work is ordered on the context's stream. */
 int bartels_ctx_create(int device, bartels_ctx *out);
+/* Destroy every plan created on ctx before destroying ctx. */
 int bartels_ctx_destroy(bartels_ctx ctx);
 int bartels_ctx_synchronize(bartels_ctx ctx);
 /* The context's cudaStream_t, as void*. */
