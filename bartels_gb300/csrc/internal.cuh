@@ -87,7 +87,7 @@ struct bartels_ctx_s {
   int64_t launches = 0;
   // lanes per vertex row in the block-layout SpMV (4, 8 or 16; tuned per GPU,
   // overridable with BARTELS_SPMV_LANES)
-  int spmv_lanes = 8;
+  int spmv_lanes = 16;
   // pinned host staging for small read-backs
   double *host_scalars = nullptr;
   // device scratch for reductions

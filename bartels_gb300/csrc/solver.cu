@@ -30,10 +30,11 @@ constexpr int kSpmvBlocksPerSM = 8;
 // Device-side PCG scalars. Reductions finish in the last block of the kernel
 // that produces them (fixed summation order), so consumers read scalars.
 struct PcgState {
-  double rz, rz_prev;   // r.z of the current and previous iterate
+  double rz;            // r.z of the current iterate
   double rr;            // r.r of the current iterate
   double pap;           // p.Ap of the current direction
   double rr0, tol2;
+  float alpha, beta;    // step and direction coefficients, computed once by the last block
   int it;               // iterations completed in the current inner solve
   int done;
   int max_it;
@@ -257,6 +258,25 @@ __device__ __forceinline__ bool last_block(unsigned int *count) {
   return am_last;
 }
 
+// Block sum of per-thread FP32 partials: FP32 within a warp (fixed shuffle
+// tree), FP64 across warps. Valid in thread 0. Keeps the FP64 pipe (1/64 of
+// FP32 on GB300) off the per-element path.
+__device__ __forceinline__ double cta_sum_f(float v) {
+  __shared__ double redf[32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) redf[w] = (double)v;
+  __syncthreads();
+  double s = 0.0;
+  if (w == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    s = lane < nw ? redf[lane] : 0.0;
+    s = warp_sum(s);
+  }
+  __syncthreads();
+  return s;
+}
+
 // deterministic sum of n partials (fixed order), valid in thread 0
 __device__ __forceinline__ double sum_partials(const double *a, int n) {
   double acc = 0.0;
@@ -270,7 +290,7 @@ __global__ void k_pcg_init(int nb, int n, const double *__restrict__ r64, const 
                            float *__restrict__ p0, float *__restrict__ p1, double *__restrict__ part_a,
                            double *__restrict__ part_b, PcgState *__restrict__ st, double inner_rel2, double abs_tol2,
                            int max_it) {
-  double arz = 0.0, arr = 0.0;
+  float arz = 0.f, arr = 0.f;
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nb; v += gridDim.x * blockDim.x) {
     float rv[3], zv[3];
     for (int k = 0; k < 3; ++k) rv[k] = (3 * v + k < n) ? (float)r64[3 * v + k] : 0.f;
@@ -283,24 +303,25 @@ __global__ void k_pcg_init(int nb, int n, const double *__restrict__ r64, const 
         z[i] = zv[k];
         p0[i] = 0.f;
         p1[i] = 0.f;
-        arz += (double)rv[k] * zv[k];
-        arr += (double)rv[k] * rv[k];
+        arz += rv[k] * zv[k];
+        arr += rv[k] * rv[k];
       }
     }
   }
-  double s = cta_sum(arz);
+  double s = cta_sum_f(arz);
   if (threadIdx.x == 0) part_a[blockIdx.x] = s;
-  s = cta_sum(arr);
+  s = cta_sum_f(arr);
   if (threadIdx.x == 0) part_b[blockIdx.x] = s;
   if (last_block(&st->count)) {
     const double rz = sum_partials(part_a, gridDim.x);
     const double rr = sum_partials(part_b, gridDim.x);
     if (threadIdx.x == 0) {
       st->rz = rz;
-      st->rz_prev = rz;
       st->rr = rr;
       st->rr0 = rr;
       st->pap = 0.0;
+      st->alpha = 0.f;
+      st->beta = 0.f;
       st->tol2 = fmax(inner_rel2 * rr, abs_tol2);
       st->it = 0;
       st->max_it = max_it;
@@ -379,11 +400,11 @@ k_pcg_spmv_blk(int nV, const int *__restrict__ brp, const int *__restrict__ bcol
                const unsigned char *__restrict__ pinned, double *__restrict__ part, PcgState *__restrict__ st) {
   if (st->done) return;
   const int it = st->it;
-  const float beta = it == 0 ? 0.f : (float)(st->rz / st->rz_prev);
+  const float beta = st->beta;
   // iteration it reads p_{it-1} from (it odd ? pa : pb) and writes p_it to the other
   const float *p_old = (it & 1) ? pa : pb;
   float *p_new = (it & 1) ? pb : pa;
-  double acc = 0.0;
+  float acc = 0.f;
   BT_ROW_LOOP_BEGIN(G)
   float s0 = 0.f, s1 = 0.f, s2 = 0.f;
   if (active)
@@ -400,15 +421,16 @@ k_pcg_spmv_blk(int nV, const int *__restrict__ brp, const int *__restrict__ bcol
     ap[3 * v] = s0;
     ap[3 * v + 1] = s1;
     ap[3 * v + 2] = s2;
-    acc += (double)(pv[0] * s0 + pv[1] * s1 + pv[2] * s2);
+    acc += pv[0] * s0 + pv[1] * s1 + pv[2] * s2;
   }
   BT_ROW_LOOP_END
-  double s = cta_sum(acc);
+  double s = cta_sum_f(acc);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
   if (last_block(&st->count)) {
     const double pap = sum_partials(part, gridDim.x);
     if (threadIdx.x == 0) {
       st->pap = pap;
+      st->alpha = (float)(st->rz / pap);
       st->count = 0;
     }
   }
@@ -421,13 +443,13 @@ k_pcg_spmv_csr(int n, const int *__restrict__ rp, const int *__restrict__ ci, co
                double *__restrict__ part, PcgState *__restrict__ st) {
   if (st->done) return;
   const int it = st->it;
-  const float beta = it == 0 ? 0.f : (float)(st->rz / st->rz_prev);
+  const float beta = st->beta;
   const float *p_old = (it & 1) ? pa : pb;
   float *p_new = (it & 1) ? pb : pa;
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  double acc = 0.0;
+  float acc = 0.f;
   for (int i = warp; i < n; i += nwarps) {
     float s = 0.f;
     for (int k = rp[i] + lane; k < rp[i + 1]; k += 32) {
@@ -439,22 +461,46 @@ k_pcg_spmv_csr(int n, const int *__restrict__ rp, const int *__restrict__ ci, co
       const float pv = __ldcg(z + i) + beta * __ldcg(p_old + i);
       p_new[i] = pv;
       ap[i] = s;
-      acc += (double)(pv * s);
+      acc += pv * s;
     }
   }
-  double s = cta_sum(acc);
+  double s = cta_sum_f(acc);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
   if (last_block(&st->count)) {
     const double pap = sum_partials(part, gridDim.x);
     if (threadIdx.x == 0) {
       st->pap = pap;
+      st->alpha = (float)(st->rz / pap);
       st->count = 0;
     }
   }
 }
 
 // alpha = rz / pAp; x += alpha p; r -= alpha Ap; z = M^-1 r; r.z and r.r;
-// convergence test and iteration count in the last block.
+// convergence test, beta and iteration count in the last block. One thread
+// per group of 4 vertices (12 floats = 3 aligned float4 per vector, 24 floats
+// = 6 float4 of block-Jacobi); the ragged tail is handled per vertex.
+__device__ __forceinline__ void update_vertex(int v, float alpha, const float *__restrict__ minv,
+                                              const float *__restrict__ p, const float *__restrict__ ap,
+                                              float *__restrict__ x, float *__restrict__ r, float *__restrict__ z,
+                                              float &arz, float &arr) {
+  float rv[3], zv[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int i = 3 * v + k;
+    x[i] += alpha * __ldcg(p + i);
+    rv[k] = r[i] - alpha * __ldcg(ap + i);
+    r[i] = rv[k];
+  }
+  apply_minv(minv, v, rv, zv);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    z[3 * v + k] = zv[k];
+    arz += rv[k] * zv[k];
+    arr += rv[k] * rv[k];
+  }
+}
+
 __global__ void __launch_bounds__(256)
 k_pcg_update(int nb, int n, const float *__restrict__ minv, const float *__restrict__ pa,
              const float *__restrict__ pb, const float *__restrict__ ap, float *__restrict__ x,
@@ -463,41 +509,85 @@ k_pcg_update(int nb, int n, const float *__restrict__ minv, const float *__restr
   if (st->done) return;
   const int it = st->it;
   const float *p = (it & 1) ? pb : pa;
-  const float alpha = (float)(st->rz / st->pap);
-  double arz = 0.0, arr = 0.0;
-  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nb; v += gridDim.x * blockDim.x) {
-    float rv[3], zv[3];
+  const float alpha = st->alpha;
+  float arz = 0.f, arr = 0.f;
+  const int nfull = (n % 3 == 0) ? nb / 4 : 0;  // groups of 4 complete vertices (vector path)
+  for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < nfull; g += gridDim.x * blockDim.x) {
+    const float4 *p4 = reinterpret_cast<const float4 *>(p) + 3 * g;
+    const float4 *a4 = reinterpret_cast<const float4 *>(ap) + 3 * g;
+    float4 *x4 = reinterpret_cast<float4 *>(x) + 3 * g;
+    float4 *r4 = reinterpret_cast<float4 *>(r) + 3 * g;
+    float4 *z4 = reinterpret_cast<float4 *>(z) + 3 * g;
+    const float4 *m4 = reinterpret_cast<const float4 *>(minv) + 6 * g;
+    float pv[12], av[12], xv[12], rv[12], mv[24], zv[12];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const int i = 3 * v + k;
-      if (i < n) {
-        x[i] += alpha * __ldcg(p + i);
-        rv[k] = r[i] - alpha * __ldcg(ap + i);
-        r[i] = rv[k];
-      } else {
-        rv[k] = 0.f;
-      }
+    for (int q = 0; q < 3; ++q) {
+      const float4 a = __ldcg(p4 + q), b = __ldcg(a4 + q), c = x4[q], d = r4[q];
+      pv[4 * q] = a.x; pv[4 * q + 1] = a.y; pv[4 * q + 2] = a.z; pv[4 * q + 3] = a.w;
+      av[4 * q] = b.x; av[4 * q + 1] = b.y; av[4 * q + 2] = b.z; av[4 * q + 3] = b.w;
+      xv[4 * q] = c.x; xv[4 * q + 1] = c.y; xv[4 * q + 2] = c.z; xv[4 * q + 3] = c.w;
+      rv[4 * q] = d.x; rv[4 * q + 1] = d.y; rv[4 * q + 2] = d.z; rv[4 * q + 3] = d.w;
     }
-    apply_minv(minv, v, rv, zv);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const int i = 3 * v + k;
-      if (i < n) {
-        z[i] = zv[k];
-        arz += (double)rv[k] * zv[k];
-        arr += (double)rv[k] * rv[k];
-      }
+    for (int q = 0; q < 6; ++q) {
+      const float4 m = __ldg(m4 + q);
+      mv[4 * q] = m.x; mv[4 * q + 1] = m.y; mv[4 * q + 2] = m.z; mv[4 * q + 3] = m.w;
+    }
+#pragma unroll
+    for (int i = 0; i < 12; ++i) {
+      xv[i] += alpha * pv[i];
+      rv[i] -= alpha * av[i];
+    }
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+      const float *m = mv + 6 * w;
+      const float *rr = rv + 3 * w;
+      zv[3 * w] = m[0] * rr[0] + m[3] * rr[1] + m[4] * rr[2];
+      zv[3 * w + 1] = m[3] * rr[0] + m[1] * rr[1] + m[5] * rr[2];
+      zv[3 * w + 2] = m[4] * rr[0] + m[5] * rr[1] + m[2] * rr[2];
+    }
+#pragma unroll
+    for (int i = 0; i < 12; ++i) {
+      arz += rv[i] * zv[i];
+      arr += rv[i] * rv[i];
+    }
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      x4[q] = make_float4(xv[4 * q], xv[4 * q + 1], xv[4 * q + 2], xv[4 * q + 3]);
+      r4[q] = make_float4(rv[4 * q], rv[4 * q + 1], rv[4 * q + 2], rv[4 * q + 3]);
+      z4[q] = make_float4(zv[4 * q], zv[4 * q + 1], zv[4 * q + 2], zv[4 * q + 3]);
     }
   }
-  double s = cta_sum(arz);
+  // tail (and the scalar path when n is not 3 nb)
+  for (int v = 4 * nfull + blockIdx.x * blockDim.x + threadIdx.x; v < nb; v += gridDim.x * blockDim.x) {
+    if (3 * v + 2 < n) {
+      update_vertex(v, alpha, minv, p, ap, x, r, z, arz, arr);
+    } else {
+      float rv[3] = {0.f, 0.f, 0.f}, zv[3];
+      for (int k = 0; k < 3; ++k)
+        if (3 * v + k < n) {
+          x[3 * v + k] += alpha * p[3 * v + k];
+          rv[k] = r[3 * v + k] - alpha * ap[3 * v + k];
+          r[3 * v + k] = rv[k];
+        }
+      apply_minv(minv, v, rv, zv);
+      for (int k = 0; k < 3; ++k)
+        if (3 * v + k < n) {
+          z[3 * v + k] = zv[k];
+          arz += rv[k] * zv[k];
+          arr += rv[k] * rv[k];
+        }
+    }
+  }
+  double s = cta_sum_f(arz);
   if (threadIdx.x == 0) part_a[blockIdx.x] = s;
-  s = cta_sum(arr);
+  s = cta_sum_f(arr);
   if (threadIdx.x == 0) part_b[blockIdx.x] = s;
   if (last_block(&st->count)) {
     const double rz = sum_partials(part_a, gridDim.x);
     const double rr = sum_partials(part_b, gridDim.x);
     if (threadIdx.x == 0) {
-      st->rz_prev = st->rz;
+      st->beta = (float)(rz / st->rz);
       st->rz = rz;
       st->rr = rr;
       st->it = it + 1;
@@ -558,7 +648,7 @@ static int grid_spmv(bartels_ctx ctx, int64_t rows) {
 static int pcg_enqueue_iters(bartels_ctx ctx, const PcgOperator &op, const PcgWork &w, int n, int nb, int iters) {
   const bool blk = op.plan != nullptr;
   const int gs = blk ? grid_spmv(ctx, (int64_t)op.plan->nV * ctx->spmv_lanes / 32 + 1) : grid_spmv(ctx, n);
-  const int gv = grid_vec(ctx, nb);
+  const int gu = grid_vec(ctx, (nb + 3) / 4);
   for (int i = 0; i < iters; ++i) {
     if (blk) {
 #define BT_K1(G)                                                                                                \
@@ -571,7 +661,7 @@ static int pcg_enqueue_iters(bartels_ctx ctx, const PcgOperator &op, const PcgWo
     } else {
       BT_LAUNCH(ctx, k_pcg_spmv_csr, gs, 256, 0, n, op.rp, op.ci, op.values, w.z, w.pa, w.pb, w.ap, w.part_a, w.st);
     }
-    BT_LAUNCH(ctx, k_pcg_update, gv, 256, 0, nb, n, w.minv, w.pa, w.pb, w.ap, w.x, w.r, w.z, w.part_a, w.part_b, w.st);
+    BT_LAUNCH(ctx, k_pcg_update, gu, 256, 0, nb, n, w.minv, w.pa, w.pb, w.ap, w.x, w.r, w.z, w.part_a, w.part_b, w.st);
   }
   return BARTELS_OK;
 }
