@@ -48,7 +48,9 @@ class NewtonReport(C.Structure):
                 ("ls_iterations", C.c_int), ("ls_failures", C.c_int), ("grad_norm0", C.c_double),
                 ("grad_norm", C.c_double), ("energy", C.c_double), ("seconds", C.c_double),
                 ("t_gradient", C.c_double), ("t_hessian", C.c_double), ("t_pcg", C.c_double),
-                ("t_linesearch", C.c_double)]
+                ("t_linesearch", C.c_double), ("last_alpha", C.c_double), ("last_pcg_rel_residual", C.c_double),
+                ("last_pcg_iterations", C.c_int), ("last_pcg_refinements", C.c_int), ("pcg_failures", C.c_int),
+                ("energy_change", C.c_double)]
 
 
 OBJECTIVE_FN = C.CFUNCTYPE(C.c_double, C.POINTER(C.c_double), C.c_int, C.c_void_p)

@@ -474,6 +474,106 @@ BT_HD void pk1_model(int model, const T *F, const T *pv, T *P) {
 }
 
 // ----------------------------------------------------------------------------
+// Cancellation-free energies from the displacement gradient H = F - I.
+// Near the rest state psi = O(|H|^2) while the textbook forms combine O(1)
+// terms (tr F^T F - 3 - 2 ln J), losing ~eps/|H|^2 relative accuracy; here
+// every term is O(|H|^2) from the start.
+// ----------------------------------------------------------------------------
+#ifdef __CUDACC__
+BT_HD double bt_log1p(double x) { return log1p(x); }
+BT_HD double bt_expm1(double x) { return expm1(x); }
+BT_HD float bt_log1p(float x) { return log1pf(x); }
+BT_HD float bt_expm1(float x) { return expm1f(x); }
+#else
+BT_HD double bt_log1p(double x) { return std::log1p(x); }
+BT_HD double bt_expm1(double x) { return std::expm1(x); }
+BT_HD float bt_log1p(float x) { return std::log1p(x); }
+BT_HD float bt_expm1(float x) { return std::expm1(x); }
+#endif
+
+// j - log1p(j) (>= 0), series sum_{k>=2} (-1)^k j^k / k for |j| < 0.02
+template <class T>
+BT_HD T j_minus_log1p(T j) {
+  if (bt_abs(j) < T(0.02)) {
+    T s = T(0);
+#pragma unroll
+    for (int k = 13; k >= 2; --k) s = s * j + ((k % 2 == 0) ? T(1) : T(-1)) / T(k);
+    return s * j * j;
+  }
+  return j - bt_log1p(j);
+}
+// expm1(y) - y, series sum_{k>=2} y^k / k! for |y| < 0.02
+template <class T>
+BT_HD T expm1_minus_y(T y) {
+  if (bt_abs(y) < T(0.02)) {
+    T s = T(0), f = T(1);
+    T c[14];
+    c[0] = T(1);
+#pragma unroll
+    for (int k = 1; k < 14; ++k) {
+      f *= T(k);
+      c[k] = T(1) / f;
+    }
+#pragma unroll
+    for (int k = 13; k >= 2; --k) s = s * y + c[k];
+    return s * y * y;
+  }
+  return bt_expm1(y) - y;
+}
+
+// invariants of H: tr H, |H|^2, q2 = ((tr H)^2 - tr(H H))/2, det H, j = det(I + H) - 1
+template <class T>
+struct DispInv {
+  T tr, nrm2, q2, det, j;
+  BT_HD DispInv(const T *H) {
+    tr = H[0] + H[4] + H[8];
+    nrm2 = T(0);
+    for (int i = 0; i < 9; ++i) nrm2 += H[i] * H[i];
+    T trHH = T(0);
+    for (int i = 0; i < 3; ++i)
+      for (int k = 0; k < 3; ++k) trHH += H[i + 3 * k] * H[k + 3 * i];
+    q2 = T(0.5) * (tr * tr - trHH);
+    det = det3(H);
+    j = tr + q2 + det;
+  }
+};
+
+// psi of the displacement gradient H (F = I + H), scaled by vol via pv
+template <class T>
+BT_HD T psi_model_disp(int model, const T *H, const T *pv) {
+  if (model == MODEL_NH || model == MODEL_NH_ISO) {
+    const DispInv<T> d(H);
+    const T g2 = j_minus_log1p(d.j);  // j - ln J
+    if (model == MODEL_NH)
+      // I1 - 3 - 2 ln J = |H|^2 + 2 (tr H - j) + 2 (j - ln J)
+      return pv[0] * (d.nrm2 - T(2) * (d.q2 + d.det) + T(2) * g2) + pv[1] * d.j * d.j;
+    // J^-2/3 I1 - 3 = 3 g1 + 2 g2 - 2 (q2 + det) + |H|^2 + e (2 tr H + |H|^2),
+    // e = J^-2/3 - 1 = expm1(y), y = -2/3 ln J, g1 = expm1(y) - y
+    const T L = bt_log1p(d.j);
+    const T y = T(-2) / T(3) * L;
+    const T g1 = expm1_minus_y(y);
+    const T e = g1 + y;
+    return pv[0] * (T(3) * g1 + T(2) * g2 - T(2) * (d.q2 + d.det) + d.nrm2 + e * (T(2) * d.tr + d.nrm2)) +
+           pv[1] * d.j * d.j;
+  }
+  if (model == MODEL_STVK) {
+    // E = (H + H^T + H^T H) / 2
+    T E[9];
+    for (int i = 0; i < 3; ++i)
+      for (int k = 0; k < 3; ++k) {
+        T hth = H[0 + 3 * i] * H[0 + 3 * k] + H[1 + 3 * i] * H[1 + 3 * k] + H[2 + 3 * i] * H[2 + 3 * k];
+        E[i + 3 * k] = T(0.5) * (H[i + 3 * k] + H[k + 3 * i] + hth);
+      }
+    T trE = E[0] + E[4] + E[8], trEE = T(0);
+    for (int i = 0; i < 9; ++i) trEE += E[i] * E[i];
+    return pv[1] * trEE + T(0.5) * pv[0] * trE * trE;
+  }
+  T F[9];
+  for (int i = 0; i < 9; ++i) F[i] = H[i] + ((i % 4) == 0 ? T(1) : T(0));
+  return psi_model(model, F, pv);
+}
+
+// ----------------------------------------------------------------------------
 // PSD projection helpers for one element (simple_psd_fix, src/simple_psd_fix.cpp)
 // K = B^T S B with B = Phi^T (x) I3 (Phi = 4x3 stack of phi_a^T). The
 // translations span null(B) and are eigenvectors of K with eigenvalue 0, so

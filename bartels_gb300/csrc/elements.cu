@@ -159,34 +159,56 @@ __global__ void k_prep_u(int nV, const double *__restrict__ x, const double *__r
 }
 
 // ---------------------------------------------------------- FP64 energy -----
+// Displacement gradient H = F - I of tet r at positions q = q_base + scale x,
+// from FP64 displacements u = q - X when the element data belongs to the rest
+// shape X (exact rest: H = 0), else F - I from positions.
+__device__ __forceinline__ void disp_grad64(const TetRec64 &r, const double *__restrict__ x,
+                                            const double *__restrict__ q_base, double scale,
+                                            const double *__restrict__ X, const double *__restrict__ dx,
+                                            double alpha, double *H) {
+  const int id[4] = {r.idx.x, r.idx.y, r.idx.z, r.idx.w};
+  double u[4][3];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const int i = 3 * id[a] + d;
+      double xv = x[i];
+      if (dx) xv += alpha * dx[i];
+      double base = q_base ? q_base[i] : 0.0;
+      if (X) base -= X[i];
+      u[a][d] = base + scale * xv;
+    }
+  def_grad(H, u[0], u[1], u[2], u[3], r.dphi, false);
+  if (!X) {
+    H[0] -= 1.0;
+    H[4] -= 1.0;
+    H[8] -= 1.0;
+  }
+}
+
 template <int MODEL>
 __global__ void k_energy(int nT, const TetRec64 *__restrict__ rec, const double *__restrict__ x,
-                         const double *__restrict__ q_base, double scale, double mass_coeff,
-                         const double *__restrict__ x_hat, int ndof, const double *__restrict__ f_ext,
-                         double force_scale, double *__restrict__ partial) {
+                         const double *__restrict__ q_base, double scale, const double *__restrict__ X,
+                         double mass_coeff, const double *__restrict__ x_hat, int ndof,
+                         const double *__restrict__ f_ext, double force_scale, double *__restrict__ partial) {
   double acc = 0.0;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nT; t += gridDim.x * blockDim.x) {
     const TetRec64 &r = rec[t];
-    const int id[4] = {r.idx.x, r.idx.y, r.idx.z, r.idx.w};
-    double q[4][3], xs[4][3];
-    for (int a = 0; a < 4; ++a)
-      for (int d = 0; d < 3; ++d) {
-        double xv = x[3 * id[a] + d];
-        xs[a][d] = xv;
-        q[a][d] = scale * xv + (q_base ? q_base[3 * id[a] + d] : 0.0);
-      }
-    double F[9];
-    def_grad(F, q[0], q[1], q[2], q[3], r.dphi, false);
-    acc += psi_model<double>(MODEL, F, r.pv);
+    double H[9];
+    disp_grad64(r, x, q_base, scale, X, nullptr, 0.0, H);
+    acc += psi_model_disp<double>(MODEL, H, r.pv);
     if (mass_coeff != 0.0) {
+      const int id[4] = {r.idx.x, r.idx.y, r.idx.z, r.idx.w};
       double s[3] = {0, 0, 0}, sh[3] = {0, 0, 0}, xx = 0.0, xh = 0.0;
       for (int a = 0; a < 4; ++a)
         for (int d = 0; d < 3; ++d) {
-          double h = x_hat ? x_hat[3 * id[a] + d] : 0.0;
-          s[d] += xs[a][d];
+          const double xv = x[3 * id[a] + d];
+          const double h = x_hat ? x_hat[3 * id[a] + d] : 0.0;
+          s[d] += xv;
           sh[d] += h;
-          xx += xs[a][d] * xs[a][d];
-          xh += xs[a][d] * h;
+          xx += xv * xv;
+          xh += xv * h;
         }
       double m20 = r.mass / 20.0;
       acc += mass_coeff * m20 * (0.5 * (dot3(s, s) + xx) - (dot3(s, sh) + xh));
@@ -195,6 +217,47 @@ __global__ void k_energy(int nT, const TetRec64 *__restrict__ rec, const double 
   if (f_ext && force_scale != 0.0)
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ndof; i += gridDim.x * blockDim.x)
       acc -= force_scale * f_ext[i] * x[i];
+  double s = block_sum(acc);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+// f(x + alpha d) - f(x) of the objective, element by element, so that the
+// constant part of f (which dominates |f| near a minimum) cancels exactly:
+// per tet psi(H1) - psi(H0), alpha d^T M (x - x_hat) + alpha^2/2 d^T M d,
+// and - force_scale alpha d^T f.
+template <int MODEL>
+__global__ void k_energy_diff(int nT, const TetRec64 *__restrict__ rec, const double *__restrict__ x,
+                              const double *__restrict__ dx, double alpha, const double *__restrict__ q_base,
+                              double scale, const double *__restrict__ X, double mass_coeff,
+                              const double *__restrict__ x_hat, int ndof, const double *__restrict__ f_ext,
+                              double force_scale, double *__restrict__ partial) {
+  double acc = 0.0;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nT; t += gridDim.x * blockDim.x) {
+    const TetRec64 &r = rec[t];
+    double H0[9], H1[9];
+    disp_grad64(r, x, q_base, scale, X, nullptr, 0.0, H0);
+    disp_grad64(r, x, q_base, scale, X, dx, alpha, H1);
+    acc += psi_model_disp<double>(MODEL, H1, r.pv) - psi_model_disp<double>(MODEL, H0, r.pv);
+    if (mass_coeff != 0.0) {
+      const int id[4] = {r.idx.x, r.idx.y, r.idx.z, r.idx.w};
+      double sd[3] = {0, 0, 0}, se[3] = {0, 0, 0}, de = 0.0, dd = 0.0;
+      for (int a = 0; a < 4; ++a)
+        for (int d = 0; d < 3; ++d) {
+          const int i = 3 * id[a] + d;
+          const double dv = dx[i], ev = x[i] - (x_hat ? x_hat[i] : 0.0);
+          sd[d] += dv;
+          se[d] += ev;
+          de += dv * ev;
+          dd += dv * dv;
+        }
+      // d^T M_e y = m/20 (sum d . sum y + sum_a d_a . y_a)
+      const double m20 = r.mass / 20.0;
+      acc += mass_coeff * m20 * (alpha * (dot3(sd, se) + de) + 0.5 * alpha * alpha * (dot3(sd, sd) + dd));
+    }
+  }
+  if (f_ext && force_scale != 0.0)
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < ndof; i += gridDim.x * blockDim.x)
+      acc -= force_scale * alpha * f_ext[i] * dx[i];
   double s = block_sum(acc);
   if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
@@ -552,8 +615,9 @@ int energy(bartels_ctx ctx, bartels_mesh_plan plan, int model, const ObjectiveDe
   if (g > kRedBlocks) g = kRedBlocks;
   double *part = ctx->partials.as<double>();
   const int ndof = 3 * plan->nV;
-#define BT_EN(M)                                                                                              \
-  BT_LAUNCH(ctx, k_energy<M>, g, 256, 0, plan->nT, plan->rec64, x, obj.q_base, obj.scale, obj.mass_coeff,    \
+  const double *X = plan->dphi_matches_rest ? plan->X : nullptr;
+#define BT_EN(M)                                                                                                \
+  BT_LAUNCH(ctx, k_energy<M>, g, 256, 0, plan->nT, plan->rec64, x, obj.q_base, obj.scale, X, obj.mass_coeff,   \
             obj.x_hat, ndof, obj.f_ext, obj.force_scale, part)
   switch (model) {
     case MODEL_NH: BT_EN(MODEL_NH); break;
@@ -563,6 +627,28 @@ int energy(bartels_ctx ctx, bartels_mesh_plan plan, int model, const ObjectiveDe
     default: return fail(BARTELS_E_INVALID_ARG, "unknown model");
   }
 #undef BT_EN
+  return reduce_sum(ctx, part, g, d_out);
+}
+
+int energy_diff(bartels_ctx ctx, bartels_mesh_plan plan, int model, const ObjectiveDev &obj, const double *x,
+                const double *dx, double alpha, double *d_out) {
+  BT_CHECK(ctx->partials.ensure(kRedBlocks * sizeof(double)));
+  int g = grid_for(ctx, plan->nT, 256);
+  if (g > kRedBlocks) g = kRedBlocks;
+  double *part = ctx->partials.as<double>();
+  const int ndof = 3 * plan->nV;
+  const double *X = plan->dphi_matches_rest ? plan->X : nullptr;
+#define BT_ED(M)                                                                                                \
+  BT_LAUNCH(ctx, k_energy_diff<M>, g, 256, 0, plan->nT, plan->rec64, x, dx, alpha, obj.q_base, obj.scale, X,    \
+            obj.mass_coeff, obj.x_hat, ndof, obj.f_ext, obj.force_scale, part)
+  switch (model) {
+    case MODEL_NH: BT_ED(MODEL_NH); break;
+    case MODEL_STVK: BT_ED(MODEL_STVK); break;
+    case MODEL_COROT: BT_ED(MODEL_COROT); break;
+    case MODEL_NH_ISO: BT_ED(MODEL_NH_ISO); break;
+    default: return fail(BARTELS_E_INVALID_ARG, "unknown model");
+  }
+#undef BT_ED
   return reduce_sum(ctx, part, g, d_out);
 }
 

@@ -166,6 +166,9 @@ int energy(bartels_ctx ctx, bartels_mesh_plan plan, int model, const ObjectiveDe
            double *d_out);
 int gradient(bartels_ctx ctx, bartels_mesh_plan plan, int model, const ObjectiveDev &obj, const double *x,
              double *g);
+// f(x + alpha dx) - f(x), element by element (line search)
+int energy_diff(bartels_ctx ctx, bartels_mesh_plan plan, int model, const ObjectiveDev &obj, const double *x,
+                const double *dx, double alpha, double *d_out);
 int hessian(bartels_ctx ctx, bartels_mesh_plan plan, int model, int psd_mode, float psd_tol, int flags,
             double coeff_K, double coeff_M, const double *q_or_null, const ObjectiveDev &obj, const double *x,
             float *values);

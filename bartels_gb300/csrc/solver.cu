@@ -872,30 +872,34 @@ int newton_iterate(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton
   bartels_pcg_report pr;
   int s = pcg_solve(ctx, op, n, w.xt, w.d, plan->w_pcg, p.pcg, &pr);
   rep->pcg_iterations += pr.iterations;
+  rep->last_pcg_iterations = pr.iterations;
+  rep->last_pcg_refinements = pr.refinements;
+  rep->last_pcg_rel_residual = pr.rel_residual;
+  if (!pr.converged) rep->pcg_failures++;
   double t3 = now_s();
   rep->t_pcg += t3 - t2;
   if (s != BARTELS_OK && s != BARTELS_E_NOT_CONVERGED) return s;
-  // line search (src/linesearch_backtracking_bisection.cpp:17-30)
-  double gd, f0;
+  // line search (src/linesearch_backtracking_bisection.cpp:17-30): while
+  // f(x + alpha d) > f(x) + c g.d and it < max: alpha *= p. The difference
+  // f(x + alpha d) - f(x) is evaluated element by element (energy_diff) so that
+  // it stays accurate when it is many orders below |f| near the minimum.
+  double gd;
   BT_CHECK(dot(ctx, w.g, w.d, n, w.scal));
   BT_CHECK(read_scalar(ctx, w.scal, &gd));
-  BT_CHECK(energy(ctx, plan, p.model, obj, x, w.scal));
-  BT_CHECK(read_scalar(ctx, w.scal, &f0));
   double alpha = p.ls_alpha;
   int it = 0;
+  double df = 0.0;
   for (;;) {
-    BT_LAUNCH(ctx, k_axpy_to, grid_vec(ctx, n), 256, 0, n, x, alpha, w.d, w.xt);
-    double ft;
-    BT_CHECK(energy(ctx, plan, p.model, obj, w.xt, w.scal));
-    BT_CHECK(read_scalar(ctx, w.scal, &ft));
-    if (!(ft > f0 + p.ls_c * gd && it < p.max_iterations_ls)) {
-      if (!(ft > f0 + p.ls_c * gd)) rep->energy = ft;
-      break;
-    }
+    BT_CHECK(energy_diff(ctx, plan, p.model, obj, x, w.d, alpha, w.scal));
+    BT_CHECK(read_scalar(ctx, w.scal, &df));
+    if (!(df > p.ls_c * gd && it < p.max_iterations_ls)) break;
     alpha *= p.ls_p;
     it++;
   }
+  BT_LAUNCH(ctx, k_axpy_to, grid_vec(ctx, n), 256, 0, n, x, alpha, w.d, w.xt);
+  rep->energy_change = df;
   if (it == p.max_iterations_ls) rep->ls_failures++;
+  rep->last_alpha = alpha;
   BT_CUDA(cudaMemcpyAsync(x, w.xt, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
   rep->ls_iterations += it;
   BT_CUDA(cudaStreamSynchronize(ctx->stream));

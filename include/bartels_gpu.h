@@ -256,6 +256,13 @@ typedef struct {
   double energy;
   double seconds;        /* wall time of the solve (device-synchronised) */
   double t_gradient, t_hessian, t_pcg, t_linesearch; /* seconds per stage, summed */
+  /* last Newton iteration */
+  double last_alpha;             /* accepted line-search step */
+  double last_pcg_rel_residual;  /* FP64 ||b - A d|| / ||b|| of the search direction */
+  int last_pcg_iterations;
+  int last_pcg_refinements;
+  int pcg_failures;              /* searches whose PCG did not reach rel_tol */
+  double energy_change;          /* f(x_new) - f(x_old) of the last step */
 } bartels_newton_report;
 
 void bartels_newton_default_params(bartels_newton_params *p);

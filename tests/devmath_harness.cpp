@@ -74,3 +74,7 @@ void dm_def_grad_d(const double *x0, const double *x1, const double *x2, const d
   def_grad<double>(F, x0, x1, x2, x3, dphi9, add_identity != 0);
 }
 }
+
+extern "C" double dm_psi_disp_d(int model, const double *H, const double *pv) {
+  return psi_model_disp<double>(model, H, pv);
+}

@@ -149,3 +149,33 @@ def test_svd3_float_and_double(oracle):
         assert np.allclose(S32, S0, rtol=2e-5, atol=2e-6 * np.abs(S0).max())
         Um, Vm = U32.reshape(3, 3, order="F").astype(float), V32.reshape(3, 3, order="F").astype(float)
         assert np.linalg.norm(Um @ np.diag(S32.astype(float)) @ Vm.T - F) <= 1e-5 * np.linalg.norm(F)
+
+
+@pytest.mark.parametrize("model", ["neohookean", "neohookean_isochoric", "stvk"])
+def test_cancellation_free_energy_accuracy(oracle, model):
+    """psi from the displacement gradient H = F - I (used by the GPU energy and
+    line search) against a 40-digit evaluation of the reference's formula: the
+    textbook FP64 form loses ~eps/|H|^2 near rest, this one must not."""
+    mpmath = pytest.importorskip("mpmath")
+    mpmath.mp.dps = 40
+    L = devmath()
+    L.dm_psi_disp_d.restype = C.c_double
+    rng = np.random.default_rng(21)
+    p = PARAMS[model]
+    for scale in (1e-6, 1e-4, 1e-2, 0.2):
+        for _ in range(5):
+            H = scale * rng.standard_normal((3, 3))
+            F = mpmath.matrix([[mpmath.mpf(1) * (i == j) + mpmath.mpf(float(H[i, j])) for j in range(3)]
+                               for i in range(3)])
+            J = mpmath.det(F)
+            I1 = sum(F[i, j] ** 2 for i in range(3) for j in range(3))
+            if model == "neohookean":
+                ref = p[0] * (I1 - 3 - 2 * mpmath.log(J)) + p[1] * (J - 1) ** 2
+            elif model == "neohookean_isochoric":
+                ref = p[0] * (J ** (mpmath.mpf(-2) / 3) * I1 - 3) + p[1] * (J - 1) ** 2
+            else:
+                Em = (F.T * F - mpmath.eye(3)) / 2
+                ref = p[1] * sum((Em * Em)[i, i] for i in range(3)) + p[0] / 2 * sum(Em[i, i] for i in range(3)) ** 2
+            hv = np.ascontiguousarray(H.ravel(order="F"))
+            got = L.dm_psi_disp_d(MODEL_ID[model], dp(hv), dp(p))
+            assert abs(got - float(ref)) <= 1e-13 * abs(float(ref)), (scale, got, float(ref))
