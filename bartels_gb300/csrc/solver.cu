@@ -391,37 +391,47 @@ k_spmv_blk_g(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, 
   BT_ROW_LOOP_END
 }
 
-// Direction + SpMV, block layout: p = z + beta p_old (computed on the fly for
-// every column read, written by the row owner), ap = A p, partials of p.Ap.
-template <int G>
+// Direction p = z + beta p_old (into the other p buffer), 4 vertices = 12
+// floats = 3 aligned float4 per thread, scalar tail.
 __global__ void __launch_bounds__(256)
-k_pcg_spmv_blk(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, const float *__restrict__ val,
-               const float *__restrict__ z, float *__restrict__ pa, float *__restrict__ pb, float *__restrict__ ap,
-               const unsigned char *__restrict__ pinned, double *__restrict__ part, PcgState *__restrict__ st) {
+k_pcg_dir(int n, const float *__restrict__ z, float *__restrict__ pa, float *__restrict__ pb,
+          const PcgState *__restrict__ st) {
   if (st->done) return;
   const int it = st->it;
   const float beta = st->beta;
-  // iteration it reads p_{it-1} from (it odd ? pa : pb) and writes p_it to the other
   const float *p_old = (it & 1) ? pa : pb;
   float *p_new = (it & 1) ? pb : pa;
+  const int n4 = n / 4;
+  const float4 *z4 = reinterpret_cast<const float4 *>(z);
+  const float4 *o4 = reinterpret_cast<const float4 *>(p_old);
+  float4 *n4p = reinterpret_cast<float4 *>(p_new);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += gridDim.x * blockDim.x) {
+    const float4 a = __ldcg(z4 + i), o = __ldcg(o4 + i);
+    n4p[i] = make_float4(a.x + beta * o.x, a.y + beta * o.y, a.z + beta * o.z, a.w + beta * o.w);
+  }
+  for (int i = 4 * n4 + blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    p_new[i] = z[i] + beta * p_old[i];
+}
+
+// ap = A p (block layout), partials of p.Ap; alpha in the last block.
+template <int G>
+__global__ void __launch_bounds__(256)
+k_pcg_spmv_blk(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, const float *__restrict__ val,
+               const float *__restrict__ pa, const float *__restrict__ pb, float *__restrict__ ap,
+               const unsigned char *__restrict__ pinned, double *__restrict__ part, PcgState *__restrict__ st) {
+  if (st->done) return;
+  const float *p = (st->it & 1) ? pb : pa;
   float acc = 0.f;
   BT_ROW_LOOP_BEGIN(G)
   float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-  if (active)
-    spmv_row_acc<G>(v, sl, brp, bcol, val, [&](int c) { return __ldcg(z + c) + beta * __ldcg(p_old + c); }, s0, s1,
-                    s2);
+  if (active) spmv_row_acc<G>(v, sl, brp, bcol, val, [&](int c) { return __ldcg(p + c); }, s0, s1, s2);
   group_reduce<G>(s0, s1, s2);
   if (active && sl == 0) {
-    float pv[3];
-    for (int k = 0; k < 3; ++k) pv[k] = __ldcg(z + 3 * v + k) + beta * __ldcg(p_old + 3 * v + k);
     if (pinned && pinned[v]) s0 = s1 = s2 = 0.f;
-    p_new[3 * v] = pv[0];
-    p_new[3 * v + 1] = pv[1];
-    p_new[3 * v + 2] = pv[2];
     ap[3 * v] = s0;
     ap[3 * v + 1] = s1;
     ap[3 * v + 2] = s2;
-    acc += pv[0] * s0 + pv[1] * s1 + pv[2] * s2;
+    acc += __ldcg(p + 3 * v) * s0 + __ldcg(p + 3 * v + 1) * s1 + __ldcg(p + 3 * v + 2) * s2;
   }
   BT_ROW_LOOP_END
   double s = cta_sum_f(acc);
@@ -436,32 +446,24 @@ k_pcg_spmv_blk(int nV, const int *__restrict__ brp, const int *__restrict__ bcol
   }
 }
 
-// Direction + SpMV for a generic scalar CSR (one warp per row).
+// ap = A p for a generic scalar CSR (one warp per row), partials of p.Ap.
 __global__ void __launch_bounds__(256)
 k_pcg_spmv_csr(int n, const int *__restrict__ rp, const int *__restrict__ ci, const float *__restrict__ val,
-               const float *__restrict__ z, float *__restrict__ pa, float *__restrict__ pb, float *__restrict__ ap,
+               const float *__restrict__ pa, const float *__restrict__ pb, float *__restrict__ ap,
                double *__restrict__ part, PcgState *__restrict__ st) {
   if (st->done) return;
-  const int it = st->it;
-  const float beta = st->beta;
-  const float *p_old = (it & 1) ? pa : pb;
-  float *p_new = (it & 1) ? pb : pa;
+  const float *p = (st->it & 1) ? pb : pa;
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   float acc = 0.f;
   for (int i = warp; i < n; i += nwarps) {
     float s = 0.f;
-    for (int k = rp[i] + lane; k < rp[i + 1]; k += 32) {
-      const int c = ci[k];
-      s += val[k] * (__ldcg(z + c) + beta * __ldcg(p_old + c));
-    }
+    for (int k = rp[i] + lane; k < rp[i + 1]; k += 32) s += val[k] * __ldcg(p + ci[k]);
     s = warp_sumf(s);
     if (lane == 0) {
-      const float pv = __ldcg(z + i) + beta * __ldcg(p_old + i);
-      p_new[i] = pv;
       ap[i] = s;
-      acc += pv * s;
+      acc += __ldcg(p + i) * s;
     }
   }
   double s = cta_sum_f(acc);
@@ -649,17 +651,19 @@ static int pcg_enqueue_iters(bartels_ctx ctx, const PcgOperator &op, const PcgWo
   const bool blk = op.plan != nullptr;
   const int gs = blk ? grid_spmv(ctx, (int64_t)op.plan->nV * ctx->spmv_lanes / 32 + 1) : grid_spmv(ctx, n);
   const int gu = grid_vec(ctx, (nb + 3) / 4);
+  const int gd = grid_vec(ctx, (n + 3) / 4);
   for (int i = 0; i < iters; ++i) {
+    BT_LAUNCH(ctx, k_pcg_dir, gd, 256, 0, n, w.z, w.pa, w.pb, w.st);
     if (blk) {
-#define BT_K1(G)                                                                                                \
-  BT_LAUNCH(ctx, k_pcg_spmv_blk<G>, gs, 256, 0, op.plan->nV, op.plan->brp, op.plan->bcol, op.values, w.z, w.pa, \
-            w.pb, w.ap, op.pinned, w.part_a, w.st)
+#define BT_K1(G)                                                                                                 \
+  BT_LAUNCH(ctx, k_pcg_spmv_blk<G>, gs, 256, 0, op.plan->nV, op.plan->brp, op.plan->bcol, op.values, w.pa, w.pb, \
+            w.ap, op.pinned, w.part_a, w.st)
       if (ctx->spmv_lanes == 4) BT_K1(4);
       else if (ctx->spmv_lanes == 16) BT_K1(16);
       else BT_K1(8);
 #undef BT_K1
     } else {
-      BT_LAUNCH(ctx, k_pcg_spmv_csr, gs, 256, 0, n, op.rp, op.ci, op.values, w.z, w.pa, w.pb, w.ap, w.part_a, w.st);
+      BT_LAUNCH(ctx, k_pcg_spmv_csr, gs, 256, 0, n, op.rp, op.ci, op.values, w.pa, w.pb, w.ap, w.part_a, w.st);
     }
     BT_LAUNCH(ctx, k_pcg_update, gu, 256, 0, nb, n, w.minv, w.pa, w.pb, w.ap, w.x, w.r, w.z, w.part_a, w.part_b, w.st);
   }
@@ -775,7 +779,7 @@ static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double
               prm.inner_rel_tol * prm.inner_rel_tol, abs2, prm.max_iters - rep->iterations);
     for (;;) {
       BT_CUDA(cudaGraphLaunch(exec, ctx->stream));
-      ctx->launches += 2 * chunk;
+      ctx->launches += 3 * chunk;
       BT_CUDA(cudaMemcpyAsync(&hs, w.st, sizeof(PcgState), cudaMemcpyDeviceToHost, ctx->stream));
       BT_CUDA(cudaStreamSynchronize(ctx->stream));
       if (hs.done) break;
