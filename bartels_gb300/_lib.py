@@ -95,6 +95,7 @@ SIGNATURES = [
      [_P, _P, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_double, _P, _P]),
     ("bartels_plan_spmv_d", C.c_int, [_P, _P, _P, _P, _P]),
     ("bartels_newton_advance_implicit_euler_d", C.c_int, [_P, _P, C.c_double, _P]),
+    ("bartels_tetmesh_dq_noalloc_d", C.c_int, [_P, _P, C.c_int, _P, _P]),
     ("bartels_newton_iterate_d", C.c_int,
      [_P, _P, C.POINTER(NewtonParams), _P, C.c_double, _I, C.POINTER(NewtonReport)]),
 ]

@@ -26,6 +26,7 @@ int csr_search_direction(bartels_ctx ctx, int n, const int *rp, const int *ci, c
                          double *d, const bartels_pcg_params &prm, bartels_pcg_report *rep);
 int advance_implicit_euler(bartels_ctx ctx, bartels_mesh_plan plan, double dt, const double *v);
 int plan_spmv(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const float *x, float *y);
+int noalloc_gradient(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q_d, double *g_d);
 }  // namespace bartels
 
 using namespace bartels;
@@ -545,6 +546,13 @@ int bartels_newton_advance_implicit_euler_d(bartels_ctx ctx, bartels_mesh_plan p
   BT_CHECK(check_plan(ctx, plan));
   if (!v_d) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
   return advance_implicit_euler(ctx, plan, dt, v_d);
+}
+
+int bartels_tetmesh_dq_noalloc_d(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q_d,
+                                 double *g_d) {
+  BT_CHECK(check_plan(ctx, plan));
+  if (!valid_model(model) || !q_d || !g_d) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  return noalloc_gradient(ctx, plan, model, q_d, g_d);
 }
 
 }  // extern "C"

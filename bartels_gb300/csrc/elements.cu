@@ -2,6 +2,9 @@
 // per-tet records, FP64 energy and gradient, and the fused FP32 Hessian
 // assembly (element math + PSD projection + deterministic per-row sums in tet
 // order, written straight into the CSR value array).
+#include <mutex>
+#include <string>
+
 #include "devmath.cuh"
 #include "internal.cuh"
 
@@ -729,6 +732,50 @@ int ext_force(bartels_ctx ctx, bartels_mesh_plan plan, const double traction[3],
 
 int values_to_double(bartels_ctx ctx, const float *v32, double *v64, int64_t n) {
   BT_LAUNCH(ctx, k_to_double, grid_for(ctx, n, 256), 256, 0, n, v32, v64);
+  return BARTELS_OK;
+}
+
+// ------------------------------------------------ allocation-free gradient ---
+// Scratch of bartels_tetmesh_dq_noalloc_d: the 12 per-tet gradient entries of
+// up to kNoAllocMaxTets tets (6 MiB). Every GPU that loads the library keeps
+// this array until the process exits. All calls share it and it keeps the last
+// call's contents; every entry a call reads is written by that call first, so
+// nothing needs clearing. Calls that overlap on the GPU race on it.
+constexpr int kNoAllocMaxTets = 1 << 16;
+static __device__ __align__(256) double g_noalloc_scratch[12 * kNoAllocMaxTets];
+static double *g_noalloc_ptr[64];  // device address of the scratch, per device
+static std::mutex g_noalloc_mutex;
+
+int noalloc_gradient(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q_d, double *g_d) {
+  if (plan->nT > kNoAllocMaxTets)
+    return fail(BARTELS_E_UNSUPPORTED, "bartels_tetmesh_dq_noalloc_d handles at most 65536 tets (the mesh has " +
+                                           std::to_string(plan->nT) + "); use bartels_tetmesh_dq");
+  if (ctx->device < 0 || ctx->device >= 64) return fail(BARTELS_E_UNSUPPORTED, "device index above 63");
+  double *ge;
+  {
+    // one-time set-up per device (the caller's device is current): the array's
+    // host-side name is not a device address, so look the address up
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[ctx->device]) {
+      void *p = nullptr;
+      BT_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+      g_noalloc_ptr[ctx->device] = static_cast<double *>(p);
+    }
+    ge = g_noalloc_ptr[ctx->device];
+  }
+  if (plan->nT == 0) return BARTELS_OK;
+  const int gt = grid_for(ctx, plan->nT, 256);
+#define BT_GN(M) BT_LAUNCH(ctx, k_grad_elem<M>, gt, 256, 0, plan->nT, plan->rec64, q_d, nullptr, 1.0, 0.0, nullptr, ge)
+  switch (model) {
+    case MODEL_NH: BT_GN(MODEL_NH); break;
+    case MODEL_STVK: BT_GN(MODEL_STVK); break;
+    case MODEL_COROT: BT_GN(MODEL_COROT); break;
+    case MODEL_NH_ISO: BT_GN(MODEL_NH_ISO); break;
+    default: return fail(BARTELS_E_INVALID_ARG, "unknown model");
+  }
+#undef BT_GN
+  BT_LAUNCH(ctx, k_grad_gather, grid_for(ctx, plan->nV, 256), 256, 0, plan->nV, plan->inc_ptr, plan->inc_tet, ge,
+            (const double *)nullptr, 0.0, (const unsigned char *)nullptr, g_d);
   return BARTELS_OK;
 }
 

@@ -299,6 +299,21 @@ int bartels_plan_spmv_d(bartels_ctx ctx, bartels_mesh_plan plan, const float *va
  * q_base += dt * v, x_hat = v (device v_d, 3nV). */
 int bartels_newton_advance_implicit_euler_d(bartels_ctx ctx, bartels_mesh_plan plan, double dt, const double *v_d);
 
+/* ------------------------------------------------- allocation-free variant -- */
+/* Gradient of the elastic energy (as bartels_tetmesh_dq, with the plan's
+ * element data) at device positions q_d (3nV doubles) into device g_d (3nV),
+ * without allocating any memory: for callers that cannot call cudaMalloc,
+ * such as code running while a CUDA graph is being captured around it, memory
+ * pools that forbid growth, or hosts that account every device allocation.
+ * Its element-gradient scratch is a fixed array compiled into the library
+ * (6 MiB, held by every GPU that loads it), so meshes of at most 65536 tets
+ * are accepted; larger ones return BARTELS_E_UNSUPPORTED. The first call on a
+ * device looks up the array's device address (make it before any stream
+ * capture). All calls share the array: calls that overlap on the GPU race.
+ * This entry point has no counterpart in the reference. */
+int bartels_tetmesh_dq_noalloc_d(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q_d,
+                                 double *g_d);
+
 #ifdef __cplusplus
 }
 #endif
