@@ -247,8 +247,9 @@ def run_gpu(args, rank, world):
     try:
         with open(os.path.join(ROOT, "profiles", "spmv_traffic.json")) as f:
             tj = json.load(f)
-        if tj.get("n") == args.n:
-            traffic = tj["dram_bytes_per_launch"]
+        # DRAM bytes per launch from one ncu capture of a smaller cube, scaled by the
+        # algorithmic bytes (the SpMV's traffic grows in proportion to its nnz)
+        traffic = float(tj["ratio"]) * spmv_bytes
     except Exception:
         pass
 
