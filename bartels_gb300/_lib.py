@@ -17,6 +17,7 @@ CONVERGED, MAX_ITERATIONS_REACHED = 0, 1
 NEOHOOKEAN, STVK, COROTATIONAL, NEOHOOKEAN_ISOCHORIC = 0, 1, 2, 3
 PSD_NONE, PSD_SIMPLE_FIX = 0, 1
 DQ2_COROT_EXACT = 1
+PRECOND_BLOCK_JACOBI, PRECOND_LEARNED = 0, 1
 
 
 class BartelsError(RuntimeError):
@@ -50,7 +51,7 @@ class NewtonReport(C.Structure):
                 ("t_gradient", C.c_double), ("t_hessian", C.c_double), ("t_pcg", C.c_double),
                 ("t_linesearch", C.c_double), ("last_alpha", C.c_double), ("last_pcg_rel_residual", C.c_double),
                 ("last_pcg_iterations", C.c_int), ("last_pcg_refinements", C.c_int), ("pcg_failures", C.c_int),
-                ("energy_change", C.c_double)]
+                ("energy_change", C.c_double), ("precond_fallbacks", C.c_int), ("t_precond", C.c_double)]
 
 
 OBJECTIVE_FN = C.CFUNCTYPE(C.c_double, C.POINTER(C.c_double), C.c_int, C.c_void_p)
@@ -96,6 +97,18 @@ SIGNATURES = [
     ("bartels_plan_spmv_d", C.c_int, [_P, _P, _P, _P, _P]),
     ("bartels_newton_advance_implicit_euler_d", C.c_int, [_P, _P, C.c_double, _P]),
     ("bartels_tetmesh_dq_noalloc_d", C.c_int, [_P, _P, C.c_int, _P, _P]),
+    ("bartels_lpcg_create", C.c_int, [_P, C.POINTER(_P)]),
+    ("bartels_lpcg_destroy", C.c_int, [_P]),
+    ("bartels_lpcg_num_params", C.c_int, []),
+    ("bartels_lpcg_set_params", C.c_int, [_P, _P]),
+    ("bartels_lpcg_get_params", C.c_int, [_P, _P, _P]),
+    ("bartels_lpcg_train_step", C.c_int, [_P, _P, _P, _P, C.c_int, C.c_uint, C.c_float, C.c_float, _D]),
+    ("bartels_lpcg_outputs", C.c_int, [_P, _P, _P, _P, _P]),
+    ("bartels_plan_factor_size", C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    ("bartels_plan_set_preconditioner", C.c_int, [_P, C.c_int, _P]),
+    ("bartels_plan_pcg_d", C.c_int, [_P, _P, _P, _P, _P, C.POINTER(PcgParams), C.POINTER(PcgReport)]),
+    ("bartels_newton_gradient_d", C.c_int, [_P, _P, C.POINTER(NewtonParams), _P, _P]),
+    ("bartels_gemm_bf16_d", C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, C.c_int, _P, _P, C.c_int, _P, C.c_int]),
     ("bartels_newton_iterate_d", C.c_int,
      [_P, _P, C.POINTER(NewtonParams), _P, C.c_double, _I, C.POINTER(NewtonReport)]),
 ]

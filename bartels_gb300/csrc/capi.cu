@@ -7,6 +7,7 @@
 
 #include "devmath.cuh"
 #include "internal.cuh"
+#include "lpcg_internal.cuh"
 
 namespace bartels {
 int plan_set_element_data(bartels_mesh_plan plan, const double *dphidX, const double *vol, const double *params,
@@ -27,6 +28,10 @@ int csr_search_direction(bartels_ctx ctx, int n, const int *rp, const int *ci, c
 int advance_implicit_euler(bartels_ctx ctx, bartels_mesh_plan plan, double dt, const double *v);
 int plan_spmv(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const float *x, float *y);
 int noalloc_gradient(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q_d, double *g_d);
+int plan_pcg(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const double *b, double *x,
+             const bartels_pcg_params &prm, bartels_pcg_report *rep);
+int newton_gradient(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params &p, const double *x,
+                    double *g);
 }  // namespace bartels
 
 using namespace bartels;
@@ -95,6 +100,10 @@ int bartels_ctx_create(int device, bartels_ctx *out) {
   if (const char *e = std::getenv("BARTELS_SPMV_LANES")) {
     const int g = std::atoi(e);
     if (g == 4 || g == 8 || g == 16) ctx->spmv_lanes = g;
+  }
+  if (const char *e = std::getenv("BARTELS_TRI_LANES")) {
+    const int g = std::atoi(e);
+    if (g == 4 || g == 8) ctx->tri_lanes = g;
   }
   *out = ctx;
   return BARTELS_OK;
@@ -553,6 +562,122 @@ int bartels_tetmesh_dq_noalloc_d(bartels_ctx ctx, bartels_mesh_plan plan, int mo
   BT_CHECK(check_plan(ctx, plan));
   if (!valid_model(model) || !q_d || !g_d) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
   return noalloc_gradient(ctx, plan, model, q_d, g_d);
+}
+
+
+int bartels_lpcg_create(bartels_ctx ctx, bartels_lpcg *out) {
+  BT_CHECK(check_ctx(ctx));
+  if (!out) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  return lpcg_create(ctx, out);
+}
+
+int bartels_lpcg_destroy(bartels_lpcg net) {
+  if (!net) return BARTELS_OK;
+  BT_CHECK(check_ctx(lpcg_ctx(net)));
+  lpcg_destroy(net);
+  return BARTELS_OK;
+}
+
+int bartels_lpcg_num_params(void) { return lpcg_num_params(); }
+
+int bartels_lpcg_set_params(bartels_lpcg net, const float *params) {
+  if (!net || !params) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  BT_CHECK(check_ctx(lpcg_ctx(net)));
+  return lpcg_set_params(net, params);
+}
+
+int bartels_lpcg_get_params(bartels_lpcg net, float *params, float *grad) {
+  if (!net) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  BT_CHECK(check_ctx(lpcg_ctx(net)));
+  return lpcg_get_params(net, params, grad);
+}
+
+int bartels_lpcg_train_step(bartels_lpcg net, bartels_mesh_plan plan, const float *values_d,
+                            const double *residual_d, int nprobes, unsigned seed, float lr, float clip,
+                            double *loss) {
+  if (!net || !values_d || !loss || nprobes < 0 || nprobes > 64) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  BT_CHECK(check_plan(lpcg_ctx(net), plan));
+  return lpcg_train_step(net, plan, values_d, residual_d, nprobes, seed, lr, clip, loss);
+}
+
+int bartels_lpcg_outputs(bartels_lpcg net, bartels_mesh_plan plan, const float *values_d, float *raw,
+                         float *g_lower) {
+  if (!net || !values_d) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  BT_CHECK(check_plan(lpcg_ctx(net), plan));
+  return lpcg_outputs(net, plan, values_d, raw, g_lower);
+}
+
+int bartels_plan_factor_size(bartels_mesh_plan plan, int64_t *nnzl_blocks, int64_t *nnzu_blocks) {
+  if (!plan) return fail(BARTELS_E_INVALID_ARG, "null plan");
+  BT_CHECK(check_ctx(plan->ctx));
+  FactorPattern *fp;
+  BT_CHECK(plan_factor_pattern(plan, &fp));
+  if (nnzl_blocks) *nnzl_blocks = fp->nnzl;
+  if (nnzu_blocks) *nnzu_blocks = fp->nnzu;
+  return BARTELS_OK;
+}
+
+int bartels_plan_set_preconditioner(bartels_mesh_plan plan, int kind, bartels_lpcg net) {
+  if (!plan) return fail(BARTELS_E_INVALID_ARG, "null plan");
+  if (kind == BARTELS_PRECOND_BLOCK_JACOBI) {
+    plan->precond = kind;
+    plan->lpcg_net = nullptr;
+    return BARTELS_OK;
+  }
+  if (kind != BARTELS_PRECOND_LEARNED || !net) return fail(BARTELS_E_INVALID_ARG, "unknown preconditioner");
+  if (lpcg_ctx(net) != plan->ctx) return fail(BARTELS_E_INVALID_ARG, "network belongs to another context");
+  plan->precond = kind;
+  plan->lpcg_net = net;
+  return BARTELS_OK;
+}
+
+int bartels_plan_pcg_d(bartels_ctx ctx, bartels_mesh_plan plan, const float *values_d, const double *b_d,
+                       double *x_d, const bartels_pcg_params *params, bartels_pcg_report *report) {
+  BT_CHECK(check_plan(ctx, plan));
+  if (!b_d || !x_d || !report) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  if (!values_d) {
+    if (plan->w_values.bytes < sizeof(float) * 9 * (size_t)plan->nnzb)
+      return fail(BARTELS_E_INVALID_ARG, "the plan has no assembled Hessian yet");
+    values_d = plan->w_values.as<float>();
+  }
+  bartels_pcg_params p;
+  if (params) p = *params;
+  else bartels_pcg_default_params(&p);
+  return plan_pcg(ctx, plan, values_d, b_d, x_d, p, report);
+}
+
+int bartels_newton_gradient_d(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params *params,
+                              const double *x_d, double *g_d) {
+  BT_CHECK(check_plan(ctx, plan));
+  if (!params || !x_d || !g_d || !valid_model(params->model)) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  return newton_gradient(ctx, plan, *params, x_d, g_d);
+}
+
+int bartels_gemm_bf16_d(bartels_ctx ctx, int M, int N, int K, const void *x_d, int ldx, const void *w_d,
+                        const float *bias_d, int relu, float *y_d, int ldy) {
+  BT_CHECK(check_ctx(ctx));
+  if (M < 0 || !x_d || !w_d || !y_d) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  BT_CHECK(ctx->stage_e.ensure(sizeof(int)));
+  int *err = ctx->stage_e.as<int>();
+  BT_CUDA(cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
+  GemmArgs g;
+  g.M = M;
+  g.N = N;
+  g.K = K;
+  g.x = static_cast<const __nv_bfloat16 *>(x_d);
+  g.ldx = ldx;
+  g.w = static_cast<const __nv_bfloat16 *>(w_d);
+  g.bias = bias_d;
+  g.relu = relu;
+  g.y = y_d;
+  g.ldy = ldy;
+  g.err = err;
+  BT_CHECK(gemm_bf16(ctx, g));
+  int h = 0;
+  BT_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  BT_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (h) return fail(BARTELS_E_TIMEOUT, "tensor-core GEMM: a bounded wait gave up");
+  return BARTELS_OK;
 }
 
 }  // extern "C"

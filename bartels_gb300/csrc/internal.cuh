@@ -68,6 +68,9 @@ struct alignas(16) TetRec64 {
 };
 static_assert(sizeof(TetRec64) == 128, "TetRec64 must be 128 bytes");
 
+struct FactorPattern;  // lower / upper block storage maps (learned preconditioner)
+struct LpcgPlanState;  // per-plan buffers of the learned preconditioner
+
 // Device buffer with geometric growth.
 struct DevBuf {
   void *p = nullptr;
@@ -88,6 +91,8 @@ struct bartels_ctx_s {
   // lanes per vertex row in the block-layout SpMV (4, 8 or 16; tuned per GPU,
   // overridable with BARTELS_SPMV_LANES)
   int spmv_lanes = 16;
+  // lanes per vertex row in the triangular factor passes (4 or 8; BARTELS_TRI_LANES)
+  int tri_lanes = 8;
   // pinned host staging for small read-backs
   double *host_scalars = nullptr;
   // device scratch for reductions
@@ -130,6 +135,11 @@ struct bartels_mesh_plan_s {
   unsigned char *pinned = nullptr;
   // true when dphidX is the rest shape's own (F = I + sum (u_a - u_0) phi_a^T)
   bool dphi_matches_rest = true;
+  // triangular-factor pattern and learned-preconditioner buffers (built on first use)
+  bartels::FactorPattern *factor = nullptr;
+  bartels::LpcgPlanState *lpcg = nullptr;
+  int precond = BARTELS_PRECOND_BLOCK_JACOBI;
+  bartels_lpcg lpcg_net = nullptr;
   // solver workspace
   bartels::DevBuf w_values, w_minv, w_vec, w_grad_e, w_energy, w_u, w_pcg, w_psd;
 };

@@ -17,6 +17,7 @@
 
 #include "devmath.cuh"
 #include "internal.cuh"
+#include "lpcg_internal.cuh"
 
 namespace bartels {
 
@@ -239,7 +240,88 @@ int plan_set_element_data(bartels_mesh_plan plan, const double *dphidX, const do
   return BARTELS_OK;
 }
 
+void FactorPattern::release() {
+  int *ptrs[] = {lrp, urp, low2up, up2low, rev};
+  for (int *p : ptrs)
+    if (p) cudaFree(p);
+  if (meta) cudaFree(meta);
+  meta = nullptr;
+  lrp = urp = low2up = up2low = rev = nullptr;
+  built = false;
+}
+
+// Lower / upper storage maps of a triangular factor on the plan's block
+// pattern (rows are sorted, so the lower part of a row is a prefix of it).
+int plan_factor_pattern(bartels_mesh_plan plan, FactorPattern **out) {
+  if (!plan->factor) plan->factor = new FactorPattern();
+  FactorPattern &f = *plan->factor;
+  *out = plan->factor;
+  if (f.built) return BARTELS_OK;
+  const int nV = plan->nV;
+  const std::vector<int> &brp = plan->h_brp, &bcol = plan->h_bcol;
+  std::vector<int> diag(nV), lrp(nV + 1, 0), urp(nV + 1, 0);
+  for (int v = 0; v < nV; ++v) {
+    const int *r = bcol.data() + brp[v];
+    const int nb = brp[v + 1] - brp[v];
+    diag[v] = (int)(std::lower_bound(r, r + nb, v) - r);
+    lrp[v + 1] = lrp[v] + diag[v] + 1;
+    urp[v + 1] = urp[v] + nb - diag[v];
+  }
+  const int64_t nnzl = lrp[nV], nnzu = urp[nV];
+  std::vector<int> low2up(nnzl), up2low(nnzu), rev(plan->nnzb);
+#pragma omp parallel for schedule(dynamic, 1024)
+  for (int v = 0; v < nV; ++v) {
+    const int nb = brp[v + 1] - brp[v];
+    for (int b = 0; b < nb; ++b) {
+      const int j = bcol[brp[v] + b];
+      const int *rj = bcol.data() + brp[j];
+      const int nbj = brp[j + 1] - brp[j];
+      const int pos = (int)(std::lower_bound(rj, rj + nbj, v) - rj);  // v in row j
+      rev[brp[v] + b] = brp[j] + pos;
+      if (b <= diag[v]) {
+        // lower block (v, j), j <= v  ->  upper block (j, v) of row j
+        low2up[lrp[v] + b] = urp[j] + (pos - diag[j]);
+      } else {
+        // upper block (v, j), j > v   ->  lower block (j, v) of row j
+        up2low[urp[v] + (b - diag[v])] = lrp[j] + pos;
+      }
+    }
+    up2low[urp[v]] = lrp[v] + diag[v];  // diagonal block
+  }
+  std::vector<int4> meta(nV);
+  int64_t lseg = 0, useg = 0;
+  for (int v = 0; v < nV; ++v) {
+    const int nb = brp[v + 1] - brp[v];
+    meta[v] = make_int4(brp[v], (int)lseg, (int)useg, diag[v] | (nb << 16));
+    lseg += 3ll * padded_row(diag[v] + 1);
+    useg += 3ll * padded_row(nb - diag[v]);
+  }
+  if (lseg > INT32_MAX || useg > INT32_MAX) return fail(BARTELS_E_UNSUPPORTED, "factor storage above 2^31 entries");
+  f.lsize = lseg;
+  f.usize = useg;
+  bartels_ctx ctx = plan->ctx;
+  BT_CHECK(upload(ctx, &f.meta, meta.data(), meta.size()));
+  BT_CHECK(upload(ctx, &f.lrp, lrp.data(), lrp.size()));
+  BT_CHECK(upload(ctx, &f.urp, urp.data(), urp.size()));
+  BT_CHECK(upload(ctx, &f.low2up, low2up.data(), low2up.size()));
+  BT_CHECK(upload(ctx, &f.up2low, up2low.data(), up2low.size()));
+  BT_CHECK(upload(ctx, &f.rev, rev.data(), rev.size()));
+  BT_CUDA(cudaStreamSynchronize(ctx->stream));
+  f.nnzl = nnzl;
+  f.nnzu = nnzu;
+  f.built = true;
+  return BARTELS_OK;
+}
+
+void lpcg_plan_release(bartels_mesh_plan plan);
+
 void plan_free(bartels_mesh_plan plan) {
+  if (plan->factor) {
+    plan->factor->release();
+    delete plan->factor;
+    plan->factor = nullptr;
+  }
+  lpcg_plan_release(plan);
   void *ptrs[] = {plan->X,        plan->E,      plan->dphi64,  plan->vol,     plan->params,  plan->density,
                   plan->rec32,    plan->rec64,  plan->inc_ptr, plan->inc_tet, plan->inc_pos, plan->brp,
                   plan->bcol,     plan->diag_pos, plan->chunk_v, plan->csr_rp, plan->csr_col, plan->q_base,

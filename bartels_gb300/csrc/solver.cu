@@ -16,6 +16,7 @@
 
 #include "devmath.cuh"
 #include "internal.cuh"
+#include "lpcg_internal.cuh"
 
 namespace bartels {
 
@@ -617,6 +618,184 @@ __global__ void k_f64_to_f32(int64_t n, const double *__restrict__ a, float *__r
     b[i] = (float)a[i];
 }
 
+// ------------------------------------------- factor preconditioner (G^T G) ---
+// z = G^T (G r) with G block-lower-triangular on the plan's pattern (the
+// learned preconditioner). G is held twice: by rows of its lower part and by
+// rows of G^T (the transposed blocks), so both products are row gathers.
+//
+// Row v of a triangular operand: blocks [b0, b0 + nblk) of the full pattern row
+// (columns cols[j] = bcol[brp[v] + b0 + j]), BF16 values in three scalar rows of
+// rs = 3 nblk entries padded to rsp (a multiple of 4). Each lane takes 4
+// consecutive columns per step: one 8-byte load per scalar row, and the 4
+// vector entries of the (at most two) blocks those columns fall in.
+// meta[v] = {brp, lower segment, upper segment, diag | nblocks << 16}.
+template <int G, class XV>
+__device__ __forceinline__ void tri_row_acc4(int sl, const int *__restrict__ cols, const __nv_bfloat16 *__restrict__ r0,
+                                             int rs, int rsp, XV &&xval, float &s0, float &s1, float &s2) {
+  for (int e0 = 4 * sl; e0 < rs; e0 += 4 * G) {
+    const uint2 w0 = __ldcs(reinterpret_cast<const uint2 *>(r0 + e0));
+    const uint2 w1 = __ldcs(reinterpret_cast<const uint2 *>(r0 + rsp + e0));
+    const uint2 w2 = __ldcs(reinterpret_cast<const uint2 *>(r0 + 2 * rsp + e0));
+    const int j0 = e0 / 3, l0 = e0 - 3 * j0;
+    const int c0 = __ldg(cols + j0);
+    const int c1 = 3 * (j0 + 1) < rs ? __ldg(cols + j0 + 1) : 0;
+    float xv[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int l = l0 + q;
+      const int c = l >= 3 ? c1 : c0;
+      xv[q] = e0 + q < rs ? xval(3 * c + (l >= 3 ? l - 3 : l)) : 0.f;
+    }
+    const uint32_t u0[2] = {w0.x, w0.y}, u1[2] = {w1.x, w1.y}, u2[2] = {w2.x, w2.y};
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      s0 += __uint_as_float(u0[h] << 16) * xv[2 * h] + __uint_as_float(u0[h] & 0xFFFF0000u) * xv[2 * h + 1];
+      s1 += __uint_as_float(u1[h] << 16) * xv[2 * h] + __uint_as_float(u1[h] & 0xFFFF0000u) * xv[2 * h + 1];
+      s2 += __uint_as_float(u2[h] << 16) * xv[2 * h] + __uint_as_float(u2[h] & 0xFFFF0000u) * xv[2 * h + 1];
+    }
+  }
+}
+
+// y = G r (lower rows). Rows of pinned vertices give 0.
+template <int G>
+__global__ void __launch_bounds__(256)
+k_pcg_prec_lower(int nV, const int4 *__restrict__ meta, const int *__restrict__ bcol,
+                 const __nv_bfloat16 *__restrict__ gl, const float *__restrict__ r, float *__restrict__ y,
+                 const unsigned char *__restrict__ pinned, const PcgState *__restrict__ st) {
+  if (st->done) return;
+  BT_ROW_LOOP_BEGIN(G)
+  float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+  if (active) {
+    const int4 m = __ldg(meta + v);
+    const int nl = (m.w & 0xFFFF) + 1;
+    tri_row_acc4<G>(sl, bcol + m.x, gl + m.y, 3 * nl, padded_row(nl), [&](int c) { return __ldcg(r + c); }, s0, s1,
+                    s2);
+  }
+  group_reduce<G>(s0, s1, s2);
+  if (active && sl == 0) {
+    if (pinned && pinned[v]) s0 = s1 = s2 = 0.f;
+    y[3 * v] = s0;
+    y[3 * v + 1] = s1;
+    y[3 * v + 2] = s2;
+  }
+  BT_ROW_LOOP_END
+}
+
+// z = G^T y (upper rows), partials of r.z; beta = r.z / r.z_old in the last block.
+template <int G>
+__global__ void __launch_bounds__(256)
+k_pcg_prec_upper(int nV, const int4 *__restrict__ meta, const int *__restrict__ bcol,
+                 const __nv_bfloat16 *__restrict__ gu, const float *__restrict__ y, const float *__restrict__ r,
+                 float *__restrict__ z, const unsigned char *__restrict__ pinned, double *__restrict__ part,
+                 PcgState *__restrict__ st) {
+  if (st->done) return;
+  float acc = 0.f;
+  BT_ROW_LOOP_BEGIN(G)
+  float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+  if (active) {
+    const int4 m = __ldg(meta + v);
+    const int d = m.w & 0xFFFF, nu = (m.w >> 16) - d;
+    tri_row_acc4<G>(sl, bcol + m.x + d, gu + m.z, 3 * nu, padded_row(nu), [&](int c) { return __ldcg(y + c); }, s0,
+                    s1, s2);
+  }
+  group_reduce<G>(s0, s1, s2);
+  if (active && sl == 0) {
+    if (pinned && pinned[v]) s0 = s1 = s2 = 0.f;
+    z[3 * v] = s0;
+    z[3 * v + 1] = s1;
+    z[3 * v + 2] = s2;
+    acc += __ldcg(r + 3 * v) * s0 + __ldcg(r + 3 * v + 1) * s1 + __ldcg(r + 3 * v + 2) * s2;
+  }
+  BT_ROW_LOOP_END
+  double s = cta_sum_f(acc);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+  if (last_block(&st->count)) {
+    const double rz = sum_partials(part, gridDim.x);
+    if (threadIdx.x == 0) {
+      st->beta = (float)(rz / st->rz);
+      st->rz = rz;
+      st->count = 0;
+    }
+  }
+}
+
+// x += alpha p; r -= alpha Ap; r.r, iteration count and convergence test
+// (the preconditioned residual follows in k_pcg_prec_lower / _upper).
+__global__ void __launch_bounds__(256)
+k_pcg_update_f(int n, const float *__restrict__ pa, const float *__restrict__ pb, const float *__restrict__ ap,
+               float *__restrict__ x, float *__restrict__ r, double *__restrict__ part, PcgState *__restrict__ st) {
+  if (st->done) return;
+  const int it = st->it;
+  const float *p = (it & 1) ? pb : pa;
+  const float alpha = st->alpha;
+  float arr = 0.f;
+  const int n4 = n / 4;
+  const float4 *p4 = reinterpret_cast<const float4 *>(p);
+  const float4 *a4 = reinterpret_cast<const float4 *>(ap);
+  float4 *x4 = reinterpret_cast<float4 *>(x);
+  float4 *r4 = reinterpret_cast<float4 *>(r);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += gridDim.x * blockDim.x) {
+    const float4 pv = __ldcg(p4 + i), av = __ldcg(a4 + i);
+    float4 xv = x4[i], rv = r4[i];
+    xv.x += alpha * pv.x; xv.y += alpha * pv.y; xv.z += alpha * pv.z; xv.w += alpha * pv.w;
+    rv.x -= alpha * av.x; rv.y -= alpha * av.y; rv.z -= alpha * av.z; rv.w -= alpha * av.w;
+    x4[i] = xv;
+    r4[i] = rv;
+    arr += rv.x * rv.x + rv.y * rv.y + rv.z * rv.z + rv.w * rv.w;
+  }
+  for (int i = 4 * n4 + blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    x[i] += alpha * p[i];
+    const float rv = r[i] - alpha * ap[i];
+    r[i] = rv;
+    arr += rv * rv;
+  }
+  double s = cta_sum_f(arr);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+  if (last_block(&st->count)) {
+    const double rr = sum_partials(part, gridDim.x);
+    if (threadIdx.x == 0) {
+      st->rr = rr;
+      st->it = it + 1;
+      if (rr <= st->tol2 || it + 1 >= st->max_it || !(rr == rr)) st->done = 1;
+      st->count = 0;
+    }
+  }
+}
+
+// start of an inner solve with the factor preconditioner: x = 0, r = (float) r64,
+// p = 0; r.r and the tolerance; r.z is set by the following k_pcg_prec_upper.
+__global__ void k_pcg_init_f(int n, const double *__restrict__ r64, float *__restrict__ x, float *__restrict__ r,
+                             float *__restrict__ p0, float *__restrict__ p1, double *__restrict__ part,
+                             PcgState *__restrict__ st, double inner_rel2, double abs_tol2, int max_it) {
+  float arr = 0.f;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float rv = (float)r64[i];
+    x[i] = 0.f;
+    r[i] = rv;
+    p0[i] = 0.f;
+    p1[i] = 0.f;
+    arr += rv * rv;
+  }
+  double s = cta_sum_f(arr);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+  if (last_block(&st->count)) {
+    const double rr = sum_partials(part, gridDim.x);
+    if (threadIdx.x == 0) {
+      st->rr = rr;
+      st->rr0 = rr;
+      st->rz = 1.0;
+      st->pap = 0.0;
+      st->alpha = 0.f;
+      st->beta = 0.f;
+      st->tol2 = fmax(inner_rel2 * rr, abs_tol2);
+      st->it = 0;
+      st->max_it = max_it;
+      st->done = (rr <= st->tol2 || max_it <= 0 || !(rr == rr)) ? 1 : 0;
+      st->count = 0;
+    }
+  }
+}
+
 // ================================================================ host ======
 struct PcgOperator {
   // block layout (plan)
@@ -627,6 +806,9 @@ struct PcgOperator {
   int n = 0;
   const int *rp = nullptr, *ci = nullptr;
   const double *values64 = nullptr;  // exact values for the FP64 refinement residual
+  // factor preconditioner z = G^T G r (block layout only): lower and upper storage
+  const __nv_bfloat16 *gl = nullptr, *gu = nullptr;
+  const FactorPattern *fp = nullptr;
 };
 
 struct PcgWork {
@@ -647,8 +829,28 @@ static int grid_spmv(bartels_ctx ctx, int64_t rows) {
 }
 
 
+static int pcg_enqueue_prec(bartels_ctx ctx, const PcgOperator &op, const PcgWork &w) {
+  const bartels_mesh_plan plan = op.plan;
+  // triangular rows are about half as long as the matrix rows (4 or 8 lanes, 4 columns a lane)
+  const int G = ctx->tri_lanes;
+  const int gt = grid_spmv(ctx, (int64_t)plan->nV * G / 32 + 1);
+#define BT_T(G_)                                                                                                 \
+  BT_LAUNCH(ctx, k_pcg_prec_lower<G_>, gt, 256, 0, plan->nV, op.fp->meta, plan->bcol, op.gl, w.r, w.ap, op.pinned, \
+            w.st);                                                                                               \
+  BT_LAUNCH(ctx, k_pcg_prec_upper<G_>, gt, 256, 0, plan->nV, op.fp->meta, plan->bcol, op.gu, w.ap, w.r, w.z,       \
+            op.pinned, w.part_b, w.st)
+  if (G == 4) {
+    BT_T(4);
+  } else {
+    BT_T(8);
+  }
+#undef BT_T
+  return BARTELS_OK;
+}
+
 static int pcg_enqueue_iters(bartels_ctx ctx, const PcgOperator &op, const PcgWork &w, int n, int nb, int iters) {
   const bool blk = op.plan != nullptr;
+  const bool fac = blk && op.gl != nullptr;
   const int gs = blk ? grid_spmv(ctx, (int64_t)op.plan->nV * ctx->spmv_lanes / 32 + 1) : grid_spmv(ctx, n);
   const int gu = grid_vec(ctx, (nb + 3) / 4);
   const int gd = grid_vec(ctx, (n + 3) / 4);
@@ -665,7 +867,13 @@ static int pcg_enqueue_iters(bartels_ctx ctx, const PcgOperator &op, const PcgWo
     } else {
       BT_LAUNCH(ctx, k_pcg_spmv_csr, gs, 256, 0, n, op.rp, op.ci, op.values, w.pa, w.pb, w.ap, w.part_a, w.st);
     }
-    BT_LAUNCH(ctx, k_pcg_update, gu, 256, 0, nb, n, w.minv, w.pa, w.pb, w.ap, w.x, w.r, w.z, w.part_a, w.part_b, w.st);
+    if (fac) {
+      BT_LAUNCH(ctx, k_pcg_update_f, gd, 256, 0, n, w.pa, w.pb, w.ap, w.x, w.r, w.part_b, w.st);
+      BT_CHECK(pcg_enqueue_prec(ctx, op, w));
+    } else {
+      BT_LAUNCH(ctx, k_pcg_update, gu, 256, 0, nb, n, w.minv, w.pa, w.pb, w.ap, w.x, w.r, w.z, w.part_a, w.part_b,
+                w.st);
+    }
   }
   return BARTELS_OK;
 }
@@ -775,11 +983,17 @@ static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double
     rep->refinements = pass + 1;
     // inner FP32 PCG on r64
     const double abs2 = (0.5 * target) * (0.5 * target);
-    BT_LAUNCH(ctx, k_pcg_init, gv, 256, 0, nb, n, w.r64, w.minv, w.x, w.r, w.z, w.pa, w.pb, w.part_a, w.part_b, w.st,
-              prm.inner_rel_tol * prm.inner_rel_tol, abs2, prm.max_iters - rep->iterations);
+    if (op.gl) {
+      BT_LAUNCH(ctx, k_pcg_init_f, gv, 256, 0, n, w.r64, w.x, w.r, w.pa, w.pb, w.part_a, w.st,
+                prm.inner_rel_tol * prm.inner_rel_tol, abs2, prm.max_iters - rep->iterations);
+      BT_CHECK(pcg_enqueue_prec(ctx, op, w));
+    } else {
+      BT_LAUNCH(ctx, k_pcg_init, gv, 256, 0, nb, n, w.r64, w.minv, w.x, w.r, w.z, w.pa, w.pb, w.part_a, w.part_b,
+                w.st, prm.inner_rel_tol * prm.inner_rel_tol, abs2, prm.max_iters - rep->iterations);
+    }
     for (;;) {
       BT_CUDA(cudaGraphLaunch(exec, ctx->stream));
-      ctx->launches += 3 * chunk;
+      ctx->launches += (op.gl ? 5 : 3) * chunk;
       BT_CUDA(cudaMemcpyAsync(&hs, w.st, sizeof(PcgState), cudaMemcpyDeviceToHost, ctx->stream));
       BT_CUDA(cudaStreamSynchronize(ctx->stream));
       if (hs.done) break;
@@ -789,6 +1003,51 @@ static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double
   }
   cudaGraphExecDestroy(exec);
   return status;
+}
+
+static double now_s() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// PCG on a plan's Hessian with the plan's preconditioner. The learned factor is
+// built from the current values; when its solve fails (not converged, not
+// finite) the system is solved again with block-Jacobi.
+static int plan_pcg_impl(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const double *b, double *x,
+                         const bartels_pcg_params &prm, bartels_pcg_report *rep, int *fallback, double *t_factor) {
+  const int n = 3 * plan->nV;
+  PcgOperator op;
+  op.plan = plan;
+  op.values = values;
+  op.pinned = plan->pinned;
+  if (fallback) *fallback = 0;
+  if (plan->precond == BARTELS_PRECOND_LEARNED && plan->lpcg_net) {
+    const double t0 = now_s();
+    const __nv_bfloat16 *gl = nullptr, *gu = nullptr;
+    BT_CHECK(lpcg_factor(plan->lpcg_net, plan, values, &gl, &gu));
+    BT_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (t_factor) *t_factor += now_s() - t0;
+    op.gl = gl;
+    op.gu = gu;
+    op.fp = plan->factor;
+    int s = pcg_solve(ctx, op, n, b, x, plan->w_pcg, prm, rep);
+    if (s == BARTELS_OK && rep->converged) return BARTELS_OK;
+    if (s != BARTELS_OK && s != BARTELS_E_NOT_CONVERGED && s != BARTELS_E_NONFINITE) return s;
+    if (fallback) *fallback = 1;
+    const int used = rep->iterations;
+    op.gl = op.gu = nullptr;
+    op.fp = nullptr;
+    BT_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, ctx->stream));
+    s = pcg_solve(ctx, op, n, b, x, plan->w_pcg, prm, rep);
+    rep->iterations += used;
+    return s;
+  }
+  return pcg_solve(ctx, op, n, b, x, plan->w_pcg, prm, rep);
+}
+
+int plan_pcg(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const double *b, double *x,
+             const bartels_pcg_params &prm, bartels_pcg_report *rep) {
+  BT_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * 3 * (size_t)plan->nV, ctx->stream));
+  return plan_pcg_impl(ctx, plan, values, b, x, prm, rep, nullptr, nullptr);
 }
 
 // ============================================================ Newton =======
@@ -823,10 +1082,6 @@ static ObjectiveDev objective_of(bartels_mesh_plan plan, const bartels_newton_pa
   o.f_ext = plan->f_ext;
   o.pinned = plan->pinned;
   return o;
-}
-
-static double now_s() {
-  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
 static int read_scalar(bartels_ctx ctx, const double *d, double *h) {
@@ -869,12 +1124,10 @@ int newton_iterate(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton
   // search direction d = -H^-1 g (src/search_direction_newton_sparse.cpp:12-24)
   BT_LAUNCH(ctx, k_scale_copy, grid_vec(ctx, n), 256, 0, n, -1.0, w.g, w.xt);
   BT_CUDA(cudaMemsetAsync(w.d, 0, sizeof(double) * n, ctx->stream));
-  PcgOperator op;
-  op.plan = plan;
-  op.values = w.values;
-  op.pinned = plan->pinned;
   bartels_pcg_report pr;
-  int s = pcg_solve(ctx, op, n, w.xt, w.d, plan->w_pcg, p.pcg, &pr);
+  int fb = 0;
+  int s = plan_pcg_impl(ctx, plan, w.values, w.xt, w.d, p.pcg, &pr, &fb, &rep->t_precond);
+  rep->precond_fallbacks += fb;
   rep->pcg_iterations += pr.iterations;
   rep->last_pcg_iterations = pr.iterations;
   rep->last_pcg_refinements = pr.refinements;
@@ -910,6 +1163,11 @@ int newton_iterate(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton
   rep->t_linesearch += now_s() - t3;
   rep->iterations += 1;
   return BARTELS_OK;
+}
+
+int newton_gradient(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params &p, const double *x,
+                    double *g) {
+  return gradient(ctx, plan, p.model, objective_of(plan, p), x, g);
 }
 
 int newton_solve(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params &p, double *x,

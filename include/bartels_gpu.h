@@ -263,6 +263,8 @@ typedef struct {
   int last_pcg_refinements;
   int pcg_failures;              /* searches whose PCG did not reach rel_tol */
   double energy_change;          /* f(x_new) - f(x_old) of the last step */
+  int precond_fallbacks;         /* learned-preconditioner solves redone with block-Jacobi */
+  double t_precond;              /* seconds spent building the learned factor */
 } bartels_newton_report;
 
 void bartels_newton_default_params(bartels_newton_params *p);
@@ -283,6 +285,60 @@ int bartels_newton_solve_d(bartels_ctx ctx, bartels_mesh_plan plan, const bartel
  * relative test (<= 0 to compute it now). */
 int bartels_newton_iterate_d(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params *params,
                              double *x_d, double g0_norm, int *done, bartels_newton_report *report);
+
+/* Gradient of the Newton objective at device x_d into g_d (3nV, rows of pinned
+ * vertices 0): the residual the Newton step solves against. */
+int bartels_newton_gradient_d(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params *params,
+                              const double *x_d, double *g_d);
+
+/* --------------------------------------------------- learned preconditioner -- */
+/* No counterpart in the reference, whose linear solver is Eigen::SparseLU
+ * (include/search_direction_newton_sparse.h:8). A message-passing network over
+ * the mesh vertex graph outputs a block-lower-triangular factor G on the
+ * Hessian's pattern; PCG uses M^-1 = G^T G (two triangular gathers, no
+ * triangular solves). With its output layers at zero the factor is the 3x3
+ * block-Jacobi one. It is trained on the GPU (forward, backward and Adam in
+ * this library) to minimise log of Kaporin's condition number of G H G^T,
+ * estimated with probe vectors, on Hessians the Newton solver produces. */
+typedef struct bartels_lpcg_s *bartels_lpcg;
+enum { BARTELS_PRECOND_BLOCK_JACOBI = 0, BARTELS_PRECOND_LEARNED = 1 };
+
+int bartels_lpcg_create(bartels_ctx ctx, bartels_lpcg *out);
+int bartels_lpcg_destroy(bartels_lpcg net);
+/* number of FP32 parameters (flat vector; layout in bartels_gb300/lpcg.py) */
+int bartels_lpcg_num_params(void);
+int bartels_lpcg_set_params(bartels_lpcg net, const float *params);
+/* params and/or grad (host, num_params floats each; either may be NULL) */
+int bartels_lpcg_get_params(bartels_lpcg net, float *params, float *grad);
+/* One training step on a plan's Hessian (values_d: FP32, the plan's CSR order,
+ * device; pinned vertices from bartels_newton_set_problem). Probes: nprobes
+ * Rademacher vectors from seed, plus residual_d (device, 3nV FP64) when not
+ * NULL. Computes the loss and the parameter gradient; lr > 0 also applies
+ * one Adam step (gradient clipped to norm clip when clip > 0). */
+int bartels_lpcg_train_step(bartels_lpcg net, bartels_mesh_plan plan, const float *values_d,
+                            const double *residual_d, int nprobes, unsigned seed, float lr, float clip,
+                            double *loss);
+/* Network outputs for the plan's Hessian values_d: raw (host, 9 per lower block:
+ * the 3x3 Ghat block, or d0..d5 at the diagonal) and G in lower storage (host,
+ * 9 per lower block, three scalar rows per vertex). Either may be NULL. */
+int bartels_lpcg_outputs(bartels_lpcg net, bartels_mesh_plan plan, const float *values_d, float *raw,
+                         float *g_lower);
+/* Number of lower (j <= v) and upper (j >= v) blocks of the plan's pattern. */
+int bartels_plan_factor_size(bartels_mesh_plan plan, int64_t *nnzl_blocks, int64_t *nnzu_blocks);
+/* Preconditioner of the plan's PCG solves (Newton and bartels_plan_pcg_d):
+ * BARTELS_PRECOND_BLOCK_JACOBI, or BARTELS_PRECOND_LEARNED with net (block-
+ * Jacobi is the fallback when the learned solve does not converge). */
+int bartels_plan_set_preconditioner(bartels_mesh_plan plan, int kind, bartels_lpcg net);
+/* x_d = H^-1 b_d by PCG on the plan's Hessian (values_d, or NULL for the plan's
+ * internal Hessian buffer) with the plan's preconditioner; device FP64 vectors,
+ * rows of pinned vertices excluded. */
+int bartels_plan_pcg_d(bartels_ctx ctx, bartels_mesh_plan plan, const float *values_d, const double *b_d,
+                       double *x_d, const bartels_pcg_params *params, bartels_pcg_report *report);
+/* Building block: Y = act(X W^T + bias) on the tensor cores (tcgen05, TMA);
+ * X: M x K BF16 (row stride ldx elements), W: N x K BF16, bias: N FP32 or NULL,
+ * Y: M x N FP32 (row stride ldy); N, K in {64, 128}; device pointers. */
+int bartels_gemm_bf16_d(bartels_ctx ctx, int M, int N, int K, const void *x_d, int ldx, const void *w_d,
+                        const float *bias_d, int relu, float *y_d, int ldy);
 
 /* ------------------------------------------------- device-pointer variants -- */
 /* Hessian H = coeff_M M + coeff_K K(q) of the plan's element data into FP32
