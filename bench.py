@@ -3,11 +3,17 @@
 Workload (one "step" = one Newton iteration): implicit Euler in velocity form
 (dt = 0.01) from rest under gravity, z = 0 face pinned, Neo-Hookean E = 2e6 Pa,
 nu = 0.45, rho = 1000, Hessians PSD-projected (simple_psd_fix, tol 1e-6), each
-Newton system solved by block-Jacobi PCG to 1e-8 relative residual (FP32 PCG,
-FP64 residual refinement), Newton to 1e-8 relative gradient norm; when a time
-step converges the next one starts. Synthetic, seeded inputs (no dataset).
+Newton system solved by PCG to 1e-8 relative residual (FP32 PCG, FP64 residual
+refinement), Newton to 1e-8 relative gradient norm; when a time step converges
+the next one starts. Synthetic, seeded inputs (no dataset).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+The headline value uses the learned preconditioner (the network's factor G is
+rebuilt from each Newton Hessian inside the timed region; M^-1 = G^T G), with
+weights trained by bartels_gb300/train_lpcg.py on other cubes (n = 24..48,
+three material models). The same workload is then timed with block-Jacobi PCG
+on the same GPU ("jacobi_pcg" in the JSON line).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--precond jacobi]
 
 Prints one JSON line. Under torchrun (N > 1) every rank runs an independent
 replica on its own GPU (the path does not shard: replicas only) and rank 0
@@ -45,6 +51,9 @@ def parse():
     ap.add_argument("--no-psd", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precond", default="learned", choices=["learned", "jacobi"])
+    ap.add_argument("--weights", default=os.path.join(ROOT, "bartels_gb300", "weights", "lpcg_neohookean.npz"))
+    ap.add_argument("--no-jacobi-arm", action="store_true", help="skip the block-Jacobi comparison run")
     return ap.parse_args()
 
 
@@ -168,47 +177,67 @@ def run_gpu(args, rank, world):
                            mass_coeff=1.0, scale=pb["dt"], force_scale=pb["dt"], max_iterations=100)
     x = torch.zeros(3 * nV, dtype=torch.float64, device=f"cuda:{dev}")
     xp = C.c_void_p(x.data_ptr())
-    state = {"g0": -1.0, "steps": 0}
-    rep = _lib.NewtonReport()
+    net = None
+    if args.precond == "learned":
+        from bartels_gb300 import lpcg
+        net = lpcg.LearnedPreconditioner.load(args.weights, ctx)
 
-    def newton_step():
-        """Run until one Newton iteration (Hessian + PCG + line search) completed."""
-        while True:
-            done = C.c_int()
-            _lib.check(L.bartels_newton_iterate_d(ctx.handle, plan.handle, C.byref(prm), xp, state["g0"],
-                                                  C.byref(done), C.byref(rep)), "newton_iterate")
-            if state["g0"] < 0:
-                state["g0"] = rep.grad_norm
-            if done.value:
-                # converged time step: q_t += dt v, v_t = v; next step starts from v
-                _lib.check(L.bartels_newton_advance_implicit_euler_d(ctx.handle, plan.handle, pb["dt"], xp),
-                           "advance")
-                state["g0"] = -1.0
-                state["steps"] += 1
-                continue
-            return
+    def timed_newton(use_learned):
+        """W warm-up and K timed Newton iterations from rest (fresh state)."""
+        if use_learned:
+            net.attach(plan)
+        else:
+            L.bartels_plan_set_preconditioner(plan.handle, _lib.PRECOND_BLOCK_JACOBI, None)
+        plan.set_problem(q_base=qt, x_hat=vt, f_ext=f_g, pinned=pb["pinned"])
+        x.zero_()
+        state = {"g0": -1.0, "steps": 0}
+        rep = _lib.NewtonReport()
 
-    for _ in range(args.warmup):
-        newton_step()
-    ctx.synchronize()
-    rep_before = (rep.iterations, rep.pcg_iterations, rep.ls_iterations)
-    launches0 = ctx.kernel_launches
-    if world > 1:
-        torch.distributed.barrier()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with Clocks(dev) as clk:
-        ctx.synchronize()
-        ev0.record(stream)
-        for _ in range(args.steps):
+        def newton_step():
+            """Run until one Newton iteration (Hessian + PCG + line search) completed."""
+            while True:
+                done = C.c_int()
+                _lib.check(L.bartels_newton_iterate_d(ctx.handle, plan.handle, C.byref(prm), xp, state["g0"],
+                                                      C.byref(done), C.byref(rep)), "newton_iterate")
+                if state["g0"] < 0:
+                    state["g0"] = rep.grad_norm
+                if done.value:
+                    # converged time step: q_t += dt v, v_t = v; next step starts from v
+                    _lib.check(L.bartels_newton_advance_implicit_euler_d(ctx.handle, plan.handle, pb["dt"], xp),
+                               "advance")
+                    state["g0"] = -1.0
+                    state["steps"] += 1
+                    continue
+                return
+
+        for _ in range(args.warmup):
             newton_step()
-        ev1.record(stream)
         ctx.synchronize()
-        torch.cuda.synchronize()
-    ms = ev0.elapsed_time(ev1)
-    launches = ctx.kernel_launches - launches0
-    ms = reduce_max_ms(ms, world, f"cuda:{dev}")
-    pcg_its = rep.pcg_iterations - rep_before[1]
-    newton_its = rep.iterations - rep_before[0]
+        before = (rep.iterations, rep.pcg_iterations, rep.ls_iterations, rep.precond_fallbacks, rep.t_precond)
+        launches0 = ctx.kernel_launches
+        if world > 1:
+            torch.distributed.barrier()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with Clocks(dev) as clk:
+            ctx.synchronize()
+            ev0.record(stream)
+            for _ in range(args.steps):
+                newton_step()
+            ev1.record(stream)
+            ctx.synchronize()
+            torch.cuda.synchronize()
+        ms = reduce_max_ms(ev0.elapsed_time(ev1), world, f"cuda:{dev}")
+        return dict(ms=ms, launches=ctx.kernel_launches - launches0, clocks=clk.summary(), rep=rep,
+                    newton_its=rep.iterations - before[0], pcg_its=rep.pcg_iterations - before[1],
+                    ls_its=rep.ls_iterations - before[2], fallbacks=rep.precond_fallbacks - before[3],
+                    t_precond=rep.t_precond - before[4], steps=state["steps"])
+
+    main_arm = timed_newton(net is not None)
+    jac = main_arm if net is None else (None if args.no_jacobi_arm else timed_newton(False))
+    L.bartels_plan_set_preconditioner(plan.handle, _lib.PRECOND_BLOCK_JACOBI, None)
+    ms, launches, rep = main_arm["ms"], main_arm["launches"], main_arm["rep"]
+    pcg_its, newton_its = main_arm["pcg_its"], main_arm["newton_its"]
+    state = {"steps": main_arm["steps"]}
 
     # --- roofline of the dominant kernel (PCG SpMV) and the dq2 assembly, live
     n_dof = 3 * nV
@@ -257,6 +286,8 @@ def run_gpu(args, rank, world):
     e2e = None
     if rank == 0 and args.e2e_steps > 0:
         plan.set_problem(q_base=qt, x_hat=vt, f_ext=f_g, pinned=pb["pinned"])
+        if net is not None:
+            net.attach(plan)
         v_host = np.zeros(3 * nV)
         its = 0
         t = 0.0
@@ -268,29 +299,41 @@ def run_gpu(args, rank, world):
             its += r.iterations
             h2d += v_host.nbytes
             d2h += v_out.nbytes
+        L.bartels_plan_set_preconditioner(plan.handle, _lib.PRECOND_BLOCK_JACOBI, None)
         e2e = {"value": its / t if t > 0 else None, "unit": UNIT,
                "h2d_bytes_per_step": h2d // args.e2e_steps, "d2h_bytes_per_step": d2h // args.e2e_steps,
                "newton_iterations": its, "seconds": t}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        counts = {"pcg_per_newton": pcg_its / max(newton_its, 1),
-                  "ls_per_newton": (rep.ls_iterations - rep_before[2]) / max(newton_its, 1)}
+        ref_arm = jac if jac is not None else main_arm
+        counts = {"pcg_per_newton": ref_arm["pcg_its"] / max(ref_arm["newton_its"], 1),
+                  "ls_per_newton": ref_arm["ls_its"] / max(ref_arm["newton_its"], 1)}
         est, parts, threads, _ = cpu_newton_sample(pb, args, counts)
         cpu = {"value": 1.0 / est[0], "unit": UNIT, "cores": threads, "kind": "port",
                "sample": cpu_sample_text(counts, args.n).replace("from the GPU run of the same workload", "from this run"),
                "components": parts}
 
+    precond_name = "learned factor G^T G" if net is not None else "block-Jacobi"
+    value = replica_value(newton_its, world, ms)
+    jacobi_pcg = None
+    if jac is not None and net is not None:
+        jv = replica_value(jac["newton_its"], world, jac["ms"])
+        jacobi_pcg = {"value": jv, "unit": UNIT, "ms_per_step": jac["ms"] / max(jac["newton_its"], 1),
+                      "pcg_iters_per_newton": jac["pcg_its"] / max(jac["newton_its"], 1),
+                      "newton_iterations": jac["newton_its"], "clocks": jac["clocks"],
+                      "learned_over_jacobi": value / jv if jv > 0 else None}
     out = {
-        "metric": METRIC, "value": replica_value(newton_its, world, ms), "unit": UNIT, "n_gpus": world,
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / max(newton_its, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded Kuhn cube, gravity)",
         "config": {"workload": f"implicit-Euler Newton, Neo-Hookean Kuhn cube n={args.n} "
                                f"({nV} vertices, {nT} tets), dt=0.01, z=0 pinned, PSD "
-                               f"{'off' if args.no_psd else 'simple_psd_fix 1e-6'}, block-Jacobi PCG 1e-8, "
-                               "Newton 1e-8 relative", "preconditioner": "block-Jacobi",
-                   "learned_pcg": "not built", "parallelism": f"replicas x{world}",
+                               f"{'off' if args.no_psd else 'simple_psd_fix 1e-6'}, {precond_name} PCG 1e-8, "
+                               "Newton 1e-8 relative", "preconditioner": precond_name,
+                   "learned_pcg_weights": os.path.relpath(args.weights, ROOT) if net is not None else None,
+                   "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (CSR values %.0f MB)" % (4 * nnz / 1e6)},
         "newton_iterations": newton_its, "pcg_iterations": pcg_its,
         "pcg_iters_per_newton": pcg_its / max(newton_its, 1),
@@ -300,7 +343,12 @@ def run_gpu(args, rank, world):
         "kernels": {"dq2_fused_assembly": {"us_per_launch": hess_s * 1e6, "compulsory_bytes": hess_bytes,
                                            "achieved_gbs": hess_bytes / hess_s / 1e9,
                                            "frac": hess_bytes / hess_s / 1e9 / peak}},
-        "clocks": clk.summary(), "gpu_launches": int(launches), "e2e": e2e, "cpu_baseline": cpu,
+        "jacobi_pcg": jacobi_pcg,
+        "learned_precond": None if net is None else {
+            "factor_build_ms_per_newton": 1e3 * main_arm["t_precond"] / max(newton_its, 1),
+            "fallbacks_to_block_jacobi": main_arm["fallbacks"],
+            "pcg_us_per_iteration": 1e6 * rep.t_pcg / max(rep.pcg_iterations, 1)},
+        "clocks": main_arm["clocks"], "gpu_launches": int(launches), "e2e": e2e, "cpu_baseline": cpu,
         "setup_s": {"plan": t_plan}, "time_steps_completed": state["steps"],
         "stage_seconds": {"gradient": rep.t_gradient, "hessian": rep.t_hessian, "pcg": rep.t_pcg,
                           "linesearch": rep.t_linesearch},
