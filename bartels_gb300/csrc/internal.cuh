@@ -92,7 +92,7 @@ struct bartels_ctx_s {
   // overridable with BARTELS_SPMV_LANES)
   int spmv_lanes = 16;
   // lanes per vertex row in the triangular factor passes (4 or 8; BARTELS_TRI_LANES)
-  int tri_lanes = 8;
+  int tri_lanes = 4;
   // pinned host staging for small read-backs
   double *host_scalars = nullptr;
   // device scratch for reductions

@@ -195,7 +195,8 @@ class System:
         self.plan, self.values, self.residual, self.meta = plan, values, residual, meta
 
 
-def sample_configs(count: int, seed: int = 0, n_range=(8, 20), models=("neohookean",)):
+def sample_configs(count: int, seed: int = 0, n_range=(8, 20), models=("neohookean",), ratio_range=(30.0, 3e4),
+                   nu_range=(0.30, 0.48), stretch=0.15):
     """Implicit-Euler cubes with a spread of stiffness-to-inertia ratios
     E dt^2 / (rho h^2) around the n=96 benchmark's (1.8e3), Poisson ratios,
     initial stretches and (optionally) material models."""
@@ -203,14 +204,14 @@ def sample_configs(count: int, seed: int = 0, n_range=(8, 20), models=("neohooke
     out = []
     for _ in range(count):
         n = int(rng.integers(n_range[0], n_range[1] + 1))
-        ratio = float(np.exp(rng.uniform(np.log(30.0), np.log(3e4))))
+        ratio = float(np.exp(rng.uniform(np.log(ratio_range[0]), np.log(ratio_range[1]))))
         young = float(np.exp(rng.uniform(np.log(1e5), np.log(1e7))))
-        nu = float(rng.uniform(0.30, 0.48))
+        nu = float(rng.uniform(*nu_range))
         rho, h = 1000.0, 1.0 / n
         dt = math.sqrt(ratio * rho * h * h / young)
-        stretch = rng.uniform(0.85, 1.15, size=3)
+        st = rng.uniform(1.0 - stretch, 1.0 + stretch, size=3)
         model = models[int(rng.integers(len(models)))]
-        out.append(dict(n=n, young=young, nu=nu, rho=rho, dt=dt, ratio=ratio, stretch=stretch.tolist(), model=model))
+        out.append(dict(n=n, young=young, nu=nu, rho=rho, dt=dt, ratio=ratio, stretch=st.tolist(), model=model))
     return out
 
 

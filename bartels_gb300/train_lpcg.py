@@ -1,6 +1,9 @@
 """Train the learned PCG preconditioner on the GPU and write its weights.
 
-    python -m bartels_gb300.train_lpcg --systems 48 --steps 3000 --out bartels_gb300/weights/lpcg_neohookean.npz
+    python -m bartels_gb300.train_lpcg --systems 32 --steps 4000 --nmin 24 --nmax 48 --probes 8 \
+        --models neohookean,stvk,corotational --eval 32 --out bartels_gb300/weights/lpcg_neohookean.npz
+    python -m bartels_gb300.train_lpcg --systems 0 --steps 0 --init bartels_gb300/weights/lpcg_neohookean.npz --eval 96
+        (evaluation only: PCG iterations and seconds, learned vs block-Jacobi)
 
 Training systems are (Hessian, residual) pairs from implicit-Euler Newton
 iterations on Neo-Hookean Kuhn cubes of random size, stiffness, Poisson ratio,
@@ -37,12 +40,16 @@ def evaluate(ctx, net, sizes, model="neohookean", newton_iters=2, log=print):
                     net.attach(sysm.plan)
                 else:
                     lpcg.use_block_jacobi(sysm.plan)
+                torch.cuda.synchronize()
+                t = time.perf_counter()
                 rep = lpcg.plan_pcg(sysm.plan, sysm.values, b, x)
-                res[kind] = (rep.iterations, bool(rep.converged), rep.rel_residual)
+                torch.cuda.synchronize()
+                res[kind] = (rep.iterations, bool(rep.converged), rep.rel_residual, time.perf_counter() - t)
             lpcg.use_block_jacobi(sysm.plan)
             row = dict(n=n, newton_iteration=sysm.meta["newton_iteration"], jacobi=res["jacobi"][0],
                        learned=res["learned"][0], converged=res["jacobi"][1] and res["learned"][1],
-                       ratio=res["learned"][0] / max(res["jacobi"][0], 1))
+                       ratio=res["learned"][0] / max(res["jacobi"][0], 1),
+                       seconds_jacobi=round(res["jacobi"][3], 4), seconds_learned=round(res["learned"][3], 4))
             out.append(row)
             log(json.dumps(row))
     return out
@@ -63,6 +70,9 @@ def main(argv=None):
     ap.add_argument("--out", default=None)
     ap.add_argument("--init", default=None, help="start from these weights")
     ap.add_argument("--models", default="neohookean", help="comma-separated material models of the training cubes")
+    ap.add_argument("--ratio", default="30,30000", help="range of E dt^2 / (rho h^2) of the training cubes")
+    ap.add_argument("--nu", default="0.30,0.48", help="range of Poisson ratios")
+    ap.add_argument("--stretch", type=float, default=0.15, help="initial per-axis stretch range 1 +- s")
     args = ap.parse_args(argv)
     import bartels_gb300 as bg
     from . import lpcg
@@ -70,21 +80,27 @@ def main(argv=None):
     t0 = time.time()
     systems = []
     models = tuple(m for m in args.models.split(",") if m)
-    for cfg in lpcg.sample_configs(args.systems, seed=args.seed, n_range=(args.nmin, args.nmax), models=models):
+    rr = tuple(float(v) for v in args.ratio.split(","))
+    nr = tuple(float(v) for v in args.nu.split(","))
+    for cfg in lpcg.sample_configs(args.systems, seed=args.seed, n_range=(args.nmin, args.nmax), models=models,
+                                   ratio_range=rr, nu_range=nr, stretch=args.stretch):
         systems += lpcg.newton_systems(ctx, cfg, newton_iters=args.newton_iters)
     t_data = time.time() - t0
-    print(f"{len(systems)} systems from {args.systems} Newton runs in {t_data:.1f}s", flush=True)
+    if args.systems:
+        print(f"{len(systems)} systems from {args.systems} Newton runs in {t_data:.1f}s", flush=True)
     net = lpcg.LearnedPreconditioner.load(args.init, ctx) if args.init else lpcg.LearnedPreconditioner(ctx,
                                                                                                       seed=args.seed)
     t1 = time.time()
-    hist = lpcg.train(net, systems, args.steps, lr=args.lr, lr_end=args.lr_end, nprobes=args.probes,
-                      seed=args.seed, log=lambda s: print(s, flush=True))
-    t_train = time.time() - t1
-    print(f"training: {args.steps} steps in {t_train:.1f}s ({1e3 * t_train / max(args.steps, 1):.2f} ms/step)",
-          flush=True)
+    hist = []
+    if args.steps and systems:
+        hist = lpcg.train(net, systems, args.steps, lr=args.lr, lr_end=args.lr_end, nprobes=args.probes,
+                          seed=args.seed, log=lambda s: print(s, flush=True))
+        t_train = time.time() - t1
+        print(f"training: {args.steps} steps in {t_train:.1f}s ({1e3 * t_train / max(args.steps, 1):.2f} ms/step)",
+              flush=True)
     sizes = [int(s) for s in args.eval.split(",") if s]
     rows = evaluate(ctx, net, sizes)
-    if args.out:
+    if args.out and hist:
         net.save(args.out, loss_first=np.mean(hist[:20]), loss_last=np.mean(hist[-50:]), steps=args.steps,
                  systems=len(systems), seed=args.seed, lr=args.lr, probes=args.probes,
                  eval_ratio=np.mean([r["ratio"] for r in rows]) if rows else np.nan)
