@@ -656,13 +656,15 @@ __device__ __forceinline__ void tri_row_acc4(int sl, const int *__restrict__ col
   }
 }
 
-// y = G r (lower rows). Rows of pinned vertices give 0.
+// y = G r (lower rows; rows of pinned vertices give 0) and r.z = r^T G^T G r =
+// |y|^2; beta = r.z / r.z_old in the last block.
 template <int G>
 __global__ void __launch_bounds__(256)
 k_pcg_prec_lower(int nV, const int4 *__restrict__ meta, const int *__restrict__ bcol,
                  const __nv_bfloat16 *__restrict__ gl, const float *__restrict__ r, float *__restrict__ y,
-                 const unsigned char *__restrict__ pinned, const PcgState *__restrict__ st) {
+                 const unsigned char *__restrict__ pinned, double *__restrict__ part, PcgState *__restrict__ st) {
   if (st->done) return;
+  float acc = 0.f;
   BT_ROW_LOOP_BEGIN(G)
   float s0 = 0.f, s1 = 0.f, s2 = 0.f;
   if (active) {
@@ -677,34 +679,7 @@ k_pcg_prec_lower(int nV, const int4 *__restrict__ meta, const int *__restrict__ 
     y[3 * v] = s0;
     y[3 * v + 1] = s1;
     y[3 * v + 2] = s2;
-  }
-  BT_ROW_LOOP_END
-}
-
-// z = G^T y (upper rows), partials of r.z; beta = r.z / r.z_old in the last block.
-template <int G>
-__global__ void __launch_bounds__(256)
-k_pcg_prec_upper(int nV, const int4 *__restrict__ meta, const int *__restrict__ bcol,
-                 const __nv_bfloat16 *__restrict__ gu, const float *__restrict__ y, const float *__restrict__ r,
-                 float *__restrict__ z, const unsigned char *__restrict__ pinned, double *__restrict__ part,
-                 PcgState *__restrict__ st) {
-  if (st->done) return;
-  float acc = 0.f;
-  BT_ROW_LOOP_BEGIN(G)
-  float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-  if (active) {
-    const int4 m = __ldg(meta + v);
-    const int d = m.w & 0xFFFF, nu = (m.w >> 16) - d;
-    tri_row_acc4<G>(sl, bcol + m.x + d, gu + m.z, 3 * nu, padded_row(nu), [&](int c) { return __ldcg(y + c); }, s0,
-                    s1, s2);
-  }
-  group_reduce<G>(s0, s1, s2);
-  if (active && sl == 0) {
-    if (pinned && pinned[v]) s0 = s1 = s2 = 0.f;
-    z[3 * v] = s0;
-    z[3 * v + 1] = s1;
-    z[3 * v + 2] = s2;
-    acc += __ldcg(r + 3 * v) * s0 + __ldcg(r + 3 * v + 1) * s1 + __ldcg(r + 3 * v + 2) * s2;
+    acc += s0 * s0 + s1 * s1 + s2 * s2;
   }
   BT_ROW_LOOP_END
   double s = cta_sum_f(acc);
@@ -717,6 +692,36 @@ k_pcg_prec_upper(int nV, const int4 *__restrict__ meta, const int *__restrict__ 
       st->count = 0;
     }
   }
+}
+
+// z = G^T y (upper rows) and the next direction p = z + beta p_old for the own
+// rows (p double-buffered by iteration parity, as k_pcg_dir does).
+template <int G>
+__global__ void __launch_bounds__(256)
+k_pcg_prec_upper(int nV, const int4 *__restrict__ meta, const int *__restrict__ bcol,
+                 const __nv_bfloat16 *__restrict__ gu, const float *__restrict__ y, float *__restrict__ pa,
+                 float *__restrict__ pb, const unsigned char *__restrict__ pinned, const PcgState *__restrict__ st) {
+  if (st->done) return;
+  const int it = st->it;
+  const float beta = st->beta;
+  const float *p_old = (it & 1) ? pa : pb;
+  float *p_new = (it & 1) ? pb : pa;
+  BT_ROW_LOOP_BEGIN(G)
+  float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+  if (active) {
+    const int4 m = __ldg(meta + v);
+    const int d = m.w & 0xFFFF, nu = (m.w >> 16) - d;
+    tri_row_acc4<G>(sl, bcol + m.x + d, gu + m.z, 3 * nu, padded_row(nu), [&](int c) { return __ldcg(y + c); }, s0,
+                    s1, s2);
+  }
+  group_reduce<G>(s0, s1, s2);
+  if (active && sl == 0) {
+    if (pinned && pinned[v]) s0 = s1 = s2 = 0.f;
+    p_new[3 * v] = s0 + beta * __ldcg(p_old + 3 * v);
+    p_new[3 * v + 1] = s1 + beta * __ldcg(p_old + 3 * v + 1);
+    p_new[3 * v + 2] = s2 + beta * __ldcg(p_old + 3 * v + 2);
+  }
+  BT_ROW_LOOP_END
 }
 
 // x += alpha p; r -= alpha Ap; r.r, iteration count and convergence test
@@ -829,6 +834,7 @@ static int grid_spmv(bartels_ctx ctx, int64_t rows) {
 }
 
 
+// z = G^T G r, r.z and beta, then p = z + beta p (two launches)
 static int pcg_enqueue_prec(bartels_ctx ctx, const PcgOperator &op, const PcgWork &w) {
   const bartels_mesh_plan plan = op.plan;
   // triangular rows are about half as long as the matrix rows (4 or 8 lanes, 4 columns a lane)
@@ -836,9 +842,9 @@ static int pcg_enqueue_prec(bartels_ctx ctx, const PcgOperator &op, const PcgWor
   const int gt = grid_spmv(ctx, (int64_t)plan->nV * G / 32 + 1);
 #define BT_T(G_)                                                                                                 \
   BT_LAUNCH(ctx, k_pcg_prec_lower<G_>, gt, 256, 0, plan->nV, op.fp->meta, plan->bcol, op.gl, w.r, w.ap, op.pinned, \
-            w.st);                                                                                               \
-  BT_LAUNCH(ctx, k_pcg_prec_upper<G_>, gt, 256, 0, plan->nV, op.fp->meta, plan->bcol, op.gu, w.ap, w.r, w.z,       \
-            op.pinned, w.part_b, w.st)
+            w.part_b, w.st);                                                                                     \
+  BT_LAUNCH(ctx, k_pcg_prec_upper<G_>, gt, 256, 0, plan->nV, op.fp->meta, plan->bcol, op.gu, w.ap, w.pa, w.pb,     \
+            op.pinned, w.st)
   if (G == 4) {
     BT_T(4);
   } else {
@@ -855,7 +861,8 @@ static int pcg_enqueue_iters(bartels_ctx ctx, const PcgOperator &op, const PcgWo
   const int gu = grid_vec(ctx, (nb + 3) / 4);
   const int gd = grid_vec(ctx, (n + 3) / 4);
   for (int i = 0; i < iters; ++i) {
-    BT_LAUNCH(ctx, k_pcg_dir, gd, 256, 0, n, w.z, w.pa, w.pb, w.st);
+    // with the factor preconditioner the direction is formed by k_pcg_prec_upper
+    if (!fac) BT_LAUNCH(ctx, k_pcg_dir, gd, 256, 0, n, w.z, w.pa, w.pb, w.st);
     if (blk) {
 #define BT_K1(G)                                                                                                 \
   BT_LAUNCH(ctx, k_pcg_spmv_blk<G>, gs, 256, 0, op.plan->nV, op.plan->brp, op.plan->bcol, op.values, w.pa, w.pb, \
@@ -993,7 +1000,7 @@ static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double
     }
     for (;;) {
       BT_CUDA(cudaGraphLaunch(exec, ctx->stream));
-      ctx->launches += (op.gl ? 5 : 3) * chunk;
+      ctx->launches += (op.gl ? 4 : 3) * chunk;
       BT_CUDA(cudaMemcpyAsync(&hs, w.st, sizeof(PcgState), cudaMemcpyDeviceToHost, ctx->stream));
       BT_CUDA(cudaStreamSynchronize(ctx->stream));
       if (hs.done) break;
