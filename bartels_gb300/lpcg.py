@@ -260,8 +260,32 @@ def newton_systems(ctx: Context, cfg: dict, newton_iters: int = 3, model: str | 
     return out
 
 
+def perturbed_systems(ctx: Context, cfg: dict, count: int = 1, noise: float = 0.02, model: str | None = None):
+    """Hessians M + dt^2 K(q) of one configuration at perturbed rest states
+    q = X + noise h U(-1, 1) (no residual): the near-rest systems the first
+    Newton iterations of a simulation see."""
+    import torch
+    model = model or cfg.get("model", "neohookean")
+    dev = torch.device(f"cuda:{ctx.device}")
+    V, E = kuhn_cube(cfg["n"])
+    plan = MeshPlan(V, E, ctx)
+    plan.set_element_data(params=material_params(model, len(E), cfg["young"], cfg["nu"]),
+                          density=np.full(len(E), cfg["rho"]))
+    plan.set_problem(pinned=(np.abs(V[:, 2]) <= 1e-12).astype(np.uint8))
+    rng = np.random.default_rng(cfg.get("seed", 0))
+    out = []
+    for k in range(count):
+        q = torch.from_numpy((V + noise / cfg["n"] * rng.uniform(-1, 1, V.shape)).ravel()).to(dev)
+        values = torch.empty(plan.nnz, dtype=torch.float32, device=dev)
+        check(lib().bartels_plan_hessian_d(ctx.handle, plan.handle, MODELS[model], _lib.PSD_SIMPLE_FIX, 1e-6, 0,
+                                           cfg["dt"] ** 2, 1.0, _ptr(q), _ptr(values)), "bartels_plan_hessian_d")
+        out.append(System(plan, values, None, dict(cfg, sample=k)))
+    ctx.synchronize()
+    return out
+
+
 def train(net: LearnedPreconditioner, systems, steps: int, lr: float = 2e-3, lr_end: float = 1e-4,
-          nprobes: int = 4, seed: int = 0, log=None):
+          nprobes: int = 4, seed: int = 0, log=None, residual_probe: bool = True):
     """Adam on the Kaporin loss, cycling through the systems (cosine learning rate)."""
     rng = np.random.default_rng(seed)
     hist = []
@@ -269,7 +293,7 @@ def train(net: LearnedPreconditioner, systems, steps: int, lr: float = 2e-3, lr_
     for s in range(steps):
         sysm = systems[int(rng.integers(len(systems)))]
         a = lr_end + 0.5 * (lr - lr_end) * (1 + math.cos(math.pi * s / max(steps, 1)))
-        loss = net.train_step(sysm.plan, sysm.values, sysm.residual, nprobes=nprobes,
+        loss = net.train_step(sysm.plan, sysm.values, sysm.residual if residual_probe else None, nprobes=nprobes,
                               seed=int(rng.integers(1 << 31)), lr=a, clip=1.0)
         hist.append(loss)
         if log and (s % max(steps // 20, 1) == 0 or s == steps - 1):

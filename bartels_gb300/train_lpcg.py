@@ -73,6 +73,9 @@ def main(argv=None):
     ap.add_argument("--ratio", default="30,30000", help="range of E dt^2 / (rho h^2) of the training cubes")
     ap.add_argument("--nu", default="0.30,0.48", help="range of Poisson ratios")
     ap.add_argument("--stretch", type=float, default=0.15, help="initial per-axis stretch range 1 +- s")
+    ap.add_argument("--kind", default="newton", choices=["newton", "rest"],
+                    help="newton: Newton-iteration Hessians with residuals; rest: Hessians at perturbed rest states")
+    ap.add_argument("--no-residual", action="store_true", help="train with Rademacher probes only")
     args = ap.parse_args(argv)
     import bartels_gb300 as bg
     from . import lpcg
@@ -84,7 +87,11 @@ def main(argv=None):
     nr = tuple(float(v) for v in args.nu.split(","))
     for cfg in lpcg.sample_configs(args.systems, seed=args.seed, n_range=(args.nmin, args.nmax), models=models,
                                    ratio_range=rr, nu_range=nr, stretch=args.stretch):
-        systems += lpcg.newton_systems(ctx, cfg, newton_iters=args.newton_iters)
+        cfg["seed"] = len(systems)
+        if args.kind == "newton":
+            systems += lpcg.newton_systems(ctx, cfg, newton_iters=args.newton_iters)
+        else:
+            systems += lpcg.perturbed_systems(ctx, cfg, count=args.newton_iters)
     t_data = time.time() - t0
     if args.systems:
         print(f"{len(systems)} systems from {args.systems} Newton runs in {t_data:.1f}s", flush=True)
@@ -94,7 +101,7 @@ def main(argv=None):
     hist = []
     if args.steps and systems:
         hist = lpcg.train(net, systems, args.steps, lr=args.lr, lr_end=args.lr_end, nprobes=args.probes,
-                          seed=args.seed, log=lambda s: print(s, flush=True))
+                          seed=args.seed, log=lambda s: print(s, flush=True), residual_probe=not args.no_residual)
         t_train = time.time() - t1
         print(f"training: {args.steps} steps in {t_train:.1f}s ({1e3 * t_train / max(args.steps, 1):.2f} ms/step)",
               flush=True)

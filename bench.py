@@ -9,7 +9,7 @@ the next one starts. Synthetic, seeded inputs (no dataset).
 
 The headline value uses the learned preconditioner (the network's factor G is
 rebuilt from each Newton Hessian inside the timed region; M^-1 = G^T G), with
-weights trained by bartels_gb300/train_lpcg.py on other cubes (n = 24..48,
+weights trained by bartels_gb300/train_lpcg.py on other cubes (n = 5..24,
 three material models). The same workload is then timed with block-Jacobi PCG
 on the same GPU ("jacobi_pcg" in the JSON line).
 

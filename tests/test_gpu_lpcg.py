@@ -193,22 +193,23 @@ def test_residual_probe_training_step_runs():
 
 
 def test_training_reduces_pcg_iterations():
-    """Adam steps on Newton systems of small cubes (Neo-Hookean, StVK and
-    corotational, random stiffness, time step and stretch): on an unseen, larger
-    Neo-Hookean cube the learned factor needs fewer PCG iterations than
-    block-Jacobi, and both reach the same solution."""
+    """600 Adam steps (about 1.5 s) on Hessians of small cubes (n = 5..12,
+    Neo-Hookean / StVK / corotational, random stiffness and time step, perturbed
+    rest states): on an unseen, larger Neo-Hookean cube the learned factor needs
+    far fewer PCG iterations than block-Jacobi, and both reach the same solution."""
     torch = _torch()
     import bartels_gb300 as bg
     from bartels_gb300 import lpcg
     ctx = bg.Context.default()
-    cfgs = lpcg.sample_configs(8, seed=4, n_range=(14, 22), models=("neohookean", "stvk", "corotational"))
+    cfgs = lpcg.sample_configs(12, seed=4, n_range=(5, 12), models=("neohookean", "stvk", "corotational"))
     systems = []
-    for cfg in cfgs:
-        systems += lpcg.newton_systems(ctx, cfg, newton_iters=2)
+    for k, cfg in enumerate(cfgs):
+        cfg["seed"] = k
+        systems += lpcg.perturbed_systems(ctx, cfg, count=2)
     net = lpcg.LearnedPreconditioner(ctx, seed=0)
-    hist = lpcg.train(net, systems, steps=600, lr=2e-3, lr_end=2e-4, nprobes=8, seed=0)
+    hist = lpcg.train(net, systems, steps=600, lr=3e-3, lr_end=3e-4, nprobes=8, seed=0)
     assert np.mean(hist[-50:]) < np.mean(hist[:10]) - 0.05
-    n = 32
+    n = 24
     test_cfg = dict(n=n, young=2e6, nu=0.45, rho=1000.0, dt=0.01 * 96 / n, stretch=[1.0, 1.0, 1.0])
     sysm = lpcg.newton_systems(ctx, test_cfg, newton_iters=1, model="neohookean")[0]
     b = sysm.residual.clone()
@@ -220,6 +221,30 @@ def test_training_reduces_pcg_iterations():
     rl = lpcg.plan_pcg(sysm.plan, sysm.values, b, x2)
     lpcg.use_block_jacobi(sysm.plan)
     assert rj.converged and rl.converged
-    assert rl.iterations <= 0.9 * rj.iterations, (rl.iterations, rj.iterations)
+    assert rl.iterations <= 0.8 * rj.iterations, (rl.iterations, rj.iterations)
     assert torch.linalg.norm(x - x2) <= 1e-6 * torch.linalg.norm(x)
+    net.close()
+
+
+def test_committed_weights_beat_block_jacobi():
+    """The shipped weights (bartels_gb300/weights) on a Neo-Hookean cube the
+    training never saw (n = 40, the benchmark's E dt^2 / (rho h^2))."""
+    torch = _torch()
+    import bartels_gb300 as bg
+    from bartels_gb300 import lpcg
+    ctx = bg.Context.default()
+    net = lpcg.LearnedPreconditioner.load(lpcg.WEIGHTS, ctx)
+    n = 40
+    cfg = dict(n=n, young=2e6, nu=0.45, rho=1000.0, dt=0.01 * 96 / n, stretch=[1.0, 1.0, 1.0])
+    for sysm in lpcg.newton_systems(ctx, cfg, newton_iters=2, model="neohookean"):
+        b = sysm.residual.clone()
+        x = torch.zeros_like(b)
+        lpcg.use_block_jacobi(sysm.plan)
+        rj = lpcg.plan_pcg(sysm.plan, sysm.values, b, x)
+        net.attach(sysm.plan)
+        x2 = torch.zeros_like(b)
+        rl = lpcg.plan_pcg(sysm.plan, sysm.values, b, x2)
+        lpcg.use_block_jacobi(sysm.plan)
+        assert rj.converged and rl.converged
+        assert rl.iterations <= 0.7 * rj.iterations, (rl.iterations, rj.iterations)
     net.close()
