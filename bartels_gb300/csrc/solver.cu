@@ -1156,7 +1156,10 @@ int newton_iterate(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton
   for (;;) {
     BT_CHECK(energy_diff(ctx, plan, p.model, obj, x, w.d, alpha, w.scal));
     BT_CHECK(read_scalar(ctx, w.scal, &df));
-    if (!(df > p.ls_c * gd && it < p.max_iterations_ls)) break;
+    // the reference's test (a NaN energy, e.g. from an inverted Neo-Hookean
+    // element, also backtracks instead of being accepted)
+    const bool reject = !std::isfinite(df) || df > p.ls_c * gd;
+    if (!(reject && it < p.max_iterations_ls)) break;
     alpha *= p.ls_p;
     it++;
   }

@@ -81,3 +81,52 @@ def material_params(model: str, nT: int, young: float, nu: float):
     else:
         row = (lam, mu)
     return np.tile(np.array(row, dtype=np.float64), (nT, 1))
+
+
+def carved_cube(n: int, centers, radii, size: float = 1.0):
+    """Voxel carving of the n^3 Kuhn cube: keep the cells whose centre lies in
+    the union of the spheres (centers (k, 3), radii (k,)), then the largest
+    vertex-connected component. Returns V, E (renumbered) and the kept cell
+    centres per tet (for per-tet material fields)."""
+    V, E = kuhn_cube(n, size)
+    centers = np.asarray(centers, dtype=np.float64)
+    radii = np.asarray(radii, dtype=np.float64)
+    c = V[E].mean(axis=1)  # tet centroids
+    cell = np.arange(len(E)) // 6
+    m = n
+    ci = cell % m
+    cj = (cell // m) % m
+    ck = cell // (m * m)
+    cc = (np.stack([ci, cj, ck], axis=1) + 0.5) * (size / n)
+    d2 = ((cc[:, None, :] - centers[None, :, :]) ** 2).sum(axis=2)
+    keep = (d2 <= radii[None, :] ** 2).any(axis=1)
+    E = E[keep]
+    c = c[keep]
+    # largest connected component (union-find over tet vertices)
+    parent = np.arange(len(V))
+
+    def find(a):
+        root = a
+        while parent[root] != root:
+            root = parent[root]
+        while parent[a] != root:
+            parent[a], a = root, parent[a]
+        return root
+
+    for t in E:
+        r0 = find(t[0])
+        for k in range(1, 4):
+            rk = find(t[k])
+            if rk != r0:
+                parent[rk] = r0
+    roots = np.array([find(v) for v in E[:, 0]])
+    if len(roots) == 0:
+        raise ValueError("no cell inside the spheres")
+    vals, counts = np.unique(roots, return_counts=True)
+    big = vals[np.argmax(counts)]
+    E = E[roots == big]
+    c = c[roots == big]
+    used = np.unique(E.ravel())
+    remap = -np.ones(len(V), dtype=np.int64)
+    remap[used] = np.arange(len(used))
+    return V[used].copy(), remap[E].astype(np.int32), c
