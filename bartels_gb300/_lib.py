@@ -108,6 +108,8 @@ SIGNATURES = [
     ("bartels_plan_set_preconditioner", C.c_int, [_P, C.c_int, _P]),
     ("bartels_plan_pcg_d", C.c_int, [_P, _P, _P, _P, _P, C.POINTER(PcgParams), C.POINTER(PcgReport)]),
     ("bartels_newton_gradient_d", C.c_int, [_P, _P, C.POINTER(NewtonParams), _P, _P]),
+    ("bartels_plan_autotune", C.c_int, [_P, _P, _P, C.c_int, _I, _I]),
+    ("bartels_segment_sumsq_d", C.c_int, [_P, C.c_int, _P, _P, _P]),
     ("bartels_gemm_bf16_d", C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, C.c_int, _P, _P, C.c_int, _P, C.c_int]),
     ("bartels_newton_iterate_d", C.c_int,
      [_P, _P, C.POINTER(NewtonParams), _P, C.c_double, _I, C.POINTER(NewtonReport)]),

@@ -32,6 +32,9 @@ int plan_pcg(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const
              const bartels_pcg_params &prm, bartels_pcg_report *rep);
 int newton_gradient(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params &p, const double *x,
                     double *g);
+int plan_autotune(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, int force, int *spmv_out,
+                  int *tri_out);
+int segment_sumsq(bartels_ctx ctx, int nseg, const int *off, const double *v, double *out);
 }  // namespace bartels
 
 using namespace bartels;
@@ -651,6 +654,24 @@ int bartels_newton_gradient_d(bartels_ctx ctx, bartels_mesh_plan plan, const bar
   BT_CHECK(check_plan(ctx, plan));
   if (!params || !x_d || !g_d || !valid_model(params->model)) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
   return newton_gradient(ctx, plan, *params, x_d, g_d);
+}
+
+int bartels_plan_autotune(bartels_ctx ctx, bartels_mesh_plan plan, const float *values_d, int force,
+                          int *spmv_lanes, int *factor_lanes) {
+  BT_CHECK(check_plan(ctx, plan));
+  if (!values_d) {
+    if (plan->w_values.bytes < sizeof(float) * 9 * (size_t)plan->nnzb)
+      return fail(BARTELS_E_INVALID_ARG, "the plan has no assembled Hessian yet");
+    values_d = plan->w_values.as<float>();
+  }
+  return plan_autotune(ctx, plan, values_d, force, spmv_lanes, factor_lanes);
+}
+
+int bartels_segment_sumsq_d(bartels_ctx ctx, int nseg, const int *vertex_offsets_d, const double *v_d, double *out_d) {
+  BT_CHECK(check_ctx(ctx));
+  if (nseg < 0 || (nseg > 0 && (!vertex_offsets_d || !v_d || !out_d)))
+    return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  return segment_sumsq(ctx, nseg, vertex_offsets_d, v_d, out_d);
 }
 
 int bartels_gemm_bf16_d(bartels_ctx ctx, int M, int N, int K, const void *x_d, int ldx, const void *w_d,

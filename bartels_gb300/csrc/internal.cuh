@@ -5,7 +5,9 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <map>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "bartels_gpu.h"
@@ -93,6 +95,8 @@ struct bartels_ctx_s {
   int spmv_lanes = 16;
   // lanes per vertex row in the triangular factor passes (4 or 8; BARTELS_TRI_LANES)
   int tri_lanes = 4;
+  // autotuner results per size bucket (floor(log2 nV)): {SpMV lanes, factor-pass lanes}
+  std::map<int, std::pair<int, int>> tune_cache;
   // pinned host staging for small read-backs
   double *host_scalars = nullptr;
   // device scratch for reductions
@@ -139,6 +143,8 @@ struct bartels_mesh_plan_s {
   bartels::FactorPattern *factor = nullptr;
   bartels::LpcgPlanState *lpcg = nullptr;
   int precond = BARTELS_PRECOND_BLOCK_JACOBI;
+  // lanes per vertex row chosen by the autotuner for this plan (0: the context's)
+  int spmv_lanes = 0, tri_lanes = 0;
   bartels_lpcg lpcg_net = nullptr;
   // solver workspace
   bartels::DevBuf w_values, w_minv, w_vec, w_grad_e, w_energy, w_u, w_pcg, w_psd;

@@ -822,6 +822,13 @@ struct PcgWork {
   PcgState *st;
 };
 
+static int lanes_spmv(bartels_ctx ctx, bartels_mesh_plan plan) {
+  return (plan && plan->spmv_lanes) ? plan->spmv_lanes : ctx->spmv_lanes;
+}
+static int lanes_tri(bartels_ctx ctx, bartels_mesh_plan plan) {
+  return (plan && plan->tri_lanes) ? plan->tri_lanes : ctx->tri_lanes;
+}
+
 static int grid_vec(bartels_ctx ctx, int64_t n) {
   int64_t g = (n + 255) / 256;
   int64_t cap = (int64_t)ctx->num_sms * kVecBlocksPerSM;
@@ -838,7 +845,7 @@ static int grid_spmv(bartels_ctx ctx, int64_t rows) {
 static int pcg_enqueue_prec(bartels_ctx ctx, const PcgOperator &op, const PcgWork &w) {
   const bartels_mesh_plan plan = op.plan;
   // triangular rows are about half as long as the matrix rows (4 or 8 lanes, 4 columns a lane)
-  const int G = ctx->tri_lanes;
+  const int G = lanes_tri(ctx, plan);
   const int gt = grid_spmv(ctx, (int64_t)plan->nV * G / 32 + 1);
 #define BT_T(G_)                                                                                                 \
   BT_LAUNCH(ctx, k_pcg_prec_lower<G_>, gt, 256, 0, plan->nV, op.fp->meta, plan->bcol, op.gl, w.r, w.ap, op.pinned, \
@@ -857,7 +864,8 @@ static int pcg_enqueue_prec(bartels_ctx ctx, const PcgOperator &op, const PcgWor
 static int pcg_enqueue_iters(bartels_ctx ctx, const PcgOperator &op, const PcgWork &w, int n, int nb, int iters) {
   const bool blk = op.plan != nullptr;
   const bool fac = blk && op.gl != nullptr;
-  const int gs = blk ? grid_spmv(ctx, (int64_t)op.plan->nV * ctx->spmv_lanes / 32 + 1) : grid_spmv(ctx, n);
+  const int lanes = blk ? lanes_spmv(ctx, op.plan) : 0;
+  const int gs = blk ? grid_spmv(ctx, (int64_t)op.plan->nV * lanes / 32 + 1) : grid_spmv(ctx, n);
   const int gu = grid_vec(ctx, (nb + 3) / 4);
   const int gd = grid_vec(ctx, (n + 3) / 4);
   for (int i = 0; i < iters; ++i) {
@@ -867,8 +875,8 @@ static int pcg_enqueue_iters(bartels_ctx ctx, const PcgOperator &op, const PcgWo
 #define BT_K1(G)                                                                                                 \
   BT_LAUNCH(ctx, k_pcg_spmv_blk<G>, gs, 256, 0, op.plan->nV, op.plan->brp, op.plan->bcol, op.values, w.pa, w.pb, \
             w.ap, op.pinned, w.part_a, w.st)
-      if (ctx->spmv_lanes == 4) BT_K1(4);
-      else if (ctx->spmv_lanes == 16) BT_K1(16);
+      if (lanes == 4) BT_K1(4);
+      else if (lanes == 16) BT_K1(16);
       else BT_K1(8);
 #undef BT_K1
     } else {
@@ -1232,13 +1240,129 @@ int advance_implicit_euler(bartels_ctx ctx, bartels_mesh_plan plan, double dt, c
 }
 
 int plan_spmv(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const float *x, float *y) {
-  const int g = grid_spmv(ctx, (int64_t)plan->nV * ctx->spmv_lanes / 32 + 1);
-  if (ctx->spmv_lanes == 4)
+  const int lanes = lanes_spmv(ctx, plan);
+  const int g = grid_spmv(ctx, (int64_t)plan->nV * lanes / 32 + 1);
+  if (lanes == 4)
     BT_LAUNCH(ctx, k_spmv_blk_g<4>, g, 256, 0, plan->nV, plan->brp, plan->bcol, values, x, y, plan->pinned);
-  else if (ctx->spmv_lanes == 16)
+  else if (lanes == 16)
     BT_LAUNCH(ctx, k_spmv_blk_g<16>, g, 256, 0, plan->nV, plan->brp, plan->bcol, values, x, y, plan->pinned);
   else
     BT_LAUNCH(ctx, k_spmv_blk_g<8>, g, 256, 0, plan->nV, plan->brp, plan->bcol, values, x, y, plan->pinned);
+  return BARTELS_OK;
+}
+
+// Autotuner: time the block-row SpMV with 4, 8 and 16 lanes per vertex row and
+// the factor passes with 4 and 8 lanes on this plan (CUDA events on the
+// context's stream, 3 warm-up + 10 timed launches each), keep the fastest in
+// the plan and in the context's cache for the plan's size bucket
+// floor(log2 nV), which later plans of that bucket reuse without timing.
+int plan_autotune(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, int force, int *spmv_out,
+                  int *tri_out) {
+  int bucket = 0;
+  for (int v = plan->nV; v > 1; v >>= 1) bucket++;
+  auto hit = ctx->tune_cache.find(bucket);
+  if (!force && hit != ctx->tune_cache.end()) {
+    plan->spmv_lanes = hit->second.first;
+    plan->tri_lanes = hit->second.second;
+  } else {
+    FactorPattern *fp;
+    BT_CHECK(plan_factor_pattern(plan, &fp));
+    const size_t n = 3 * (size_t)plan->nV;
+    float *x = nullptr, *y = nullptr;
+    __nv_bfloat16 *gl = nullptr;
+    PcgState *st = nullptr;
+    double *part = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int status = BARTELS_OK;
+    auto cleanup = [&]() {
+      if (x) cudaFree(x);
+      if (y) cudaFree(y);
+      if (gl) cudaFree(gl);
+      if (st) cudaFree(st);
+      if (part) cudaFree(part);
+      if (e0) cudaEventDestroy(e0);
+      if (e1) cudaEventDestroy(e1);
+    };
+    auto timed = [&](auto &&launch) -> float {
+      for (int k = 0; k < 3; ++k) launch();
+      cudaEventRecord(e0, ctx->stream);
+      for (int k = 0; k < 10; ++k) launch();
+      cudaEventRecord(e1, ctx->stream);
+      cudaEventSynchronize(e1);
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      return ms;
+    };
+    if (cudaMalloc(&x, 4 * n) != cudaSuccess || cudaMalloc(&y, 4 * n) != cudaSuccess ||
+        cudaMalloc(&gl, 2 * (size_t)fp->lsize + 16) != cudaSuccess || cudaMalloc(&st, sizeof(PcgState)) != cudaSuccess ||
+        cudaMalloc(&part, 8 * 4096) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+        cudaEventCreate(&e1) != cudaSuccess) {
+      cleanup();
+      return fail(BARTELS_E_DEVICE, "autotuner scratch allocation failed");
+    }
+    cudaMemsetAsync(x, 0, 4 * n, ctx->stream);
+    cudaMemsetAsync(gl, 0, 2 * (size_t)fp->lsize + 16, ctx->stream);
+    cudaMemsetAsync(st, 0, sizeof(PcgState), ctx->stream);
+    const int nV = plan->nV;
+    float best = 1e30f;
+    int best_s = ctx->spmv_lanes, best_t = ctx->tri_lanes;
+    const int cand_s[3] = {4, 8, 16};
+    for (int G : cand_s) {
+      const int g = grid_spmv(ctx, (int64_t)nV * G / 32 + 1);
+      const float ms = timed([&] {
+        if (G == 4) k_spmv_blk_g<4><<<g, 256, 0, ctx->stream>>>(nV, plan->brp, plan->bcol, values, x, y, plan->pinned);
+        else if (G == 8) k_spmv_blk_g<8><<<g, 256, 0, ctx->stream>>>(nV, plan->brp, plan->bcol, values, x, y, plan->pinned);
+        else k_spmv_blk_g<16><<<g, 256, 0, ctx->stream>>>(nV, plan->brp, plan->bcol, values, x, y, plan->pinned);
+      });
+      if (ms < best) {
+        best = ms;
+        best_s = G;
+      }
+    }
+    best = 1e30f;
+    const int cand_t[2] = {4, 8};
+    for (int G : cand_t) {
+      const int g = grid_spmv(ctx, (int64_t)nV * G / 32 + 1);
+      const float ms = timed([&] {
+        if (G == 4)
+          k_pcg_prec_lower<4><<<g, 256, 0, ctx->stream>>>(nV, fp->meta, plan->bcol, gl, x, y, plan->pinned, part, st);
+        else
+          k_pcg_prec_lower<8><<<g, 256, 0, ctx->stream>>>(nV, fp->meta, plan->bcol, gl, x, y, plan->pinned, part, st);
+      });
+      if (ms < best) {
+        best = ms;
+        best_t = G;
+      }
+    }
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e == cudaSuccess) e = cudaGetLastError();
+    cleanup();
+    if (e != cudaSuccess) status = fail(BARTELS_E_DEVICE, std::string("autotuner: ") + cudaGetErrorString(e));
+    if (status != BARTELS_OK) return status;
+    ctx->launches += 39;
+    plan->spmv_lanes = best_s;
+    plan->tri_lanes = best_t;
+    ctx->tune_cache[bucket] = {best_s, best_t};
+  }
+  if (spmv_out) *spmv_out = plan->spmv_lanes;
+  if (tri_out) *tri_out = plan->tri_lanes;
+  return BARTELS_OK;
+}
+
+// out[s] = sum over the DOFs of vertices off[s] .. off[s+1]-1 of v^2 (one block per segment)
+__global__ void __launch_bounds__(256)
+k_segment_sumsq(int nseg, const int *__restrict__ off, const double *__restrict__ v, double *__restrict__ out) {
+  for (int sgm = blockIdx.x; sgm < nseg; sgm += gridDim.x) {
+    double acc = 0.0;
+    for (int64_t i = 3ll * off[sgm] + threadIdx.x; i < 3ll * off[sgm + 1]; i += blockDim.x) acc += v[i] * v[i];
+    const double s = cta_sum(acc);
+    if (threadIdx.x == 0) out[sgm] = s;
+  }
+}
+
+int segment_sumsq(bartels_ctx ctx, int nseg, const int *off, const double *v, double *out) {
+  if (nseg <= 0) return BARTELS_OK;
+  BT_LAUNCH(ctx, k_segment_sumsq, std::min(nseg, 65535), 256, 0, nseg, off, v, out);
   return BARTELS_OK;
 }
 

@@ -334,6 +334,20 @@ int bartels_plan_set_preconditioner(bartels_mesh_plan plan, int kind, bartels_lp
  * rows of pinned vertices excluded. */
 int bartels_plan_pcg_d(bartels_ctx ctx, bartels_mesh_plan plan, const float *values_d, const double *b_d,
                        double *x_d, const bartels_pcg_params *params, bartels_pcg_report *report);
+/* ---------------------------------------------------------------- batching -- */
+/* Autotuner: times the block-row SpMV (4, 8, 16 lanes per vertex row) and the
+ * factor passes (4, 8 lanes) on this plan's Hessian (values_d, or NULL for the
+ * plan's internal buffer) and keeps the fastest for the plan's PCG solves. The
+ * choice is cached in the context per size bucket floor(log2 nV) and reused by
+ * later plans of that bucket unless force != 0. No counterpart in the reference. */
+int bartels_plan_autotune(bartels_ctx ctx, bartels_mesh_plan plan, const float *values_d, int force,
+                          int *spmv_lanes, int *factor_lanes);
+/* Batched solves pack many meshes into one plan (a block-diagonal system, one
+ * launch per Newton stage for all of them); per-mesh convergence uses
+ * out_d[s] = sum of v_d^2 over the DOFs of vertices vertex_offsets_d[s] ..
+ * vertex_offsets_d[s+1]-1 (device arrays, nseg + 1 offsets). */
+int bartels_segment_sumsq_d(bartels_ctx ctx, int nseg, const int *vertex_offsets_d, const double *v_d,
+                            double *out_d);
 /* Building block: Y = act(X W^T + bias) on the tensor cores (tcgen05, TMA);
  * X: M x K BF16 (row stride ldx elements), W: N x K BF16, bias: N FP32 or NULL,
  * Y: M x N FP32 (row stride ldy); N, K in {64, 128}; device pointers. */
