@@ -4,11 +4,14 @@ The compute lives in libbartels_gpu.so (C ABI: include/bartels_gpu.h); this
 package mirrors the reference's mesh-level functions on top of it.
 """
 from ._lib import (BartelsError, CONVERGED, MAX_ITERATIONS_REACHED, NEOHOOKEAN, STVK, COROTATIONAL,
-                   NEOHOOKEAN_ISOCHORIC, PSD_NONE, PSD_SIMPLE_FIX, LIB_PATH, lib)
+                   NEOHOOKEAN_ISOCHORIC, ARAP, LINEAR_ELASTICITY, PSD_NONE, PSD_SIMPLE_FIX, LIB_PATH, lib)
 from .api import (Context, MeshPlan, newton_params, linear_tetmesh_dphi_dX, volume,
                   linear_tetmesh_neohookean_q, linear_tetmesh_neohookean_dq, linear_tetmesh_neohookean_dq2,
                   linear_tetmesh_stvk_q, linear_tetmesh_stvk_dq, linear_tetmesh_stvk_dq2,
                   linear_tetmesh_corotational_q, linear_tetmesh_corotational_dq, linear_tetmesh_corotational_dq2,
+                  linear_tetmesh_arap_q, linear_tetmesh_arap_dq, linear_tetmesh_arap_dq2,
+                  linear_tetmesh_linear_elasticity_q, linear_tetmesh_linear_elasticity_dq,
+                  linear_tetmesh_linear_elasticity_dq2,
                   linear_tetmesh_mass_matrix, linear_tetmesh_const_ext_force, fixed_point_constraint_matrix,
                   find_min_vertices, search_direction_newton_sparse, linesearch_backtracking_bisection)
 from . import meshes

@@ -14,7 +14,7 @@ LIB_PATH = os.path.join(HERE, "lib", "libbartels_gpu.so")
 OK = 0
 E_INVALID_ARG, E_NONFINITE, E_NOT_CONVERGED, E_DEVICE, E_TIMEOUT, E_UNSUPPORTED, E_NO_DEVICE = 1, 2, 3, 4, 5, 6, 7
 CONVERGED, MAX_ITERATIONS_REACHED = 0, 1
-NEOHOOKEAN, STVK, COROTATIONAL, NEOHOOKEAN_ISOCHORIC = 0, 1, 2, 3
+NEOHOOKEAN, STVK, COROTATIONAL, NEOHOOKEAN_ISOCHORIC, ARAP, LINEAR_ELASTICITY = 0, 1, 2, 3, 4, 5
 PSD_NONE, PSD_SIMPLE_FIX = 0, 1
 DQ2_COROT_EXACT = 1
 PRECOND_BLOCK_JACOBI, PRECOND_LEARNED = 0, 1

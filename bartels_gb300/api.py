@@ -24,7 +24,8 @@ from . import _lib
 from ._lib import BartelsError, check, lib
 
 MODELS = {"neohookean": _lib.NEOHOOKEAN, "stvk": _lib.STVK, "corotational": _lib.COROTATIONAL,
-          "neohookean_isochoric": _lib.NEOHOOKEAN_ISOCHORIC}
+          "neohookean_isochoric": _lib.NEOHOOKEAN_ISOCHORIC,
+          "arap": _lib.ARAP, "linear_elasticity": _lib.LINEAR_ELASTICITY}
 
 
 def _dptr(a):
@@ -309,6 +310,9 @@ linear_tetmesh_neohookean_q, linear_tetmesh_neohookean_dq, linear_tetmesh_neohoo
 linear_tetmesh_stvk_q, linear_tetmesh_stvk_dq, linear_tetmesh_stvk_dq2 = _make("stvk")
 linear_tetmesh_corotational_q, linear_tetmesh_corotational_dq, linear_tetmesh_corotational_dq2 = _make(
     "corotational")
+linear_tetmesh_arap_q, linear_tetmesh_arap_dq, linear_tetmesh_arap_dq2 = _make("arap")
+linear_tetmesh_linear_elasticity_q, linear_tetmesh_linear_elasticity_dq, linear_tetmesh_linear_elasticity_dq2 = \
+    _make("linear_elasticity")
 
 
 def linear_tetmesh_mass_matrix(V, E, density, volume):

@@ -41,7 +41,21 @@ using namespace bartels;
 
 namespace {
 
-bool valid_model(int m) { return m >= 0 && m <= 3; }
+bool valid_model(int m) { return m >= 0 && m <= 5; }
+
+// Linear elasticity takes the reference's (Young's modulus, Poisson ratio) per
+// tet (src/d2psi_linear_elasticity_de2.cpp:10-11); the kernels use the Lame
+// pair (lambda, mu). Returns params itself for every other model.
+const double *model_params(int model, const double *params, int nT, std::vector<double> &buf) {
+  if (model != BARTELS_LINEAR_ELASTICITY || !params) return params;
+  buf.resize(2 * (size_t)nT);
+  for (int t = 0; t < nT; ++t) {
+    const double E = params[t], nu = params[t + (size_t)nT];
+    buf[t] = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
+    buf[t + (size_t)nT] = E / (2.0 * (1.0 + nu));
+  }
+  return buf.data();
+}
 
 int check_ctx(bartels_ctx ctx) {
   if (!ctx) return fail(BARTELS_E_INVALID_ARG, "null context");
@@ -251,7 +265,8 @@ int bartels_tetmesh_q(bartels_ctx ctx, bartels_mesh_plan plan, int model, const 
                       const double *vol, const double *params, double *energy_out) {
   BT_CHECK(check_plan(ctx, plan));
   if (!valid_model(model) || !q || !energy_out) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
-  BT_CHECK(plan_set_element_data(plan, dphidX, vol, params, nullptr));
+  std::vector<double> pbuf;
+  BT_CHECK(plan_set_element_data(plan, dphidX, vol, model_params(model, params, plan->nT, pbuf), nullptr));
   double *dq;
   BT_CHECK(stage_vec(ctx, ctx->stage_e, q, 3 * (size_t)plan->nV, &dq));
   BT_CHECK(ctx->scalars.ensure(64 * sizeof(double)));
@@ -268,7 +283,8 @@ int bartels_tetmesh_dq(bartels_ctx ctx, bartels_mesh_plan plan, int model, const
                        const double *vol, const double *params, double *g) {
   BT_CHECK(check_plan(ctx, plan));
   if (!valid_model(model) || !q || !g) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
-  BT_CHECK(plan_set_element_data(plan, dphidX, vol, params, nullptr));
+  std::vector<double> pbuf;
+  BT_CHECK(plan_set_element_data(plan, dphidX, vol, model_params(model, params, plan->nT, pbuf), nullptr));
   const size_t n = 3 * (size_t)plan->nV;
   double *dq;
   BT_CHECK(stage_vec(ctx, ctx->stage_e, q, n, &dq));
@@ -288,7 +304,8 @@ int bartels_tetmesh_dq2(bartels_ctx ctx, bartels_mesh_plan plan, int model, cons
   BT_CHECK(check_plan(ctx, plan));
   if (!valid_model(model) || !q || !csr_values || (psd_mode != BARTELS_PSD_NONE && psd_mode != BARTELS_PSD_SIMPLE_FIX))
     return fail(BARTELS_E_INVALID_ARG, "bad arguments");
-  BT_CHECK(plan_set_element_data(plan, dphidX, vol, params, nullptr));
+  std::vector<double> pbuf;
+  BT_CHECK(plan_set_element_data(plan, dphidX, vol, model_params(model, params, plan->nT, pbuf), nullptr));
   const size_t n = 3 * (size_t)plan->nV;
   const int64_t nnz = 9 * plan->nnzb;
   double *dq;
@@ -322,6 +339,8 @@ int bartels_tetmesh_dq2(bartels_ctx ctx, bartels_mesh_plan plan, int model, cons
 BT_NAMED(neohookean, BARTELS_NEOHOOKEAN)
 BT_NAMED(stvk, BARTELS_STVK)
 BT_NAMED(corotational, BARTELS_COROTATIONAL)
+BT_NAMED(arap, BARTELS_ARAP)
+BT_NAMED(linear_elasticity, BARTELS_LINEAR_ELASTICITY)
 #undef BT_NAMED
 
 int bartels_tetmesh_mass_matrix(bartels_ctx ctx, bartels_mesh_plan plan, const double *density, const double *vol,

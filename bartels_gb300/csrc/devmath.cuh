@@ -41,7 +41,7 @@ BT_HD float bt_abs(float x) { return std::fabs(x); }
 BT_HD double bt_abs(double x) { return std::fabs(x); }
 #endif
 
-enum { MODEL_NH = 0, MODEL_STVK = 1, MODEL_COROT = 2, MODEL_NH_ISO = 3 };
+enum { MODEL_NH = 0, MODEL_STVK = 1, MODEL_COROT = 2, MODEL_NH_ISO = 3, MODEL_ARAP = 4, MODEL_LE = 5 };
 
 template <class T>
 BT_HD T det3(const T *A) {
@@ -392,11 +392,52 @@ struct LawCorot {
   }
 };
 
+// Linear elasticity, src/linear_tet_linear_elasticity_dq2.cpp:8-25 with
+// src/d2psi_linear_elasticity_de2.cpp:8-24: B^T C B vol with Voigt engineering
+// strains of e = sym(F) and the isotropic C; pv = vol * (lambda, mu). The
+// 3x3 block of nodes a, b: lambda pa pb^T + mu pb pa^T + mu (pa . pb) I.
+template <class T>
+struct LawLE {
+  T lam, mu;
+  BT_HD LawLE(const T *, const T *pv) : lam(pv[0]), mu(pv[1]) {}
+  BT_HD void block(const T *pa, const T *pb, T *K) const {
+    const T ab = pa[0] * pb[0] + pa[1] * pb[1] + pa[2] * pb[2];
+    for (int k = 0; k < 3; ++k)
+      for (int l = 0; l < 3; ++l) K[3 * k + l] = lam * pa[k] * pb[l] + mu * pa[l] * pb[k] + (k == l ? mu * ab : T(0));
+  }
+};
+
+// ARAP, src/psi_arap_S.cpp:8-11, src/dpsi_arap_dS.cpp:8-10, src/d2psi_arap_dS2.cpp:8-9:
+// psi = k sum_i (s_i - 1)^2 through the same stretch machinery as the
+// corotational law (src/linear_tet_arap_dq2.cpp:12-14), i.e. the corotational
+// law with lambda = 0 and mu = k; params column 0 is k.
+template <class T>
+BT_HD void arap_pv(const T *pv, T *out) {
+  out[0] = T(0);
+  out[1] = pv[0];
+}
+
 // ----------------------------------------------------------------------------
 // FP64 energy and first Piola-Kirchhoff stress (scaled by vol via pv)
 // ----------------------------------------------------------------------------
 template <class T>
 BT_HD T psi_model(int model, const T *F, const T *pv) {
+  if (model == MODEL_LE) {
+    // mu e:e + lambda/2 tr(e)^2, e = sym(F) (the reference's strain of q as given)
+    T ee = T(0);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        const T e = T(0.5) * (F[i + 3 * j] + F[j + 3 * i]);
+        ee += e * e;
+      }
+    const T tr = F[0] + F[4] + F[8];
+    return pv[1] * ee + T(0.5) * pv[0] * tr * tr;
+  }
+  if (model == MODEL_ARAP) {
+    T pa[2];
+    arap_pv(pv, pa);
+    return psi_model(MODEL_COROT, F, pa);
+  }
   if (model == MODEL_NH || model == MODEL_NH_ISO) {
     T J = det3(F), I1 = T(0);
     for (int i = 0; i < 9; ++i) I1 += F[i] * F[i];
@@ -424,6 +465,19 @@ BT_HD T psi_model(int model, const T *F, const T *pv) {
 
 template <class T>
 BT_HD void pk1_model(int model, const T *F, const T *pv, T *P) {
+  if (model == MODEL_LE) {
+    const T tr = F[0] + F[4] + F[8];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        P[i + 3 * j] = pv[1] * (F[i + 3 * j] + F[j + 3 * i]) + (i == j ? pv[0] * tr : T(0));
+    return;
+  }
+  if (model == MODEL_ARAP) {
+    T pa[2];
+    arap_pv(pv, pa);
+    pk1_model(MODEL_COROT, F, pa, P);
+    return;
+  }
   if (model == MODEL_NH || model == MODEL_NH_ISO) {
     T G[9];
     cof3(G, F);

@@ -370,7 +370,12 @@ __device__ __forceinline__ void with_law(const float *F, const float *pv, int co
   if constexpr (MODEL == MODEL_NH) fn(LawNH<float>(F, pv));
   else if constexpr (MODEL == MODEL_NH_ISO) fn(LawNHIso<float>(F, pv));
   else if constexpr (MODEL == MODEL_STVK) fn(LawStVK<float>(F, pv));
-  else fn(LawCorot<float>(F, pv, corot_exact != 0));
+  else if constexpr (MODEL == MODEL_LE) fn(LawLE<float>(F, pv));
+  else if constexpr (MODEL == MODEL_ARAP) {
+    float pa[2];
+    arap_pv(pv, pa);
+    fn(LawCorot<float>(F, pa, corot_exact != 0));
+  } else fn(LawCorot<float>(F, pv, corot_exact != 0));
 }
 
 // PSD pre-pass, one thread per tet: decide whether simple_psd_fix changes the
@@ -627,6 +632,8 @@ int energy(bartels_ctx ctx, bartels_mesh_plan plan, int model, const ObjectiveDe
     case MODEL_STVK: BT_EN(MODEL_STVK); break;
     case MODEL_COROT: BT_EN(MODEL_COROT); break;
     case MODEL_NH_ISO: BT_EN(MODEL_NH_ISO); break;
+    case MODEL_ARAP: BT_EN(MODEL_ARAP); break;
+    case MODEL_LE: BT_EN(MODEL_LE); break;
     default: return fail(BARTELS_E_INVALID_ARG, "unknown model");
   }
 #undef BT_EN
@@ -649,6 +656,8 @@ int energy_diff(bartels_ctx ctx, bartels_mesh_plan plan, int model, const Object
     case MODEL_STVK: BT_ED(MODEL_STVK); break;
     case MODEL_COROT: BT_ED(MODEL_COROT); break;
     case MODEL_NH_ISO: BT_ED(MODEL_NH_ISO); break;
+    case MODEL_ARAP: BT_ED(MODEL_ARAP); break;
+    case MODEL_LE: BT_ED(MODEL_LE); break;
     default: return fail(BARTELS_E_INVALID_ARG, "unknown model");
   }
 #undef BT_ED
@@ -667,6 +676,8 @@ int gradient(bartels_ctx ctx, bartels_mesh_plan plan, int model, const Objective
     case MODEL_STVK: BT_GE(MODEL_STVK); break;
     case MODEL_COROT: BT_GE(MODEL_COROT); break;
     case MODEL_NH_ISO: BT_GE(MODEL_NH_ISO); break;
+    case MODEL_ARAP: BT_GE(MODEL_ARAP); break;
+    case MODEL_LE: BT_GE(MODEL_LE); break;
     default: return fail(BARTELS_E_INVALID_ARG, "unknown model");
   }
 #undef BT_GE
@@ -711,6 +722,8 @@ int launch_hess(bartels_ctx ctx, bartels_mesh_plan plan, int model, int psd_mode
     case MODEL_STVK: BT_H(MODEL_STVK);
     case MODEL_COROT: BT_H(MODEL_COROT);
     case MODEL_NH_ISO: BT_H(MODEL_NH_ISO);
+    case MODEL_ARAP: BT_H(MODEL_ARAP);
+    case MODEL_LE: BT_H(MODEL_LE);
     case -1: return launch_hess_t<-1, false>(ctx, plan, u, add_identity, 0.f, cM, 0.f, 0, values);
     default: return fail(BARTELS_E_INVALID_ARG, "unknown model");
   }
@@ -771,6 +784,8 @@ int noalloc_gradient(bartels_ctx ctx, bartels_mesh_plan plan, int model, const d
     case MODEL_STVK: BT_GN(MODEL_STVK); break;
     case MODEL_COROT: BT_GN(MODEL_COROT); break;
     case MODEL_NH_ISO: BT_GN(MODEL_NH_ISO); break;
+    case MODEL_ARAP: BT_GN(MODEL_ARAP); break;
+    case MODEL_LE: BT_GN(MODEL_LE); break;
     default: return fail(BARTELS_E_INVALID_ARG, "unknown model");
   }
 #undef BT_GN

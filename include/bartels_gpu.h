@@ -51,12 +51,24 @@ enum { BARTELS_CONVERGED = 0, BARTELS_MAX_ITERATIONS_REACHED = 1 };
 /* Material laws. NEOHOOKEAN is src/psi_neohookean_F.cpp:31 (C (I1-3-2 ln J) +
  * D (J-1)^2). NEOHOOKEAN_ISOCHORIC is the reference's earlier law kept as
  * commented-out code in src/psi_neohookean_F.cpp:8-14 (C (J^-2/3 I1 - 3) +
- * D (J-1)^2); data/matrices/H_neohookean_coarser_bunny.txt was made with it. */
+ * D (J-1)^2); data/matrices/H_neohookean_coarser_bunny.txt was made with it.
+ * ARAP is src/psi_arap_S.cpp:8-11 (k sum (s_i - 1)^2 over the singular values,
+ * params column 0 = k; Hessian in the reference's stretch layout, as the
+ * corotational model). LINEAR_ELASTICITY is src/linear_tet_linear_elasticity_dq2.cpp
+ * (B^T C B vol, Voigt engineering strains of e = sym(F) of q as given, so q is
+ * a displacement; params = Young's modulus, Poisson ratio at the host entry
+ * points; a plan's stored params for this model, as the device entry points
+ * read them, are the Lame pair (lambda, mu)). Its energy, mu e:e +
+ * lambda/2 tr(e)^2, has no reference counterpart; its gradient B^T C e vol
+ * follows src/linear_tet_linear_elasticity_dq.cpp, which would not compile if
+ * instantiated (a 6x12 product stored in a 9x12 matrix). */
 enum {
   BARTELS_NEOHOOKEAN = 0,
   BARTELS_STVK = 1,
   BARTELS_COROTATIONAL = 2,
-  BARTELS_NEOHOOKEAN_ISOCHORIC = 3
+  BARTELS_NEOHOOKEAN_ISOCHORIC = 3,
+  BARTELS_ARAP = 4,
+  BARTELS_LINEAR_ELASTICITY = 5
 };
 
 /* Element-matrix callback replacement (src/linear_tetmesh_neohookean_dq2.cpp:22):
@@ -160,6 +172,23 @@ int bartels_tetmesh_corotational_dq(bartels_ctx, bartels_mesh_plan, const double
 int bartels_tetmesh_corotational_dq2(bartels_ctx, bartels_mesh_plan, const double *q, const double *dphidX,
                                      const double *vol, const double *params, int psd_mode, double psd_tol,
                                      double *csr_values);
+/* linear_tetmesh_arap_{q,dq,dq2}, src/linear_tetmesh_arap_q.cpp, _dq.cpp, _dq2.cpp */
+int bartels_tetmesh_arap_q(bartels_ctx, bartels_mesh_plan, const double *q, const double *dphidX,
+                           const double *vol, const double *params, double *energy);
+int bartels_tetmesh_arap_dq(bartels_ctx, bartels_mesh_plan, const double *q, const double *dphidX,
+                            const double *vol, const double *params, double *g);
+int bartels_tetmesh_arap_dq2(bartels_ctx, bartels_mesh_plan, const double *q, const double *dphidX,
+                             const double *vol, const double *params, int psd_mode, double psd_tol,
+                             double *csr_values);
+/* linear_tetmesh_linear_elasticity_{dq,dq2}, src/linear_tetmesh_linear_elasticity_dq.cpp,
+ * _dq2.cpp (the energy entry point has no reference counterpart) */
+int bartels_tetmesh_linear_elasticity_q(bartels_ctx, bartels_mesh_plan, const double *q, const double *dphidX,
+                                        const double *vol, const double *params, double *energy);
+int bartels_tetmesh_linear_elasticity_dq(bartels_ctx, bartels_mesh_plan, const double *q, const double *dphidX,
+                                         const double *vol, const double *params, double *g);
+int bartels_tetmesh_linear_elasticity_dq2(bartels_ctx, bartels_mesh_plan, const double *q, const double *dphidX,
+                                          const double *vol, const double *params, int psd_mode, double psd_tol,
+                                          double *csr_values);
 
 /* --------------------------------------------------- mass, loads, bounds --- */
 /* linear_tetmesh_mass_matrix, src/linear_tetmesh_mass_matrix.cpp:7-24 (per tet

@@ -163,7 +163,7 @@ inline void build_B(double *B /*9x12 col-major*/, const double *dphi12) {
 // ----------------------------------------------------------------------------
 // constitutive models. params are the reference's per-tet row (2 values).
 // ----------------------------------------------------------------------------
-enum Model { NEOHOOKEAN = 0, STVK = 1, COROTATIONAL = 2, NEOHOOKEAN_ISOCHORIC = 3 };
+enum Model { NEOHOOKEAN = 0, STVK = 1, COROTATIONAL = 2, NEOHOOKEAN_ISOCHORIC = 3, ARAP = 4, LINEAR_ELASTICITY = 5 };
 
 // psi_neohookean_F, src/psi_neohookean_F.cpp:31: C (tr F^T F - 3 - 2 ln J) + D (J-1)^2,
 // params = (C, D).
@@ -548,6 +548,104 @@ inline void d2psi_corot_dsvd_literal(double *H, const double *F, const double *p
     }
 }
 
+// --- ARAP -------------------------------------------------------------------
+// psi_arap_S, src/psi_arap_S.cpp:8-11: k sum (s_i - 1)^2 (k = params(0));
+// dpsi_arap_dS, src/dpsi_arap_dS.cpp:8-10: 2 k (s_i - 1); d2psi_arap_dS2,
+// src/d2psi_arap_dS2.cpp:8-9: 2 k I. linear_tet_arap_{q,dq,dq2}
+// (src/linear_tet_arap_q.cpp:12, _dq.cpp:13-14, _dq2.cpp:12-14) pass these
+// through the same stretch routines as the corotational model, whose
+// S-functions with (lambda, mu) = (0, k) are exactly these; so ARAP is
+// evaluated as the corotational stretch energy with lambda = 0, mu = k.
+inline void arap_params(double *pc, const double *p) {
+  pc[0] = 0.0;
+  pc[1] = p[0];
+}
+inline double psi_arap(const double *F, const double *p) {
+  double pc[2];
+  arap_params(pc, p);
+  return psi_corot(F, pc);
+}
+inline void dpsi_arap(double *P, const double *F, const double *p) {
+  double pc[2];
+  arap_params(pc, p);
+  dpsi_corot(P, F, pc);
+}
+inline void d2psi_arap(double *H, const double *F, const double *p, bool layout_reference) {
+  double pc[2];
+  arap_params(pc, p);
+  d2psi_corot(H, F, pc, layout_reference);
+}
+
+// --- linear elasticity --------------------------------------------------------
+// linear_tet_linear_elasticity_dq2, src/linear_tet_linear_elasticity_dq2.cpp:8-25:
+// B6 = P2 B with P2 (6x9) picking [F11, F22, F33, F32 + F23, F31 + F13,
+// F21 + F12] from vec(F) (column-major), C from
+// src/d2psi_linear_elasticity_de2.cpp:8-24 (params = Young's modulus, Poisson
+// ratio), K = B6^T C B6 vol. In F space: psi = 1/2 (P2 f)^T C (P2 f),
+// dpsi = P2^T C P2 f (src/linear_tet_linear_elasticity_dq.cpp:17-21 with its
+// 6/9 size mismatch resolved), d2psi = P2^T C P2.
+inline void le_C(double *C /*6x6 col-major*/, const double *p) {
+  for (int i = 0; i < 36; ++i) C[i] = 0.0;
+  const double YM = p[0], nu = p[1];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) C[i + 6 * j] = (i == j) ? 1.0 - nu : nu;
+  for (int i = 3; i < 6; ++i) C[i + 6 * i] = 0.5 * (1.0 - 2.0 * nu);
+  const double s = YM / ((1.0 + nu) * (1.0 - 2.0 * nu));
+  for (int i = 0; i < 36; ++i) C[i] *= s;
+}
+inline void le_P2(double *P /*6x9 col-major*/) {
+  for (int i = 0; i < 54; ++i) P[i] = 0.0;
+  const int rows[9][2] = {{0, -1}, {5, -1}, {4, -1}, {5, -1}, {1, -1}, {3, -1}, {4, -1}, {3, -1}, {2, -1}};
+  // column c of vec(F) contributes to Voigt row rows[c][0]
+  for (int c = 0; c < 9; ++c) P[rows[c][0] + 6 * c] = 1.0;
+}
+inline void le_CP(double *CP /*6x9*/, const double *p) {
+  double C[36], P[54];
+  le_C(C, p);
+  le_P2(P);
+  for (int i = 0; i < 6; ++i)
+    for (int c = 0; c < 9; ++c) {
+      double acc = 0.0;
+      for (int k = 0; k < 6; ++k) acc += C[i + 6 * k] * P[k + 6 * c];
+      CP[i + 6 * c] = acc;
+    }
+}
+inline double psi_le(const double *F, const double *p) {
+  double P[54], C[36], e[6] = {0, 0, 0, 0, 0, 0};
+  le_P2(P);
+  le_C(C, p);
+  for (int i = 0; i < 6; ++i)
+    for (int c = 0; c < 9; ++c) e[i] += P[i + 6 * c] * F[c];
+  double acc = 0.0;
+  for (int i = 0; i < 6; ++i)
+    for (int j = 0; j < 6; ++j) acc += e[i] * C[i + 6 * j] * e[j];
+  return 0.5 * acc;
+}
+inline void dpsi_le(double *Pk, const double *F, const double *p) {
+  double P[54], CP[54];
+  le_P2(P);
+  le_CP(CP, p);
+  double s[6] = {0, 0, 0, 0, 0, 0};
+  for (int i = 0; i < 6; ++i)
+    for (int c = 0; c < 9; ++c) s[i] += CP[i + 6 * c] * F[c];
+  for (int c = 0; c < 9; ++c) {
+    double acc = 0.0;
+    for (int i = 0; i < 6; ++i) acc += P[i + 6 * c] * s[i];
+    Pk[c] = acc;
+  }
+}
+inline void d2psi_le(double *H /*9x9 col-major*/, const double *p) {
+  double P[54], CP[54];
+  le_P2(P);
+  le_CP(CP, p);
+  for (int a = 0; a < 9; ++a)
+    for (int b = 0; b < 9; ++b) {
+      double acc = 0.0;
+      for (int i = 0; i < 6; ++i) acc += P[i + 6 * a] * CP[i + 6 * b];
+      H[a + 9 * b] = acc;
+    }
+}
+
 // ----------------------------------------------------------------------------
 // per-element energy / gradient / Hessian: linear_tet_{model}_{q,dq,dq2}
 // (src/linear_tet_neohookean_q.cpp:9-16, _dq.cpp:11-20, _dq2.cpp:12-21 and the
@@ -571,6 +669,8 @@ inline double model_psi(int model, const double *F, const double *p) {
     case NEOHOOKEAN: return psi_nh(F, p);
     case STVK: return psi_stvk(F, p);
     case NEOHOOKEAN_ISOCHORIC: return psi_nh_iso(F, p);
+    case ARAP: return psi_arap(F, p);
+    case LINEAR_ELASTICITY: return psi_le(F, p);
     default: return psi_corot(F, p);
   }
 }
@@ -579,6 +679,8 @@ inline void model_dpsi(int model, double *P, const double *F, const double *p) {
     case NEOHOOKEAN: dpsi_nh(P, F, p); break;
     case STVK: dpsi_stvk(P, F, p); break;
     case NEOHOOKEAN_ISOCHORIC: dpsi_nh_iso(P, F, p); break;
+    case ARAP: dpsi_arap(P, F, p); break;
+    case LINEAR_ELASTICITY: dpsi_le(P, F, p); break;
     default: dpsi_corot(P, F, p); break;
   }
 }
@@ -587,6 +689,8 @@ inline void model_d2psi(int model, double *H, const double *F, const double *p, 
     case NEOHOOKEAN: d2psi_nh(H, F, p); break;
     case STVK: d2psi_stvk(H, F, p); break;
     case NEOHOOKEAN_ISOCHORIC: d2psi_nh_iso(H, F, p); break;
+    case ARAP: d2psi_arap(H, F, p, fl.corot_layout_reference); break;
+    case LINEAR_ELASTICITY: d2psi_le(H, p); break;
     default: d2psi_corot(H, F, p, fl.corot_layout_reference); break;
   }
 }

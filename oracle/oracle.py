@@ -21,9 +21,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
 
-NEOHOOKEAN, STVK, COROTATIONAL, NEOHOOKEAN_ISOCHORIC = 0, 1, 2, 3
+NEOHOOKEAN, STVK, COROTATIONAL, NEOHOOKEAN_ISOCHORIC, ARAP, LINEAR_ELASTICITY = 0, 1, 2, 3, 4, 5
 MODELS = {"neohookean": NEOHOOKEAN, "stvk": STVK, "corotational": COROTATIONAL,
-          "neohookean_isochoric": NEOHOOKEAN_ISOCHORIC}
+          "neohookean_isochoric": NEOHOOKEAN_ISOCHORIC, "arap": ARAP, "linear_elasticity": LINEAR_ELASTICITY}
 
 
 def build(force: bool = False) -> str:

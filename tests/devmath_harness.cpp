@@ -9,7 +9,12 @@ static void block_t(int model, const T *F, const T *pv, const T *pa, const T *pb
   if (model == MODEL_NH) LawNH<T>(F, pv).block(pa, pb, K);
   else if (model == MODEL_NH_ISO) LawNHIso<T>(F, pv).block(pa, pb, K);
   else if (model == MODEL_STVK) LawStVK<T>(F, pv).block(pa, pb, K);
-  else LawCorot<T>(F, pv, exact != 0).block(pa, pb, K);
+  else if (model == MODEL_LE) LawLE<T>(F, pv).block(pa, pb, K);
+  else if (model == MODEL_ARAP) {
+    T pc[2];
+    arap_pv(pv, pc);
+    LawCorot<T>(F, pc, exact != 0).block(pa, pb, K);
+  } else LawCorot<T>(F, pv, exact != 0).block(pa, pb, K);
 }
 
 // 12x12 element Hessian from the block laws (row-major out[12*(3a+k) + 3b+l]),
@@ -45,7 +50,12 @@ static int element_hessian_t(int model, const T *F, const T *pv, const T *dphi9,
   if (model == MODEL_NH) run(LawNH<T>(F, pv));
   else if (model == MODEL_NH_ISO) run(LawNHIso<T>(F, pv));
   else if (model == MODEL_STVK) run(LawStVK<T>(F, pv));
-  else run(LawCorot<T>(F, pv, exact != 0));
+  else if (model == MODEL_LE) run(LawLE<T>(F, pv));
+  else if (model == MODEL_ARAP) {
+    T pc[2];
+    arap_pv(pv, pc);
+    run(LawCorot<T>(F, pc, exact != 0));
+  } else run(LawCorot<T>(F, pv, exact != 0));
   return slow;
 }
 

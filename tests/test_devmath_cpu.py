@@ -11,9 +11,19 @@ from conftest import devmath
 
 D = C.POINTER(C.c_double)
 Fp = C.POINTER(C.c_float)
-MODEL_ID = {"neohookean": 0, "stvk": 1, "corotational": 2, "neohookean_isochoric": 3}
+MODEL_ID = {"neohookean": 0, "stvk": 1, "corotational": 2, "neohookean_isochoric": 3, "arap": 4,
+            "linear_elasticity": 5}
 PARAMS = {"neohookean": np.array([3.5e5, 1.2e6]), "neohookean_isochoric": np.array([3.5e5, 1.2e6]),
-          "stvk": np.array([2.4e6, 7e5]), "corotational": np.array([2.4e6, 7e5])}
+          "stvk": np.array([2.4e6, 7e5]), "corotational": np.array([2.4e6, 7e5]), "arap": np.array([9e5, 0.0]),
+          "linear_elasticity": np.array([2e6, 0.45])}
+
+
+def device_params(model, p):
+    """The kernels take linear elasticity as the Lame pair (lambda, mu)."""
+    if model != "linear_elasticity":
+        return p
+    E, nu = p
+    return np.array([E * nu / ((1 + nu) * (1 - 2 * nu)), E / (2 * (1 + nu))])
 
 
 def dp(a):
@@ -45,7 +55,7 @@ def lib_element(model, x, dphi12, vol, p, psd_tol, exact, dtype):
     F = np.zeros(9)
     xs = [np.ascontiguousarray(x[a]) for a in range(4)]
     L.dm_def_grad_d(*[dp(v) for v in xs], dp(dphi9), 0, dp(F))
-    pv = vol * p
+    pv = vol * device_params(model, p)
     if dtype == np.float64:
         out = np.zeros(144)
         slow = L.dm_element_hessian_d(MODEL_ID[model], dp(F), dp(pv), dp(dphi9), int(exact), int(psd_tol is not None),
@@ -61,7 +71,7 @@ def lib_element(model, x, dphi12, vol, p, psd_tol, exact, dtype):
 @pytest.mark.parametrize("model", list(MODEL_ID))
 @pytest.mark.parametrize("exact", [False, True])
 def test_element_hessian_fp64(oracle, model, exact):
-    if exact and model != "corotational":
+    if exact and model not in ("corotational", "arap"):
         pytest.skip("flag only affects the corotational law")
     rng = np.random.default_rng(11)
     for _ in range(20):
@@ -83,7 +93,9 @@ def test_element_hessian_psd_fp64(oracle, model):
             slow_seen += slow
             fast_seen += 1 - slow
             assert np.linalg.norm(K - K_ref) <= 1e-9 * np.linalg.norm(K_ref)
-    assert fast_seen > 0
+    # linear elasticity has the 3 infinitesimal rotations in its null space, so
+    # simple_psd_fix always changes it (the slow path)
+    assert fast_seen > 0 or model == "linear_elasticity"
 
 
 def test_psd_slow_path_is_exercised(oracle):
@@ -122,11 +134,12 @@ def test_energy_and_stress_fp64(oracle, model):
         if model.startswith("neo") and np.linalg.det(F) <= 0:
             continue
         fv = np.ascontiguousarray(F.ravel(order="F"))
-        e = L.dm_psi_d(MODEL_ID[model], dp(fv), dp(p))
+        pd = np.ascontiguousarray(device_params(model, p))
+        e = L.dm_psi_d(MODEL_ID[model], dp(fv), dp(pd))
         e_ref = oracle.psi(model, F, p)
         assert abs(e - e_ref) <= 1e-11 * max(abs(e_ref), 1.0)
         P = np.zeros(9)
-        L.dm_pk1_d(MODEL_ID[model], dp(fv), dp(p), dp(P))
+        L.dm_pk1_d(MODEL_ID[model], dp(fv), dp(pd), dp(P))
         P_ref = oracle.dpsi(model, F, p)
         assert np.linalg.norm(P - P_ref) <= 1e-11 * np.linalg.norm(P_ref)
 

@@ -16,7 +16,7 @@ from conftest import load_golden_csr, load_golden_mesh, noisy_cube
 
 pytestmark = pytest.mark.gpu
 
-MODELS = ["neohookean", "stvk", "corotational", "neohookean_isochoric"]
+MODELS = ["neohookean", "stvk", "corotational", "neohookean_isochoric", "arap", "linear_elasticity"]
 HESS_TOL = 1e-5
 
 
@@ -108,6 +108,30 @@ def test_hessian_fp32(oracle, model, psd_tol):
         H_ref = oracle.tetmesh_dq2(model, len(V), E, q, dphi, vol, params, psd_tol=psd_tol)
         assert same_pattern(H, H_ref), name
         assert rel_max(H, H_ref) <= HESS_TOL, (name, rel_max(H, H_ref))
+
+
+def test_arap_named_drop_ins_match_generic(oracle):
+    V, E, q = noisy_cube(3, 0.01, 5)
+    params = material_params("arap", len(E), 2e6, 0.45)
+    dphi, vol = oracle.dphi_dX(V, E), oracle.volume(V, E)
+    e = bg.linear_tetmesh_arap_q(V, E, q, dphi, vol, params)
+    H = bg.linear_tetmesh_arap_dq2(V, E, q, dphi, vol, params, psd_tol=1e-6)
+    assert abs(e - oracle.tetmesh_q("arap", E, q, dphi, vol, params)) <= 1e-10 * abs(e)
+    H_ref = oracle.tetmesh_dq2("arap", len(V), E, q, dphi, vol, params, psd_tol=1e-6)
+    assert same_pattern(H, H_ref) and rel_max(H, H_ref) <= HESS_TOL
+
+
+def test_linear_elasticity_hessian_is_constant_and_gradient_linear(oracle):
+    V, E, q = noisy_cube(3, 0.01, 6)
+    params = material_params("linear_elasticity", len(E), 2e6, 0.45)
+    dphi, vol = oracle.dphi_dX(V, E), oracle.volume(V, E)
+    u = 1e-3 * np.random.default_rng(1).standard_normal(3 * len(V))
+    H0 = bg.linear_tetmesh_linear_elasticity_dq2(V, E, u, dphi, vol, params)
+    H1 = bg.linear_tetmesh_linear_elasticity_dq2(V, E, 2 * u + 1.0, dphi, vol, params)
+    assert rel_max(H0, H1) <= 1e-6
+    g = bg.linear_tetmesh_linear_elasticity_dq(V, E, u, dphi, vol, params)
+    K = oracle.tetmesh_dq2("linear_elasticity", len(V), E, u, dphi, vol, params)
+    assert np.linalg.norm(g - K @ u) <= 1e-10 * np.linalg.norm(g)
 
 
 def test_corotational_exact_flag(oracle):
