@@ -712,18 +712,40 @@ BT_HD void gram3(T *G, const T (*phi)[3]) {
 
 // fast-path test on the element law: true when every non-translational
 // eigenvalue of the element matrix is >= tol (nothing to project).
+//
+// In FP32 the test accepts eigenvalues down to tol - 1e-6 tr(M)/9: an
+// eigenvalue that close to zero is within the rounding of the FP32
+// eigen-decomposition the slow path would run (its absolute error is ~1e-7 of
+// the largest eigenvalue), and leaving it changes the element matrix by at most
+// that band (~1e-6 relative). This keeps near-rest elements, whose three
+// rotation modes have numerically-zero eigenvalues, off the slow path. FP64
+// (host checks) keeps the exact test.
 template <class Law, class T>
 BT_HD bool psd_fast_ok(const Law &law, const T (*phi)[3], T tol) {
   T S[45], G[9], Gi[9];
   law_matrix9p(law, S);
   gram3(G, phi);
   inv3(Gi, G);
+  T c = tol;
+  if (sizeof(T) == 4) {
+    T trM = T(0);  // tr(M) = tr(S (G (x) I))
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        T tb = T(0);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) tb += S[p9(k + 3 * i, k + 3 * j)];
+        trM += G[i + 3 * j] * tb;
+      }
+    c = tol - T(1e-6) * bt_abs(trM) / T(9);
+  }
 #pragma unroll
   for (int i = 0; i < 3; ++i)
 #pragma unroll
     for (int j = 0; j <= i; ++j)
 #pragma unroll
-      for (int k = 0; k < 3; ++k) S[p9(k + 3 * i, k + 3 * j)] -= tol * Gi[i + 3 * j];
+      for (int k = 0; k < 3; ++k) S[p9(k + 3 * i, k + 3 * j)] -= c * Gi[i + 3 * j];
   return chol9p_ok(S);
 }
 

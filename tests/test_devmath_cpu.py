@@ -192,3 +192,29 @@ def test_cancellation_free_energy_accuracy(oracle, model):
             hv = np.ascontiguousarray(H.ravel(order="F"))
             got = L.dm_psi_disp_d(MODEL_ID[model], dp(hv), dp(p))
             assert abs(got - float(ref)) <= 1e-13 * abs(float(ref)), (scale, got, float(ref))
+
+
+@pytest.mark.parametrize("model", ["neohookean", "stvk", "corotational"])
+def test_fp32_rest_and_rigid_elements_take_the_fast_path(oracle, model):
+    """At rest or after a rigid rotation the three rotation modes have
+    eigenvalue zero up to FP32 rounding; the FP32 fast test accepts them
+    (within the FP32 eigen-solver's own rounding) and the result matches the
+    exactly projected matrix. A strained element (1e-3) still takes the slow
+    path."""
+    rng = np.random.default_rng(17)
+    for k in range(10):
+        X, _ = random_tet(rng, 0.0)
+        A = rng.standard_normal((3, 3))
+        Q, _ = np.linalg.qr(A)
+        Q *= np.sign(np.linalg.det(Q))
+        x = X if k % 2 == 0 else X @ Q.T + rng.standard_normal(3)
+        K_ref, dphi, vol = oracle_element(oracle, model, X, x, PARAMS[model], 1e-6, False)
+        K, slow = lib_element(model, x, dphi, vol, PARAMS[model], 1e-6, False, np.float32)
+        assert slow == 0
+        assert np.linalg.norm(K - K_ref) <= 2e-5 * np.linalg.norm(K_ref)
+    X, _ = random_tet(rng, 0.0)
+    x = X @ np.diag([1.0, 1.0, 0.999])  # compressed along z: negative rotation eigenvalues
+    K_ref, dphi, vol = oracle_element(oracle, model, X, x, PARAMS[model], 1e-6, False)
+    K, slow = lib_element(model, x, dphi, vol, PARAMS[model], 1e-6, False, np.float32)
+    assert slow == 1 or model == "stvk"
+    assert np.linalg.norm(K - K_ref) <= 2e-5 * np.linalg.norm(K_ref)
