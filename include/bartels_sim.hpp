@@ -159,6 +159,8 @@ void linear_tetmesh_dphi_dX(MR &dX, const MV &V, const ME &E) {
 BARTELS_SIM_MODEL(neohookean, BARTELS_NEOHOOKEAN)
 BARTELS_SIM_MODEL(stvk, BARTELS_STVK)
 BARTELS_SIM_MODEL(corotational, BARTELS_COROTATIONAL)
+BARTELS_SIM_MODEL(arap, BARTELS_ARAP)
+BARTELS_SIM_MODEL(linear_elasticity, BARTELS_LINEAR_ELASTICITY)
 #undef BARTELS_SIM_MODEL
 
 // linear_tetmesh_mass_matrix, include/linear_tetmesh_mass_matrix.h

@@ -83,6 +83,11 @@ int main() {
   sim::SparseMatrix H;
   sim::linear_tetmesh_neohookean_dq2(H, V, E, q, dphidX, vol, params, sim::simple_psd_fix(1e-6));
   REQUIRE(H.rows() == 3 * nV && H.nonZeros() == H.outer_ptr.back());
+  // ARAP through the same names (k in params column 0)
+  sim::SparseMatrix Ha;
+  sim::linear_tetmesh_arap_dq2(Ha, V, E, q, dphidX, vol, params, sim::simple_psd_fix(1e-6));
+  REQUIRE(Ha.nonZeros() == H.nonZeros());
+  REQUIRE(sim::linear_tetmesh_arap_q(V, E, q, dphidX, vol, params) >= 0.0);
   sim::SparseMatrix M;
   sim::linear_tetmesh_mass_matrix(M, V, E, density, vol);
   double msum = 0;
