@@ -40,6 +40,7 @@ constexpr int kH = 64;
 constexpr int kLayers = 3;
 constexpr int kDx = 4;
 constexpr int kDe = 10;
+constexpr int kFe = 12;  // row stride of the edge-feature array (10 used, padded for float4 loads)
 
 // ------------------------------------------------------- parameter layout ---
 struct Layout {
@@ -196,62 +197,93 @@ __device__ __forceinline__ void linv_mat(const float *li, float (&L)[3][3]) {
   L[2][0] = li[3]; L[2][1] = li[4]; L[2][2] = li[5];
 }
 
-// Ahat_vj = Linv_v A_vj Linv_j^T for every block of the pattern, and node features.
-__global__ void k_lp_feats(int nV, const int *__restrict__ brp, const int *__restrict__ bcol,
-                           const float *__restrict__ vals, const unsigned char *__restrict__ pinned,
-                           const float *__restrict__ linv, float *__restrict__ fe, float *__restrict__ xn,
-                           float *__restrict__ invdeg) {
-  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nV; v += gridDim.x * blockDim.x) {
-    const bool pv = pinned && pinned[v];
-    const int rb = brp[v], nb = brp[v + 1] - rb;
-    const int64_t base = 9ll * rb;
-    const int rs = 3 * nb;
-    float Li[3][3];
-    linv_mat(linv + 6ll * v, Li);
+// Ahat_vj = Linv_v A_vj Linv_j^T for every block of the pattern, and node
+// features. 16 lanes per vertex row (one block each, coalesced reads of the
+// row's three scalar rows, 48-byte feature rows written as three float4).
+__global__ void __launch_bounds__(256)
+k_lp_feats(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, const float *__restrict__ vals,
+           const unsigned char *__restrict__ pinned, const float *__restrict__ linv, float *__restrict__ fe,
+           float *__restrict__ xn, float *__restrict__ invdeg) {
+  const int lane = threadIdx.x & 31, sl = lane & 15, half = lane >> 4;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int vb = 2 * warp; vb < nV; vb += 2 * nwarps) {
+    const int v = vb + half;
+    const bool active = v < nV;
     int deg = 0;
     float sum = 0.f, mx = 0.f;
-    for (int b = 0; b < nb; ++b) {
-      const int j = bcol[rb + b];
-      float *o = fe + (int64_t)kDe * (rb + b);
-      if (pv || (pinned && pinned[j])) {
-        for (int k = 0; k < kDe; ++k) o[k] = 0.f;
-        continue;
-      }
-      float Lj[3][3];
-      linv_mat(linv + 6ll * j, Lj);
-      float T[3][3];  // Linv_v A_vj
-      for (int k = 0; k < 3; ++k)
-        for (int l = 0; l < 3; ++l) {
-          float s = 0.f;
-          for (int m = 0; m <= k; ++m) s += Li[k][m] * blk_val(vals, base, rs, b, m, l);
-          T[k][l] = s;
+    if (active) {
+      const bool pv = pinned && pinned[v];
+      const int rb = brp[v], nb = brp[v + 1] - rb;
+      const int64_t base = 9ll * rb;
+      const int rs = 3 * nb;
+      float Li[3][3];
+      linv_mat(linv + 6ll * v, Li);
+      for (int b = sl; b < nb; b += 16) {
+        const int j = __ldg(bcol + rb + b);
+        float o[kFe];
+#pragma unroll
+        for (int k = 0; k < kFe; ++k) o[k] = 0.f;
+        if (!(pv || (pinned && pinned[j]))) {
+          float Lj[3][3], A[3][3], T[3][3];
+          linv_mat(linv + 6ll * j, Lj);
+#pragma unroll
+          for (int k = 0; k < 3; ++k)
+#pragma unroll
+            for (int l = 0; l < 3; ++l) A[k][l] = __ldg(vals + base + (int64_t)k * rs + 3 * b + l);
+#pragma unroll
+          for (int k = 0; k < 3; ++k)
+#pragma unroll
+            for (int l = 0; l < 3; ++l) {
+              float acc = 0.f;
+#pragma unroll
+              for (int m = 0; m <= k; ++m) acc += Li[k][m] * A[m][l];
+              T[k][l] = acc;
+            }
+          float nrm = 0.f;
+#pragma unroll
+          for (int k = 0; k < 3; ++k)
+#pragma unroll
+            for (int l = 0; l < 3; ++l) {
+              float acc = 0.f;
+#pragma unroll
+              for (int m = 0; m <= l; ++m) acc += T[k][m] * Lj[l][m];  // (Linv_j^T)[m][l] = Lj[l][m]
+              o[3 * k + l] = acc;
+              nrm += acc * acc;
+            }
+          nrm = sqrtf(nrm);
+          o[9] = nrm;
+          if (j != v) {
+            deg++;
+            sum += nrm;
+            mx = fmaxf(mx, nrm);
+          }
         }
-      float nrm = 0.f;
-      for (int k = 0; k < 3; ++k)
-        for (int l = 0; l < 3; ++l) {
-          float s = 0.f;
-          for (int m = 0; m <= l; ++m) s += T[k][m] * Lj[l][m];  // (Linv_j^T)[m][l] = Lj[l][m]
-          o[3 * k + l] = s;
-          nrm += s * s;
-        }
-      nrm = sqrtf(nrm);
-      o[9] = nrm;
-      if (j != v) {
-        deg++;
-        sum += nrm;
-        mx = fmaxf(mx, nrm);
+        float4 *dst = reinterpret_cast<float4 *>(fe + (int64_t)kFe * (rb + b));
+        dst[0] = make_float4(o[0], o[1], o[2], o[3]);
+        dst[1] = make_float4(o[4], o[5], o[6], o[7]);
+        dst[2] = make_float4(o[8], o[9], o[10], o[11]);
       }
     }
-    float *x = xn + (int64_t)kDx * v;
-    if (pv) {
-      x[0] = x[1] = x[2] = x[3] = 0.f;
-      invdeg[v] = 0.f;
-    } else {
-      x[0] = 1.f;
-      x[1] = deg * (1.f / 14.f);
-      x[2] = deg > 0 ? sum / deg : 0.f;
-      x[3] = mx;
-      invdeg[v] = deg > 0 ? 1.f / deg : 0.f;
+    // reductions over the 16 lanes of the row (all lanes of the warp take part)
+#pragma unroll
+    for (int off = 8; off > 0; off >>= 1) {
+      deg += __shfl_xor_sync(0xffffffffu, deg, off);
+      sum += __shfl_xor_sync(0xffffffffu, sum, off);
+      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+    }
+    if (active && sl == 0) {
+      float *x = xn + (int64_t)kDx * v;
+      if (pinned && pinned[v]) {
+        x[0] = x[1] = x[2] = x[3] = 0.f;
+        invdeg[v] = 0.f;
+      } else {
+        x[0] = 1.f;
+        x[1] = deg * (1.f / 14.f);
+        x[2] = deg > 0 ? sum / deg : 0.f;
+        x[3] = mx;
+        invdeg[v] = deg > 0 ? 1.f / deg : 0.f;
+      }
     }
   }
 }
@@ -281,18 +313,34 @@ __global__ void k_lp_embed(int nV, const float *__restrict__ xn, const float *__
   }
 }
 
-// edge term e We + be for two channels (c, c+1)
-__device__ __forceinline__ void edge_term(const float *__restrict__ e, const float *__restrict__ W,
-                                          const float *__restrict__ b, int c, float &r0, float &r1) {
-  r0 = b[c];
-  r1 = b[c + 1];
+// Weights of the edge term e We + be for one lane's two channels (c, c+1),
+// held in registers for the whole edge loop.
+struct EdgeW {
+  float w0[kDe], w1[kDe], b0, b1;
+  __device__ __forceinline__ EdgeW(const float *__restrict__ W, const float *__restrict__ b, int c) {
 #pragma unroll
-  for (int k = 0; k < kDe; ++k) {
-    const float ek = __ldg(e + k);
-    r0 += ek * W[k * kH + c];
-    r1 += ek * W[k * kH + c + 1];
+    for (int k = 0; k < kDe; ++k) {
+      w0[k] = W[k * kH + c];
+      w1[k] = W[k * kH + c + 1];
+    }
+    b0 = b[c];
+    b1 = b[c + 1];
   }
-}
+  // e: one edge's feature row (kFe floats, 16-byte aligned): three float4 loads
+  __device__ __forceinline__ void apply(const float *__restrict__ e, float &r0, float &r1) const {
+    const float4 a = __ldg(reinterpret_cast<const float4 *>(e));
+    const float4 bq = __ldg(reinterpret_cast<const float4 *>(e) + 1);
+    const float4 cq = __ldg(reinterpret_cast<const float4 *>(e) + 2);
+    const float ev[kDe] = {a.x, a.y, a.z, a.w, bq.x, bq.y, bq.z, bq.w, cq.x, cq.y};
+    r0 = b0;
+    r1 = b1;
+#pragma unroll
+    for (int k = 0; k < kDe; ++k) {
+      r0 += ev[k] * w0[k];
+      r1 += ev[k] * w1[k];
+    }
+  }
+};
 
 // a_v = (1/deg_v) sum_j relu(P_v + Q_j + e_vj We + be), written as BF16 into
 // the right half of [h | a]. One warp per vertex.
@@ -302,6 +350,7 @@ k_lp_msg(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, cons
          const float *__restrict__ We, const float *__restrict__ be, __nv_bfloat16 *__restrict__ ha) {
   const int lane = threadIdx.x & 31;
   const int c = 2 * lane;
+  const EdgeW ew(We, be, c);
   for (int v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < nV; v += (gridDim.x * blockDim.x) >> 5) {
     float a0 = 0.f, a1 = 0.f;
     if (!(pinned && pinned[v])) {
@@ -311,7 +360,7 @@ k_lp_msg(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, cons
         const int j = __ldg(bcol + p);
         if (j == v || (pinned && pinned[j])) continue;
         float r0, r1;
-        edge_term(fe + (int64_t)kDe * p, We, be, c, r0, r1);
+        ew.apply(fe + (int64_t)kFe * p, r0, r1);
         const float2 Q = reinterpret_cast<const float2 *>(pq + 2ll * kH * j + kH)[lane];
         a0 += fmaxf(P.x + Q.x + r0, 0.f);
         a1 += fmaxf(P.y + Q.y + r1, 0.f);
@@ -336,6 +385,13 @@ k_lp_head(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, con
           const float *__restrict__ Wskip, float *__restrict__ raw, __nv_bfloat16 *__restrict__ gl) {
   const int lane = threadIdx.x & 31;
   const int c = 2 * lane;
+  const EdgeW ew(Wf, bf, c);
+  float wo0[9], wo1[9];
+#pragma unroll
+  for (int o = 0; o < 9; ++o) {
+    wo0[o] = Wo[c * 9 + o];
+    wo1[o] = Wo[(c + 1) * 9 + o];
+  }
   for (int v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < nV; v += (gridDim.x * blockDim.x) >> 5) {
     const bool pv = pinned && pinned[v];
     const int rb = brp[v], d = diag_pos[v], nl = d + 1, lb = lrp[v];
@@ -348,16 +404,19 @@ k_lp_head(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, con
       bool zero = pv || (pinned && pinned[j]);
       if (!zero && b < d) {
         float r0, r1;
-        edge_term(fe + (int64_t)kDe * (rb + b), Wf, bf, c, r0, r1);
+        const float *e = fe + (int64_t)kFe * (rb + b);
+        ew.apply(e, r0, r1);
         const float2 T = reinterpret_cast<const float2 *>(st + 2ll * kH * j + kH)[lane];
         const float z0 = fmaxf(S.x + T.x + r0, 0.f), z1 = fmaxf(S.y + T.y + r1, 0.f);
-        const float *e = fe + (int64_t)kDe * (rb + b);
 #pragma unroll
-        for (int o = 0; o < 9; ++o) {
-          float sk = 0.f;
+        for (int o = 0; o < 9; ++o) out[o] = warp_allsum(z0 * wo0[o] + z1 * wo1[o]) + bo[o];
+        if (lane == 0) {  // linear path e Wskip (only lane 0 writes the outputs)
 #pragma unroll
-          for (int k = 0; k < kDe; ++k) sk += __ldg(e + k) * Wskip[k * 9 + o];
-          out[o] = warp_allsum(z0 * Wo[c * 9 + o] + z1 * Wo[(c + 1) * 9 + o]) + bo[o] + sk;
+          for (int k = 0; k < kDe; ++k) {
+            const float ek = __ldg(e + k);
+#pragma unroll
+            for (int o = 0; o < 9; ++o) out[o] += ek * Wskip[k * 9 + o];
+          }
         }
       } else if (!zero) {
         const float h0 = h[(int64_t)kH * v + c], h1 = h[(int64_t)kH * v + c + 1];
@@ -509,7 +568,7 @@ k_lp_ahat_apply(int nV, int np, const int *__restrict__ brp, const int *__restri
       if (!pv)
         for (int q = rb; q < re; ++q) {
           const int j = bcol[q];
-          const float *A = fe + (int64_t)kDe * q;
+          const float *A = fe + (int64_t)kFe * q;
           const float *uj = u + (int64_t)p * n + 3 * j;
 #pragma unroll
           for (int k = 0; k < 3; ++k) s[k] += A[3 * k] * uj[0] + A[3 * k + 1] * uj[1] + A[3 * k + 2] * uj[2];
@@ -621,6 +680,7 @@ k_lp_head_bwd(int nV, const int *__restrict__ brp, const int *__restrict__ bcol,
               float *__restrict__ e_h, float *__restrict__ z_h, float *__restrict__ dpre_h) {
   const int lane = threadIdx.x & 31;
   const int c = 2 * lane;
+  const EdgeW ew(Wf, bf, c);
   for (int v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < nV; v += (gridDim.x * blockDim.x) >> 5) {
     const bool pv = pinned && pinned[v];
     const int rb = brp[v], d = diag_pos[v], lb = lrp[v];
@@ -633,7 +693,7 @@ k_lp_head_bwd(int nV, const int *__restrict__ brp, const int *__restrict__ bcol,
       float z0 = 0.f, z1 = 0.f, q0 = 0.f, q1 = 0.f;
       if (!zero) {
         float r0, r1;
-        edge_term(fe + (int64_t)kDe * (rb + b), Wf, bf, c, r0, r1);
+        ew.apply(fe + (int64_t)kFe * (rb + b), r0, r1);
         const float2 T = reinterpret_cast<const float2 *>(st + 2ll * kH * j + kH)[lane];
         const float p0 = S.x + T.x + r0, p1 = S.y + T.y + r1;
         z0 = fmaxf(p0, 0.f);
@@ -654,7 +714,7 @@ k_lp_head_bwd(int nV, const int *__restrict__ brp, const int *__restrict__ bcol,
       z_h[kH * l + c + 1] = z1;
       dpre_h[kH * l + c] = q0;
       dpre_h[kH * l + c + 1] = q1;
-      if (lane < kDe) e_h[kDe * l + lane] = zero ? 0.f : fe[(int64_t)kDe * (rb + b) + lane];
+      if (lane < kDe) e_h[kDe * l + lane] = zero ? 0.f : fe[(int64_t)kFe * (rb + b) + lane];
     }
     dst[2ll * kH * v + c] = ds0;
     dst[2ll * kH * v + c + 1] = ds1;
@@ -699,6 +759,7 @@ k_lp_msg_bwd(int nV, const int *__restrict__ brp, const int *__restrict__ bcol,
              const float *__restrict__ dha, float *__restrict__ dpre_e, float *__restrict__ dpq) {
   const int lane = threadIdx.x & 31;
   const int c = 2 * lane;
+  const EdgeW ew(We, be, c);
   for (int v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < nV; v += (gridDim.x * blockDim.x) >> 5) {
     const bool pv = pinned && pinned[v];
     const int rb = brp[v], re = brp[v + 1];
@@ -711,7 +772,7 @@ k_lp_msg_bwd(int nV, const int *__restrict__ brp, const int *__restrict__ bcol,
       float q0 = 0.f, q1 = 0.f;
       if (!pv && j != v && !(pinned && pinned[j])) {
         float r0, r1;
-        edge_term(fe + (int64_t)kDe * p, We, be, c, r0, r1);
+        ew.apply(fe + (int64_t)kFe * p, r0, r1);
         const float2 Q = reinterpret_cast<const float2 *>(pq + 2ll * kH * j + kH)[lane];
         q0 = (P.x + Q.x + r0) > 0.f ? dm0 : 0.f;
         q1 = (P.y + Q.y + r1) > 0.f ? dm1 : 0.f;
@@ -891,7 +952,7 @@ static int lp_state(bartels_mesh_plan plan, bool train, int nprobe, LpcgPlanStat
   s->nnzu = fp->nnzu;
   s->train = train;
   s->nprobe = nprobe;
-  BT_CHECK(lp_alloc(*s, &s->fe, kDe * nnzb));
+  BT_CHECK(lp_alloc(*s, &s->fe, kFe * nnzb));
   BT_CHECK(lp_alloc(*s, &s->linv, 6 * nV));
   BT_CHECK(lp_alloc(*s, &s->xn, kDx * nV));
   BT_CHECK(lp_alloc(*s, &s->invdeg, nV));
@@ -1008,8 +1069,8 @@ static int lp_forward(bartels_lpcg net, bartels_mesh_plan plan, LpcgPlanState *s
   BT_CHECK(lp_refresh_bf16(net));
   const int gv = grid_for_n(ctx, nV, 256), gw = grid_warps(ctx, nV);
   BT_LAUNCH(ctx, k_lp_linv, gv, 256, 0, nV, plan->brp, plan->diag_pos, vals, plan->pinned, s->linv);
-  BT_LAUNCH(ctx, k_lp_feats, gv, 256, 0, nV, plan->brp, plan->bcol, vals, plan->pinned, s->linv, s->fe, s->xn,
-            s->invdeg);
+  BT_LAUNCH(ctx, k_lp_feats, grid_warps(ctx, (nV + 1) / 2), 256, 0, nV, plan->brp, plan->bcol, vals, plan->pinned,
+            s->linv, s->fe, s->xn, s->invdeg);
   BT_LAUNCH(ctx, k_lp_embed, gw, 256, 0, nV, s->xn, P + kL.W0, P + kL.b0, s->train ? s->pre0 : nullptr, s->h[0],
             s->ha[0]);
   for (int l = 0; l < kLayers; ++l) {
@@ -1129,7 +1190,7 @@ static int lp_loss_grad(bartels_lpcg net, bartels_mesh_plan plan, const float *v
     BT_LAUNCH(ctx, k_lp_msg_bwd, gw, 256, 0, nV, plan->brp, plan->bcol, plan->pinned, s->fe, s->invdeg, s->pq[l],
               P + kL.We[l], P + kL.be[l], s->dha, s->dpre_e, s->dpq);
     BT_LAUNCH(ctx, k_lp_msg_bwd_t, gw, 256, 0, nV, plan->brp, fp->rev, s->dpre_e, s->dpq);
-    BT_CHECK(lp_outer<float>(net, s->nnzb, kDe, kH, s->fe, kDe, s->dpre_e, kH, G + kL.We[l]));
+    BT_CHECK(lp_outer<float>(net, s->nnzb, kDe, kH, s->fe, kFe, s->dpre_e, kH, G + kL.We[l]));
     BT_CHECK(lp_outer<float>(net, s->nnzb, 1, kH, nullptr, 0, s->dpre_e, kH, G + kL.be[l]));
     BT_CHECK(lp_outer<__nv_bfloat16>(net, nV, 2 * kH, kH, s->dpq, 2 * kH, s->ha[l], 2 * kH, G + kL.Wpq[l]));
     BT_CHECK(lp_to_bf16(ctx, 2ll * kH * nV, s->dpq, s->dbf));
