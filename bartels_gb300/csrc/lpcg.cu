@@ -374,86 +374,103 @@ k_lp_msg(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, cons
 }
 
 // Output head: Ghat for the lower blocks of row v, G = Ghat Linv_col in the
-// lower storage; raw network outputs kept for training. One warp per vertex.
-__global__ void __launch_bounds__(256)
+// lower storage (BF16, padded rows); raw network outputs kept for training.
+// One thread per vertex row; the head's weights sit in shared memory and are
+// read as broadcasts, so the per-edge 64 -> 9 projection needs no shuffles.
+constexpr int kHeadThreads = 128;
+__global__ void __launch_bounds__(kHeadThreads)
 k_lp_head(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, const int *__restrict__ diag_pos,
           const int *__restrict__ lrp, const int4 *__restrict__ meta, const unsigned char *__restrict__ pinned,
-          const float *__restrict__ fe,
-          const float *__restrict__ linv, const float *__restrict__ h, const float *__restrict__ st,
-          const float *__restrict__ Wf, const float *__restrict__ bf, const float *__restrict__ Wo,
-          const float *__restrict__ bo, const float *__restrict__ Wd, const float *__restrict__ bd,
-          const float *__restrict__ Wskip, float *__restrict__ raw, __nv_bfloat16 *__restrict__ gl) {
-  const int lane = threadIdx.x & 31;
-  const int c = 2 * lane;
-  const EdgeW ew(Wf, bf, c);
-  float wo0[9], wo1[9];
-#pragma unroll
-  for (int o = 0; o < 9; ++o) {
-    wo0[o] = Wo[c * 9 + o];
-    wo1[o] = Wo[(c + 1) * 9 + o];
-  }
-  for (int v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < nV; v += (gridDim.x * blockDim.x) >> 5) {
+          const float *__restrict__ fe, const float *__restrict__ linv, const float *__restrict__ h,
+          const float *__restrict__ st, const float *__restrict__ Wf, const float *__restrict__ bf,
+          const float *__restrict__ Wo, const float *__restrict__ bo, const float *__restrict__ Wd,
+          const float *__restrict__ bd, const float *__restrict__ Wskip, float *__restrict__ raw,
+          __nv_bfloat16 *__restrict__ gl) {
+  __shared__ float sWf[kDe * kH], sbf[kH], sWo[kH * 9], sbo[9], sWd[kH * 6], sbd[6], sWs[kDe * 9];
+  for (int i = threadIdx.x; i < kDe * kH; i += blockDim.x) sWf[i] = Wf[i];
+  for (int i = threadIdx.x; i < kH * 9; i += blockDim.x) sWo[i] = Wo[i];
+  for (int i = threadIdx.x; i < kH * 6; i += blockDim.x) sWd[i] = Wd[i];
+  for (int i = threadIdx.x; i < kDe * 9; i += blockDim.x) sWs[i] = Wskip[i];
+  for (int i = threadIdx.x; i < kH; i += blockDim.x) sbf[i] = bf[i];
+  if (threadIdx.x < 9) sbo[threadIdx.x] = bo[threadIdx.x];
+  if (threadIdx.x < 6) sbd[threadIdx.x] = bd[threadIdx.x];
+  __syncthreads();
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nV; v += gridDim.x * blockDim.x) {
     const bool pv = pinned && pinned[v];
     const int rb = brp[v], d = diag_pos[v], nl = d + 1, lb = lrp[v];
     const int rs = padded_row(nl);
     __nv_bfloat16 *g = gl + meta[v].y;
-    const float2 S = reinterpret_cast<const float2 *>(st + 2ll * kH * v)[lane];
+    const float4 *S4 = reinterpret_cast<const float4 *>(st + 2ll * kH * v);
     for (int b = 0; b < nl; ++b) {
       const int j = __ldg(bcol + rb + b);
+      const bool zero = pv || (pinned && pinned[j]);
       float out[9];
-      bool zero = pv || (pinned && pinned[j]);
+#pragma unroll
+      for (int o = 0; o < 9; ++o) out[o] = 0.f;
       if (!zero && b < d) {
-        float r0, r1;
-        const float *e = fe + (int64_t)kFe * (rb + b);
-        ew.apply(e, r0, r1);
-        const float2 T = reinterpret_cast<const float2 *>(st + 2ll * kH * j + kH)[lane];
-        const float z0 = fmaxf(S.x + T.x + r0, 0.f), z1 = fmaxf(S.y + T.y + r1, 0.f);
+        const float4 *e4 = reinterpret_cast<const float4 *>(fe + (int64_t)kFe * (rb + b));
+        const float4 ea = __ldg(e4), eb = __ldg(e4 + 1), ec = __ldg(e4 + 2);
+        const float ev[kDe] = {ea.x, ea.y, ea.z, ea.w, eb.x, eb.y, eb.z, eb.w, ec.x, ec.y};
+        const float4 *T4 = reinterpret_cast<const float4 *>(st + 2ll * kH * j + kH);
+        for (int c4 = 0; c4 < kH / 4; ++c4) {
+          const float4 s4 = __ldg(S4 + c4), t4 = __ldg(T4 + c4);
+          const float sv[4] = {s4.x, s4.y, s4.z, s4.w}, tv[4] = {t4.x, t4.y, t4.z, t4.w};
 #pragma unroll
-        for (int o = 0; o < 9; ++o) out[o] = warp_allsum(z0 * wo0[o] + z1 * wo1[o]) + bo[o];
-        if (lane == 0) {  // linear path e Wskip (only lane 0 writes the outputs)
+          for (int q = 0; q < 4; ++q) {
+            const int c = 4 * c4 + q;
+            float pre = sv[q] + tv[q] + sbf[c];
 #pragma unroll
-          for (int k = 0; k < kDe; ++k) {
-            const float ek = __ldg(e + k);
+            for (int k = 0; k < kDe; ++k) pre += ev[k] * sWf[k * kH + c];
+            const float z = fmaxf(pre, 0.f);
 #pragma unroll
-            for (int o = 0; o < 9; ++o) out[o] += ek * Wskip[k * 9 + o];
+            for (int o = 0; o < 9; ++o) out[o] += z * sWo[c * 9 + o];
           }
         }
-      } else if (!zero) {
-        const float h0 = h[(int64_t)kH * v + c], h1 = h[(int64_t)kH * v + c + 1];
 #pragma unroll
-        for (int o = 0; o < 6; ++o) out[o] = warp_allsum(h0 * Wd[c * 6 + o] + h1 * Wd[(c + 1) * 6 + o]) + bd[o];
-        out[6] = out[7] = out[8] = 0.f;
-      } else {
+        for (int o = 0; o < 9; ++o) {
+          float a = out[o] + sbo[o];
 #pragma unroll
-        for (int o = 0; o < 9; ++o) out[o] = 0.f;
-      }
-      if (lane == 0) {
-        float *rw = raw + 9ll * (lb + b);
-#pragma unroll
-        for (int o = 0; o < 9; ++o) rw[o] = out[o];
-        float Gh[3][3];
-        if (b < d) {
-#pragma unroll
-          for (int k = 0; k < 3; ++k)
-#pragma unroll
-            for (int l = 0; l < 3; ++l) Gh[k][l] = out[3 * k + l];
-        } else {
-          Gh[0][0] = expf(out[0]); Gh[0][1] = 0.f;          Gh[0][2] = 0.f;
-          Gh[1][0] = out[3];       Gh[1][1] = expf(out[1]); Gh[1][2] = 0.f;
-          Gh[2][0] = out[4];       Gh[2][1] = out[5];       Gh[2][2] = expf(out[2]);
+          for (int k = 0; k < kDe; ++k) a += ev[k] * sWs[k * 9 + o];
+          out[o] = a;
         }
-        float Lj[3][3];
-        linv_mat(linv + 6ll * j, Lj);
+      } else if (!zero) {
+        const float4 *h4 = reinterpret_cast<const float4 *>(h + (int64_t)kH * v);
+        for (int c4 = 0; c4 < kH / 4; ++c4) {
+          const float4 hq = __ldg(h4 + c4);
+          const float hv[4] = {hq.x, hq.y, hq.z, hq.w};
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+#pragma unroll
+            for (int o = 0; o < 6; ++o) out[o] += hv[q] * sWd[(4 * c4 + q) * 6 + o];
+        }
+#pragma unroll
+        for (int o = 0; o < 6; ++o) out[o] += sbd[o];
+      }
+      float *rw = raw + 9ll * (lb + b);
+#pragma unroll
+      for (int o = 0; o < 9; ++o) rw[o] = out[o];
+      float Gh[3][3];
+      if (b < d) {
 #pragma unroll
         for (int k = 0; k < 3; ++k)
 #pragma unroll
-          for (int l = 0; l < 3; ++l) {
-            float s = 0.f;
-#pragma unroll
-            for (int m = 0; m < 3; ++m) s += Gh[k][m] * Lj[m][l];
-            g[k * rs + 3 * b + l] = __float2bfloat16_rn(zero ? 0.f : s);
-          }
+          for (int l = 0; l < 3; ++l) Gh[k][l] = out[3 * k + l];
+      } else {
+        Gh[0][0] = expf(out[0]); Gh[0][1] = 0.f;          Gh[0][2] = 0.f;
+        Gh[1][0] = out[3];       Gh[1][1] = expf(out[1]); Gh[1][2] = 0.f;
+        Gh[2][0] = out[4];       Gh[2][1] = out[5];       Gh[2][2] = expf(out[2]);
       }
+      float Lj[3][3];
+      linv_mat(linv + 6ll * j, Lj);
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int l = 0; l < 3; ++l) {
+          float acc = 0.f;
+#pragma unroll
+          for (int m = 0; m < 3; ++m) acc += Gh[k][m] * Lj[m][l];
+          g[k * rs + 3 * b + l] = __float2bfloat16_rn(zero ? 0.f : acc);
+        }
     }
   }
 }
@@ -1085,8 +1102,8 @@ static int lp_forward(bartels_lpcg net, bartels_mesh_plan plan, LpcgPlanState *s
   }
   BT_CHECK(lp_gemm(net, nV, 128, 64, s->ha[kLayers], 128, kB.st, nullptr, nullptr, 0, 0, nullptr, 0, s->st, 128,
                    nullptr, 0));
-  BT_LAUNCH(ctx, k_lp_head, gw, 256, 0, nV, plan->brp, plan->bcol, plan->diag_pos, fp->lrp, fp->meta, plan->pinned,
-            s->fe,
+  BT_LAUNCH(ctx, k_lp_head, grid_for_n(ctx, nV, kHeadThreads), kHeadThreads, 0, nV, plan->brp, plan->bcol,
+            plan->diag_pos, fp->lrp, fp->meta, plan->pinned, s->fe,
             s->linv, s->h[kLayers], s->st, P + kL.Wf, P + kL.bf, P + kL.Wo, P + kL.bo, P + kL.Wd, P + kL.bd,
             P + kL.Wskip, s->raw, s->gl);
   BT_LAUNCH(ctx, k_factor_transpose, gv, 256, 0, nV, plan->bcol, fp->meta, fp->lrp, fp->urp, fp->low2up, s->gl,
