@@ -107,12 +107,24 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmap_x, const __grid_constant__ CU
       float v[16];
       tc::tmem_ld16(taddr + c, v);
       if (row < M) {
+        float rv[16];
+        if (resid) {  // 16-byte loads of the residual row segment
+          const float4 *r4 = reinterpret_cast<const float4 *>(resid + (int64_t)row * ldr + c);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const float4 q = r4[i];
+            rv[4 * i] = q.x;
+            rv[4 * i + 1] = q.y;
+            rv[4 * i + 2] = q.z;
+            rv[4 * i + 3] = q.w;
+          }
+        }
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
           float t = v[i] + (bias ? bias[c + i] : 0.f);
           if (ypre) ypre[(int64_t)row * ldp + c + i] = t;
           if (relu) t = fmaxf(t, 0.f);
-          if (resid) t += resid[(int64_t)row * ldr + c + i];
+          if (resid) t += rv[i];
           v[i] = t;
         }
         if (y) {
@@ -188,8 +200,9 @@ int gemm_bf16(bartels_ctx ctx, const GemmArgs &g) {
   if (g.M <= 0) return BARTELS_OK;
   BT_CHECK(tensor_map_encoder());
   if ((g.y && (g.ldy % 4 != 0 || reinterpret_cast<uintptr_t>(g.y) % 16 != 0)) ||
-      (g.y2 && (g.ldy2 % 2 != 0 || reinterpret_cast<uintptr_t>(g.y2) % 4 != 0)))
-    return fail(BARTELS_E_INVALID_ARG, "GEMM output must be 16-byte aligned with a multiple-of-4 row stride");
+      (g.y2 && (g.ldy2 % 2 != 0 || reinterpret_cast<uintptr_t>(g.y2) % 4 != 0)) ||
+      (g.resid && (g.ldr % 4 != 0 || reinterpret_cast<uintptr_t>(g.resid) % 16 != 0)))
+    return fail(BARTELS_E_INVALID_ARG, "GEMM output / residual must be 16-byte aligned with a multiple-of-4 row stride");
   if (g.N == 128 && g.K == 64) return launch_gemm_t<128, 64>(ctx, g);
   if (g.N == 64 && g.K == 128) return launch_gemm_t<64, 128>(ctx, g);
   if (g.N == 64 && g.K == 64) return launch_gemm_t<64, 64>(ctx, g);

@@ -356,14 +356,30 @@ k_lp_msg(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, cons
     if (!(pinned && pinned[v])) {
       const float2 P = reinterpret_cast<const float2 *>(pq + 2ll * kH * v)[lane];
       const int rb = brp[v], re = brp[v + 1];
-      for (int p = rb; p < re; ++p) {
-        const int j = __ldg(bcol + p);
-        if (j == v || (pinned && pinned[j])) continue;
-        float r0, r1;
-        ew.apply(fe + (int64_t)kFe * p, r0, r1);
-        const float2 Q = reinterpret_cast<const float2 *>(pq + 2ll * kH * j + kH)[lane];
-        a0 += fmaxf(P.x + Q.x + r0, 0.f);
-        a1 += fmaxf(P.y + Q.y + r1, 0.f);
+      // two edges per step (their loads overlap); contributions added in edge order
+      for (int p = rb; p < re; p += 2) {
+        const bool has1 = p + 1 < re;
+        const int j0 = __ldg(bcol + p), j1 = has1 ? __ldg(bcol + p + 1) : v;
+        const bool ok0 = j0 != v && !(pinned && pinned[j0]);
+        const bool ok1 = has1 && j1 != v && !(pinned && pinned[j1]);
+        float r0 = 0.f, r1 = 0.f, s0 = 0.f, s1 = 0.f;
+        float2 Q0 = make_float2(0.f, 0.f), Q1 = make_float2(0.f, 0.f);
+        if (ok0) {
+          ew.apply(fe + (int64_t)kFe * p, r0, r1);
+          Q0 = reinterpret_cast<const float2 *>(pq + 2ll * kH * j0 + kH)[lane];
+        }
+        if (ok1) {
+          ew.apply(fe + (int64_t)kFe * (p + 1), s0, s1);
+          Q1 = reinterpret_cast<const float2 *>(pq + 2ll * kH * j1 + kH)[lane];
+        }
+        if (ok0) {
+          a0 += fmaxf(P.x + Q0.x + r0, 0.f);
+          a1 += fmaxf(P.y + Q0.y + r1, 0.f);
+        }
+        if (ok1) {
+          a0 += fmaxf(P.x + Q1.x + s0, 0.f);
+          a1 += fmaxf(P.y + Q1.y + s1, 0.f);
+        }
       }
       const float s = invdeg[v];
       a0 *= s;
