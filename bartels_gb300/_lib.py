@@ -28,7 +28,7 @@ class BartelsError(RuntimeError):
 
 class PcgParams(C.Structure):
     _fields_ = [("rel_tol", C.c_double), ("max_iters", C.c_int), ("inner_rel_tol", C.c_double),
-                ("max_refinements", C.c_int)]
+                ("max_refinements", C.c_int), ("restart", C.c_int)]
 
 
 class PcgReport(C.Structure):

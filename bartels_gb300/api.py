@@ -241,7 +241,7 @@ def newton_params(**kw) -> "_lib.NewtonParams":
     for k, v in kw.items():
         if k == "model" and isinstance(v, str):
             v = MODELS[v]
-        if k in ("rel_tol", "max_iters", "inner_rel_tol", "max_refinements"):
+        if k in ("rel_tol", "max_iters", "inner_rel_tol", "max_refinements", "restart"):
             setattr(p.pcg, k, v)
         else:
             setattr(p, k, v)

@@ -417,8 +417,9 @@ void bartels_pcg_default_params(bartels_pcg_params *p) {
   if (!p) return;
   p->rel_tol = 1e-8;
   p->max_iters = 20000;
-  p->inner_rel_tol = 1e-4;
-  p->max_refinements = 8;
+  p->inner_rel_tol = 0.1;
+  p->max_refinements = 40;
+  p->restart = 0;
 }
 
 int bartels_search_direction_newton_sparse(bartels_ctx ctx, int n, const int *row_ptr, const int *col_idx,

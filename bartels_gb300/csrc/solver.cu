@@ -285,12 +285,16 @@ __device__ __forceinline__ double sum_partials(const double *a, int n) {
   return cta_sum(acc);
 }
 
-// start of an inner solve: x = 0, r = (float) r64, z = M^-1 r, p = 0
+// start of an inner solve: x = 0, r = (float) r64, z = M^-1 r. A fresh solve
+// (cont = 0) clears p and the iteration count; a continued one (cont = 1, the
+// reliable update) keeps the previous pass's last direction and iteration
+// count, and takes beta = r'.z' / r_k.z_k against the replaced residual r'
+// (r_k.z_k = r.z / beta of the previous pass's last update).
 __global__ void k_pcg_init(int nb, int n, const double *__restrict__ r64, const float *__restrict__ minv,
                            float *__restrict__ x, float *__restrict__ r, float *__restrict__ z,
                            float *__restrict__ p0, float *__restrict__ p1, double *__restrict__ part_a,
                            double *__restrict__ part_b, PcgState *__restrict__ st, double inner_rel2, double abs_tol2,
-                           int max_it) {
+                           int max_it, int cont) {
   float arz = 0.f, arr = 0.f;
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nb; v += gridDim.x * blockDim.x) {
     float rv[3], zv[3];
@@ -302,8 +306,10 @@ __global__ void k_pcg_init(int nb, int n, const double *__restrict__ r64, const 
         x[i] = 0.f;
         r[i] = rv[k];
         z[i] = zv[k];
-        p0[i] = 0.f;
-        p1[i] = 0.f;
+        if (!cont) {
+          p0[i] = 0.f;
+          p1[i] = 0.f;
+        }
         arz += rv[k] * zv[k];
         arr += rv[k] * rv[k];
       }
@@ -317,15 +323,16 @@ __global__ void k_pcg_init(int nb, int n, const double *__restrict__ r64, const 
     const double rz = sum_partials(part_a, gridDim.x);
     const double rr = sum_partials(part_b, gridDim.x);
     if (threadIdx.x == 0) {
+      const double rz_old = (cont && st->beta > 0.f) ? st->rz / (double)st->beta : 0.0;
+      st->beta = (rz_old > 0.0 && rz_old < HUGE_VAL) ? (float)(rz / rz_old) : 0.f;
       st->rz = rz;
       st->rr = rr;
       st->rr0 = rr;
       st->pap = 0.0;
       st->alpha = 0.f;
-      st->beta = 0.f;
       st->tol2 = fmax(inner_rel2 * rr, abs_tol2);
-      st->it = 0;
-      st->max_it = max_it;
+      if (!cont) st->it = 0;
+      st->max_it = st->it + max_it;
       st->done = (rr <= st->tol2 || max_it <= 0 || !(rr == rr)) ? 1 : 0;
       st->count = 0;
     }
@@ -767,18 +774,23 @@ k_pcg_update_f(int n, const float *__restrict__ pa, const float *__restrict__ pb
   }
 }
 
-// start of an inner solve with the factor preconditioner: x = 0, r = (float) r64,
-// p = 0; r.r and the tolerance; r.z is set by the following k_pcg_prec_upper.
+// start of an inner solve with the factor preconditioner: x = 0, r = (float) r64;
+// r.r and the tolerance. A fresh solve (cont = 0) clears p and the iteration
+// count (r.z = 1 stands for the previous r.z; beta multiplies p = 0); a
+// continued one keeps p, the iteration count and r_k.z_k, so the following
+// k_pcg_prec_lower takes beta = r'.z' / r_k.z_k against the replaced residual.
 __global__ void k_pcg_init_f(int n, const double *__restrict__ r64, float *__restrict__ x, float *__restrict__ r,
                              float *__restrict__ p0, float *__restrict__ p1, double *__restrict__ part,
-                             PcgState *__restrict__ st, double inner_rel2, double abs_tol2, int max_it) {
+                             PcgState *__restrict__ st, double inner_rel2, double abs_tol2, int max_it, int cont) {
   float arr = 0.f;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float rv = (float)r64[i];
     x[i] = 0.f;
     r[i] = rv;
-    p0[i] = 0.f;
-    p1[i] = 0.f;
+    if (!cont) {
+      p0[i] = 0.f;
+      p1[i] = 0.f;
+    }
     arr += rv * rv;
   }
   double s = cta_sum_f(arr);
@@ -788,13 +800,14 @@ __global__ void k_pcg_init_f(int n, const double *__restrict__ r64, float *__res
     if (threadIdx.x == 0) {
       st->rr = rr;
       st->rr0 = rr;
-      st->rz = 1.0;
+      if (!cont) st->rz = 1.0;
+      else if (!(st->rz > 0.0) || !(st->rz < HUGE_VAL)) st->rz = HUGE_VAL;  // no usable r.z: beta = 0
       st->pap = 0.0;
       st->alpha = 0.f;
       st->beta = 0.f;
       st->tol2 = fmax(inner_rel2 * rr, abs_tol2);
-      st->it = 0;
-      st->max_it = max_it;
+      if (!cont) st->it = 0;
+      st->max_it = st->it + max_it;
       st->done = (rr <= st->tol2 || max_it <= 0 || !(rr == rr)) ? 1 : 0;
       st->count = 0;
     }
@@ -968,7 +981,7 @@ static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double
   }
   int status = BARTELS_OK;
   double rel = 0.0;
-  PcgState hs;
+  PcgState hs{};
   for (int pass = 0; pass <= prm.max_refinements; ++pass) {
     // r64 = b - A x (FP64)
     if (blk) {
@@ -996,15 +1009,18 @@ static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double
       break;
     }
     rep->refinements = pass + 1;
-    // inner FP32 PCG on r64
+    // inner FP32 PCG on r64: a fresh solve in the first pass, later passes
+    // continue the direction against the replaced residual unless restart is set
     const double abs2 = (0.5 * target) * (0.5 * target);
+    const int cont = (pass > 0 && !prm.restart) ? 1 : 0;
+    const int it0 = cont ? hs.it : 0;
     if (op.gl) {
       BT_LAUNCH(ctx, k_pcg_init_f, gv, 256, 0, n, w.r64, w.x, w.r, w.pa, w.pb, w.part_a, w.st,
-                prm.inner_rel_tol * prm.inner_rel_tol, abs2, prm.max_iters - rep->iterations);
+                prm.inner_rel_tol * prm.inner_rel_tol, abs2, prm.max_iters - rep->iterations, cont);
       BT_CHECK(pcg_enqueue_prec(ctx, op, w));
     } else {
       BT_LAUNCH(ctx, k_pcg_init, gv, 256, 0, nb, n, w.r64, w.minv, w.x, w.r, w.z, w.pa, w.pb, w.part_a, w.part_b,
-                w.st, prm.inner_rel_tol * prm.inner_rel_tol, abs2, prm.max_iters - rep->iterations);
+                w.st, prm.inner_rel_tol * prm.inner_rel_tol, abs2, prm.max_iters - rep->iterations, cont);
     }
     for (;;) {
       BT_CUDA(cudaGraphLaunch(exec, ctx->stream));
@@ -1013,7 +1029,7 @@ static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double
       BT_CUDA(cudaStreamSynchronize(ctx->stream));
       if (hs.done) break;
     }
-    rep->iterations += hs.it;
+    rep->iterations += hs.it - it0;
     BT_LAUNCH(ctx, k_axpy64, grid_vec(ctx, n), 256, 0, n, w.x, x);
   }
   cudaGraphExecDestroy(exec);

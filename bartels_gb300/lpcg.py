@@ -163,9 +163,10 @@ def use_block_jacobi(plan: MeshPlan):
           "bartels_plan_set_preconditioner")
 
 
-def plan_pcg(plan: MeshPlan, values, b, x, rel_tol=1e-8, max_iters=20000, inner_rel_tol=1e-4, max_refinements=8):
+def plan_pcg(plan: MeshPlan, values, b, x, rel_tol=1e-8, max_iters=20000, inner_rel_tol=0.1, max_refinements=40,
+             restart=0):
     """x = H^-1 b on the device with the plan's current preconditioner; returns the report."""
-    prm = _lib.PcgParams(rel_tol, max_iters, inner_rel_tol, max_refinements)
+    prm = _lib.PcgParams(rel_tol, max_iters, inner_rel_tol, max_refinements, restart)
     rep = _lib.PcgReport()
     s = lib().bartels_plan_pcg_d(plan.ctx.handle, plan.handle, None if values is None else _ptr(values), _ptr(b),
                                  _ptr(x), C.byref(prm), C.byref(rep))

@@ -213,8 +213,12 @@ int bartels_find_min_vertices(int nV, const double *V, int dim, double tol, int 
 typedef struct {
   double rel_tol;       /* relative residual target ||b - A x|| / ||b|| (default 1e-8) */
   int max_iters;        /* total PCG iterations cap (default 20000) */
-  double inner_rel_tol; /* FP32 inner PCG tolerance per refinement pass (default 1e-4) */
-  int max_refinements;  /* FP64 residual refinement passes (default 8) */
+  double inner_rel_tol; /* FP32 inner PCG: reduction of the residual per refinement pass (default 0.1) */
+  int max_refinements;  /* FP64 residual refinement passes (default 40) */
+  int restart;          /* 0 (default): each refinement pass replaces the FP32 residual by the FP64 one
+                           b - A x and continues the previous pass's search direction (reliable update,
+                           one replacement per 10x reduction by default); 1: each pass restarts the inner
+                           PCG from p = 0 (pair with inner_rel_tol about 1e-4) */
 } bartels_pcg_params;
 
 typedef struct {
