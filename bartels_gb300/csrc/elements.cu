@@ -358,11 +358,17 @@ __global__ void k_grad_gather(int nV, const int *__restrict__ inc_ptr, const int
 // order, as the reference's setFromTriplets does. The chunk's values are then
 // written out with coalesced stores.
 template <int MODEL>
-__device__ __forceinline__ void elem_F(const TetRec32 &r, const float4 *__restrict__ u, int add_identity, float *F) {
-  const float4 x0 = __ldg(u + r.idx.x), x1 = __ldg(u + r.idx.y), x2 = __ldg(u + r.idx.z), x3 = __ldg(u + r.idx.w);
+__device__ __forceinline__ void elem_F_from(const TetRec32 &r, const float4 &x0, const float4 &x1, const float4 &x2,
+                                            const float4 &x3, int add_identity, float *F) {
   const float p0[3] = {x0.x, x0.y, x0.z}, p1[3] = {x1.x, x1.y, x1.z}, p2[3] = {x2.x, x2.y, x2.z},
               p3[3] = {x3.x, x3.y, x3.z};
   def_grad(F, p0, p1, p2, p3, r.dphi, add_identity != 0);
+}
+
+template <int MODEL>
+__device__ __forceinline__ void elem_F(const TetRec32 &r, const float4 *__restrict__ u, int add_identity, float *F) {
+  elem_F_from<MODEL>(r, __ldg(u + r.idx.x), __ldg(u + r.idx.y), __ldg(u + r.idx.z), __ldg(u + r.idx.w), add_identity,
+                     F);
 }
 
 template <int MODEL, class Fn>
@@ -378,32 +384,168 @@ __device__ __forceinline__ void with_law(const float *F, const float *pv, int co
   } else fn(LawCorot<float>(F, pv, corot_exact != 0));
 }
 
-// PSD pre-pass, one thread per tet: decide whether simple_psd_fix changes the
-// element matrix beyond its translation modes; if so store the projected 9x9
-// N (packed, 45 floats) and flag the tet.
+// PSD pre-pass, part 1, one thread per tet: decide whether simple_psd_fix
+// changes the element matrix beyond its translation modes (the exact test
+// psd_fast_ok) and flag the tet; flagged tets are appended to a list (the
+// order of the list does not matter: each entry writes only its own tet).
 template <int MODEL>
 __global__ void __launch_bounds__(128)
-k_psd_prepass(int nT, const TetRec32 *__restrict__ rec, const float4 *__restrict__ u, int add_identity, float tol,
-              int corot_exact, unsigned char *__restrict__ slow, float *__restrict__ Nbuf) {
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nT; t += gridDim.x * blockDim.x) {
+k_psd_test(int nT, const TetRec32 *__restrict__ rec, const float4 *__restrict__ u, int add_identity, float tol,
+           int corot_exact, unsigned char *__restrict__ slow, int *__restrict__ list, int *__restrict__ count) {
+  for (int t0 = blockIdx.x * blockDim.x; t0 < nT; t0 += gridDim.x * blockDim.x) {
+    const int t = t0 + threadIdx.x;
+    bool flag = false;
+    if (t < nT) {
+      TetRec32 r;
+      load_rec32(rec, t, r);
+      float phi[4][3];
+      phi4(r.dphi, phi);
+      float F[9];
+      elem_F<MODEL>(r, u, add_identity, F);
+      with_law<MODEL>(F, r.pv, corot_exact, [&](const auto &law) { flag = !psd_fast_ok(law, phi, tol); });
+      slow[t] = flag ? 1 : 0;
+    }
+    // warp-aggregated append
+    const unsigned m = __ballot_sync(0xffffffffu, flag);
+    if (m) {
+      const int lane = threadIdx.x & 31;
+      int base = 0;
+      if (lane == 0) base = atomicAdd(count, __popc(m));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (flag) list[base + __popc(m & ((1u << lane) - 1u))] = t;
+    }
+  }
+}
+
+// PSD pre-pass, part 2, one thread per flagged tet: the projected 9x9 N
+// (packed, 45 floats) of simple_psd_fix.
+template <int MODEL>
+__global__ void __launch_bounds__(128)
+k_psd_eig(const int *__restrict__ list, const int *__restrict__ count, const TetRec32 *__restrict__ rec,
+          const float4 *__restrict__ u, int add_identity, float tol, int corot_exact, float *__restrict__ Nbuf) {
+  const int n = *count;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int t = __ldg(list + i);
     TetRec32 r;
     load_rec32(rec, t, r);
     float phi[4][3];
     phi4(r.dphi, phi);
     float F[9];
     elem_F<MODEL>(r, u, add_identity, F);
-    unsigned char flag = 0;
     with_law<MODEL>(F, r.pv, corot_exact, [&](const auto &law) {
-      if (!psd_fast_ok(law, phi, tol)) {
-        flag = 1;
-        float N[45];
-        psd_eig_N(law, phi, tol, N);
-        float *o = Nbuf + 45ll * t;
+      float N[45];
+      psd_eig_N(law, phi, tol, N);
+      float *o = Nbuf + 45ll * t;
 #pragma unroll
-        for (int i = 0; i < 45; ++i) o[i] = N[i];
-      }
+      for (int k = 0; k < 45; ++k) o[k] = N[k];
     });
-    slow[t] = flag;
+  }
+}
+
+// Inputs of one incidence (tet t seen from its vertex a): the tet record and
+// the four vertex positions.
+struct HessInc {
+  TetRec32 r;
+  float4 x[4];
+  uint32_t pos;
+  int t, a;
+  bool slow;
+};
+
+template <bool PSD>
+__device__ __forceinline__ void load_inc_head(const int *__restrict__ inc_tet, const uint32_t *__restrict__ inc_pos,
+                                              const TetRec32 *__restrict__ rec, const unsigned char *__restrict__ slow,
+                                              int k, HessInc &h) {
+  const int ta = __ldg(inc_tet + k);
+  h.t = ta >> 2;
+  h.a = ta & 3;
+  h.pos = __ldg(inc_pos + k);
+  load_rec32(rec, ta >> 2, h.r);
+  h.slow = false;
+  if constexpr (PSD) h.slow = __ldg(slow + (ta >> 2)) != 0;
+}
+
+__device__ __forceinline__ void load_inc_x(const float4 *__restrict__ u, HessInc &h) {
+  h.x[0] = __ldg(u + h.r.idx.x);
+  h.x[1] = __ldg(u + h.r.idx.y);
+  h.x[2] = __ldg(u + h.r.idx.z);
+  h.x[3] = __ldg(u + h.r.idx.w);
+}
+
+// Row block a of one element Hessian: the off-diagonal blocks (b != a) are
+// added into the thread's staged CSR rows, the diagonal block (b == a, always
+// the thread's own diagonal position) into the registers D.
+//
+// Unprojected elements: every law is linear in its parameters (K cK =
+// K(cK pv)) and bilinear in (pa, pb) with phi_0 = -(phi_1 + phi_2 + phi_3),
+// so K_a0 = -(K_a1 + K_a2 + K_a3) and only three blocks are evaluated.
+template <int MODEL, bool PSD>
+__device__ __forceinline__ void hess_inc(const HessInc &h, float *row, int rs, float *D, int add_identity, float cK,
+                                         float cM, float tol, int corot_exact, const float *__restrict__ Nbuf) {
+  const int a = h.a;
+  float phi[4][3];
+  phi4(h.r.dphi, phi);
+  float K[4][9];
+  if constexpr (MODEL >= 0) {
+    if (PSD && h.slow) {
+      float N[45];
+      const float *src = Nbuf + 45ll * h.t;
+#pragma unroll
+      for (int i = 0; i < 45; ++i) N[i] = __ldg(src + i);
+      psd_blocks_from_N(N, phi, a, K);
+#pragma unroll
+      for (int b = 0; b < 4; ++b)
+#pragma unroll
+        for (int i = 0; i < 9; ++i) K[b][i] *= cK;
+    } else {
+      float F[9];
+      elem_F_from<MODEL>(h.r, h.x[0], h.x[1], h.x[2], h.x[3], add_identity, F);
+      const float pv[2] = {cK * h.r.pv[0], cK * h.r.pv[1]};
+      float pa[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) pa[d] = a == 0 ? phi[0][d] : a == 1 ? phi[1][d] : a == 2 ? phi[2][d] : phi[3][d];
+      with_law<MODEL>(F, pv, corot_exact, [&](const auto &law) {
+#pragma unroll
+        for (int b = 1; b < 4; ++b) law.block(pa, phi[b], K[b]);
+      });
+#pragma unroll
+      for (int i = 0; i < 9; ++i) K[0][i] = -(K[1][i] + K[2][i] + K[3][i]);
+    }
+    if constexpr (PSD) {
+#pragma unroll
+      for (int b = 0; b < 4; ++b) {
+        K[b][0] += cK * 0.25f * tol;
+        K[b][4] += cK * 0.25f * tol;
+        K[b][8] += cK * 0.25f * tol;
+      }
+    }
+  } else {
+#pragma unroll
+    for (int b = 0; b < 4; ++b)
+#pragma unroll
+      for (int i = 0; i < 9; ++i) K[b][i] = 0.f;
+  }
+  if (cM != 0.f) {
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const float m = cM * h.r.mass * (a == b ? 0.1f : 0.05f);
+      K[b][0] += m;
+      K[b][4] += m;
+      K[b][8] += m;
+    }
+  }
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    if (b == a) {
+#pragma unroll
+      for (int i = 0; i < 9; ++i) D[i] += K[b][i];
+    } else {
+      const int j = (h.pos >> (8 * b)) & 255;
+#pragma unroll
+      for (int kk = 0; kk < 3; ++kk)
+#pragma unroll
+        for (int ll = 0; ll < 3; ++ll) row[kk * rs + 3 * j + ll] += K[b][3 * kk + ll];
+    }
   }
 }
 
@@ -413,7 +555,9 @@ k_psd_prepass(int nT, const TetRec32 *__restrict__ rec, const float4 *__restrict
 // pre-pass), and adds the four 3x3 blocks into its CSR rows staged in shared
 // memory at the positions precomputed in inc_pos. Every entry is therefore
 // summed over its tets in tet order, as the reference's setFromTriplets does.
-// The chunk's values are then written out with coalesced stores.
+// Incidences are loaded two at a time (both load chains, incidence -> tet
+// record -> vertex positions, in flight together) and added in order. The
+// chunk's values are then written out with coalesced stores.
 template <int MODEL, bool PSD>
 __global__ void __launch_bounds__(kChunkMaxVerts)
 k_hess(const int *__restrict__ chunk_v, const int *__restrict__ brp, const int *__restrict__ inc_ptr,
@@ -431,66 +575,27 @@ k_hess(const int *__restrict__ chunk_v, const int *__restrict__ brp, const int *
     const int rb = brp[v];
     const int rs = 3 * (brp[v + 1] - rb);
     float *row = sbuf + 9 * (rb - b0);
-    const int k1 = inc_ptr[v + 1];
-    for (int k = inc_ptr[v]; k < k1; ++k) {
-      const int ta = __ldg(inc_tet + k);
-      const int t = ta >> 2, a = ta & 3;
-      const uint32_t pos = __ldg(inc_pos + k);
-      TetRec32 r;
-      load_rec32(rec, t, r);
-      float phi[4][3];
-      phi4(r.dphi, phi);
-      float K[4][9];
-      if constexpr (MODEL >= 0) {
-        bool from_n = false;
-        if constexpr (PSD) from_n = __ldg(slow + t) != 0;
-        if (from_n) {
-          float N[45];
-          const float *src = Nbuf + 45ll * t;
+    const int k0 = inc_ptr[v], k1 = inc_ptr[v + 1];
+    float D[9];
 #pragma unroll
-          for (int i = 0; i < 45; ++i) N[i] = __ldg(src + i);
-          psd_blocks_from_N(N, phi, a, K);
-        } else {
-          float F[9];
-          elem_F<MODEL>(r, u, add_identity, F);
-          with_law<MODEL>(F, r.pv, corot_exact, [&](const auto &law) {
+    for (int i = 0; i < 9; ++i) D[i] = 0.f;
+    int jd = 0;  // the diagonal block's position in the row
+    for (int k = k0; k < k1; k += 2) {
+      const bool two = k + 1 < k1;
+      HessInc h0, h1;
+      load_inc_head<PSD>(inc_tet, inc_pos, rec, slow, k, h0);
+      load_inc_head<PSD>(inc_tet, inc_pos, rec, slow, two ? k + 1 : k, h1);
+      load_inc_x(u, h0);
+      load_inc_x(u, h1);
+      jd = (h0.pos >> (8 * h0.a)) & 255;
+      hess_inc<MODEL, PSD>(h0, row, rs, D, add_identity, cK, cM, tol, corot_exact, Nbuf);
+      if (two) hess_inc<MODEL, PSD>(h1, row, rs, D, add_identity, cK, cM, tol, corot_exact, Nbuf);
+    }
+    if (k1 > k0) {
 #pragma unroll
-            for (int b = 0; b < 4; ++b) law.block(phi[a], phi[b], K[b]);
-          });
-        }
+      for (int kk = 0; kk < 3; ++kk)
 #pragma unroll
-        for (int b = 0; b < 4; ++b) {
-#pragma unroll
-          for (int i = 0; i < 9; ++i) K[b][i] *= cK;
-          if constexpr (PSD) {
-            K[b][0] += cK * 0.25f * tol;
-            K[b][4] += cK * 0.25f * tol;
-            K[b][8] += cK * 0.25f * tol;
-          }
-        }
-      } else {
-#pragma unroll
-        for (int b = 0; b < 4; ++b)
-#pragma unroll
-          for (int i = 0; i < 9; ++i) K[b][i] = 0.f;
-      }
-      if (cM != 0.f) {
-#pragma unroll
-        for (int b = 0; b < 4; ++b) {
-          const float m = cM * r.mass * (a == b ? 0.1f : 0.05f);
-          K[b][0] += m;
-          K[b][4] += m;
-          K[b][8] += m;
-        }
-      }
-#pragma unroll
-      for (int b = 0; b < 4; ++b) {
-        const int j = (pos >> (8 * b)) & 255;
-#pragma unroll
-        for (int kk = 0; kk < 3; ++kk)
-#pragma unroll
-          for (int ll = 0; ll < 3; ++ll) row[kk * rs + 3 * j + ll] += K[b][3 * kk + ll];
-      }
+        for (int ll = 0; ll < 3; ++ll) row[kk * rs + 3 * jd + ll] += D[3 * kk + ll];
     }
   }
   __syncthreads();
@@ -699,11 +804,17 @@ static int launch_hess_t(bartels_ctx ctx, bartels_mesh_plan plan, const float4 *
   float *nbuf = nullptr;
   if constexpr (PSD && MODEL >= 0) {
     const size_t nT = (size_t)plan->nT;
-    BT_CHECK(plan->w_psd.ensure(nT * (45 * sizeof(float) + 1) + 256));
+    // N (45 floats per tet), the slow-tet list and its count, the flags
+    BT_CHECK(plan->w_psd.ensure(nT * (45 * sizeof(float) + sizeof(int) + 1) + 512));
     nbuf = plan->w_psd.as<float>();
-    slow = reinterpret_cast<unsigned char *>(nbuf + 45 * nT);
-    BT_LAUNCH(ctx, k_psd_prepass<MODEL>, grid_for(ctx, plan->nT, 128), 128, 0, plan->nT, plan->rec32, u,
-              add_identity, tol, corot_exact, slow, nbuf);
+    int *list = reinterpret_cast<int *>(nbuf + 45 * nT);
+    int *count = list + nT;
+    slow = reinterpret_cast<unsigned char *>(count + 32);
+    BT_CUDA(cudaMemsetAsync(count, 0, sizeof(int), ctx->stream));
+    BT_LAUNCH(ctx, k_psd_test<MODEL>, grid_for(ctx, plan->nT, 128), 128, 0, plan->nT, plan->rec32, u, add_identity,
+              tol, corot_exact, slow, list, count);
+    BT_LAUNCH(ctx, k_psd_eig<MODEL>, grid_for(ctx, plan->nT, 128), 128, 0, list, count, plan->rec32, u,
+              add_identity, tol, corot_exact, nbuf);
   }
   BT_LAUNCH(ctx, (k_hess<MODEL, PSD>), plan->nchunks, kChunkMaxVerts, smem, plan->chunk_v, plan->brp, plan->inc_ptr,
             plan->inc_tet, plan->inc_pos, plan->rec32, u, add_identity, cK, cM, tol, corot_exact, slow, nbuf, values);
