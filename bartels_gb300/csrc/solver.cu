@@ -83,43 +83,6 @@ __device__ __forceinline__ double cta_sum_array(const double *__restrict__ a, in
 }
 
 // ------------------------------------------------------------------ SpMV ---
-// FP64 residual r = b - A x (block layout), partial sums of r.r
-__global__ void __launch_bounds__(256)
-k_resid_blk64(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, const float *__restrict__ val,
-              const double *__restrict__ x, const double *__restrict__ b, double *__restrict__ r,
-              const unsigned char *__restrict__ pinned, double *__restrict__ partial) {
-  const int lane = threadIdx.x & 31;
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  double acc = 0.0;
-  for (int v = warp; v < nV; v += nwarps) {
-    const int rb = brp[v];
-    const int rs = 3 * (brp[v + 1] - rb);
-    const float *r0 = val + 9ll * rb;
-    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
-    for (int e = lane; e < rs; e += 32) {
-      const int j = e / 3, l = e - 3 * j;
-      const double xv = x[3 * bcol[rb + j] + l];
-      s0 += (double)r0[e] * xv;
-      s1 += (double)r0[rs + e] * xv;
-      s2 += (double)r0[2 * rs + e] * xv;
-    }
-    s0 = warp_sum(s0);
-    s1 = warp_sum(s1);
-    s2 = warp_sum(s2);
-    if (lane == 0) {
-      double q0 = b[3 * v] - s0, q1 = b[3 * v + 1] - s1, q2 = b[3 * v + 2] - s2;
-      if (pinned && pinned[v]) q0 = q1 = q2 = 0.0;
-      r[3 * v] = q0;
-      r[3 * v + 1] = q1;
-      r[3 * v + 2] = q2;
-      acc += q0 * q0 + q1 * q1 + q2 * q2;
-    }
-  }
-  double s = cta_sum(acc);
-  if (threadIdx.x == 0) partial[blockIdx.x] = s;
-}
-
 // generic scalar CSR (drop-in search direction): one warp per row
 template <bool DOT>
 __global__ void __launch_bounds__(256)
@@ -607,8 +570,92 @@ k_pcg_update(int nb, int n, const float *__restrict__ minv, const float *__restr
   }
 }
 
-__global__ void k_axpy64(int n, const float *__restrict__ dx, double *__restrict__ x) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] += (double)dx[i];
+// x += dx (FP64) and x split into two floats, x = xh + xl to ~2^-48 relative
+// (the vector the refinement residual gathers).
+__global__ void k_axpy64(int n, const float *__restrict__ dx, double *__restrict__ x, float *__restrict__ xh,
+                         float *__restrict__ xl) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double v = dx ? x[i] + (double)dx[i] : x[i];
+    if (dx) x[i] = v;
+    const float h = (float)v;
+    xh[i] = h;
+    xl[i] = (float)(v - (double)h);
+  }
+}
+
+// ---------------------------------------------- float-float residual -------
+// GB300 runs FP64 at a small fraction of its FP32 rate, so the refinement
+// residual r = b - A x works in float-float arithmetic (Dekker / Knuth
+// error-free transformations): each product v (xh + xl) is v xh exactly as
+// p + pe (pe by FMA) plus v xl, and the sums carry their rounding errors in a
+// second float (TwoSum). The explicit-rounding intrinsics keep the compiler
+// from fusing the additions into FMAs, which would break the transformations.
+// The relative error of a row sum is ~2^-48 of sum |A_ij x_j|; FP64 is used
+// only once per row (b - s and r.r).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+__device__ __forceinline__ void ff_mac(float v, float xh, float xl, float &h, float &l) {
+  const float p = __fmul_rn(v, xh);
+  const float pe = __fmaf_rn(v, xh, -p);
+  float t, e;
+  two_sum(h, p, t, e);
+  h = t;
+  l = __fadd_rn(l, __fadd_rn(e, __fmaf_rn(v, xl, pe)));
+}
+
+template <int G>
+__device__ __forceinline__ void ff_group_reduce(float &h, float &l) {
+#pragma unroll
+  for (int o = G / 2; o > 0; o >>= 1) {
+    const float h2 = __shfl_xor_sync(0xffffffffu, h, o), l2 = __shfl_xor_sync(0xffffffffu, l, o);
+    float t, e;
+    two_sum(h, h2, t, e);
+    h = t;
+    l = __fadd_rn(__fadd_rn(l, l2), e);
+  }
+}
+
+// r = b - A x (block layout, x = xh + xl), partial sums of r.r per block
+template <int G>
+__global__ void __launch_bounds__(256)
+k_resid_blk_ff(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, const float *__restrict__ val,
+               const float *__restrict__ xh, const float *__restrict__ xl, const double *__restrict__ b,
+               double *__restrict__ r, const unsigned char *__restrict__ pinned, double *__restrict__ partial) {
+  double acc = 0.0;
+  BT_ROW_LOOP_BEGIN(G)
+  float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f, h2 = 0.f, l2 = 0.f;
+  if (active) {
+    const int rb = __ldg(brp + v);
+    const int rs = 3 * (__ldg(brp + v + 1) - rb);
+    const float *r0 = val + 9ll * rb;
+    for (int e = sl; e < rs; e += G) {
+      const int j = e / 3, c = 3 * __ldg(bcol + rb + j) + (e - 3 * j);
+      const float a = __ldg(xh + c), al = __ldg(xl + c);
+      ff_mac(__ldcs(r0 + e), a, al, h0, l0);
+      ff_mac(__ldcs(r0 + rs + e), a, al, h1, l1);
+      ff_mac(__ldcs(r0 + 2 * rs + e), a, al, h2, l2);
+    }
+  }
+  ff_group_reduce<G>(h0, l0);
+  ff_group_reduce<G>(h1, l1);
+  ff_group_reduce<G>(h2, l2);
+  if (active && sl == 0) {
+    double q0 = b[3 * v] - ((double)h0 + (double)l0);
+    double q1 = b[3 * v + 1] - ((double)h1 + (double)l1);
+    double q2 = b[3 * v + 2] - ((double)h2 + (double)l2);
+    if (pinned && pinned[v]) q0 = q1 = q2 = 0.0;
+    r[3 * v] = q0;
+    r[3 * v + 1] = q1;
+    r[3 * v + 2] = q2;
+    acc += q0 * q0 + q1 * q1 + q2 * q2;
+  }
+  BT_ROW_LOOP_END
+  double s = cta_sum(acc);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
 
 __global__ void k_scale_copy(int n, double a, const double *__restrict__ x, double *__restrict__ y) {
@@ -830,7 +877,7 @@ struct PcgOperator {
 };
 
 struct PcgWork {
-  float *x, *r, *z, *pa, *pb, *ap, *minv;
+  float *x, *r, *z, *pa, *pb, *ap, *minv, *xh, *xl;
   double *r64, *part_a, *part_b;
   PcgState *st;
 };
@@ -924,6 +971,7 @@ static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double
   };
   const size_t o_x = take(4ull * n), o_r = take(4ull * n), o_z = take(4ull * n), o_pa = take(4ull * n),
                o_pb = take(4ull * n), o_ap = take(4ull * n), o_minv = take(24ull * nb), o_r64 = take(8ull * n),
+               o_xh = take(4ull * n), o_xl = take(4ull * n),
                o_pa8 = take(8ull * nparts), o_pb8 = take(8ull * nparts), o_st = take(sizeof(PcgState));
   BT_CHECK(wbuf.ensure(off));
   char *base = wbuf.as<char>();
@@ -936,6 +984,8 @@ static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double
   w.ap = (float *)(base + o_ap);
   w.minv = (float *)(base + o_minv);
   w.r64 = (double *)(base + o_r64);
+  w.xh = (float *)(base + o_xh);
+  w.xl = (float *)(base + o_xl);
   w.part_a = (double *)(base + o_pa8);
   w.part_b = (double *)(base + o_pb8);
   w.st = (PcgState *)(base + o_st);
@@ -985,8 +1035,9 @@ static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double
   for (int pass = 0; pass <= prm.max_refinements; ++pass) {
     // r64 = b - A x (FP64)
     if (blk) {
-      BT_LAUNCH(ctx, k_resid_blk64, gs, 256, 0, op.plan->nV, op.plan->brp, op.plan->bcol, op.values, x, b, w.r64,
-                op.pinned, w.part_a);
+      if (pass == 0) BT_LAUNCH(ctx, k_axpy64, grid_vec(ctx, n), 256, 0, n, nullptr, x, w.xh, w.xl);
+      BT_LAUNCH(ctx, k_resid_blk_ff<16>, gs, 256, 0, op.plan->nV, op.plan->brp, op.plan->bcol, op.values, w.xh, w.xl,
+                b, w.r64, op.pinned, w.part_a);
     } else {
       BT_LAUNCH(ctx, k_resid_csr64, gs, 256, 0, n, op.rp, op.ci, op.values, op.values64, x, b, w.r64, w.part_a);
     }
@@ -1030,7 +1081,7 @@ static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double
       if (hs.done) break;
     }
     rep->iterations += hs.it - it0;
-    BT_LAUNCH(ctx, k_axpy64, grid_vec(ctx, n), 256, 0, n, w.x, x);
+    BT_LAUNCH(ctx, k_axpy64, grid_vec(ctx, n), 256, 0, n, w.x, x, w.xh, w.xl);
   }
   cudaGraphExecDestroy(exec);
   return status;

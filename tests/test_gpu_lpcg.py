@@ -180,6 +180,29 @@ def test_zero_head_factor_pcg_equals_block_jacobi():
     net.close()
 
 
+def test_refinement_residual_matches_fp64():
+    """The float-float refinement residual (k_resid_blk_ff) against an FP64 host
+    residual of the same FP32 matrix, with reliable updates and with restarts."""
+    torch = _torch()
+    plan, vals, g, A = _system(12, coeff=1e-2)
+    from bartels_gb300 import lpcg
+    lpcg.use_block_jacobi(plan)
+    pin = np.repeat(g.pinned, 3)
+    bh = np.random.default_rng(5).standard_normal(3 * g.nV)
+    bh[pin] = 0.0
+    H = plan.csr(vals.cpu().numpy().astype(np.float64))
+    for restart, inner in ((0, 0.1), (1, 1e-4)):
+        b = torch.from_numpy(bh).cuda()
+        x = torch.zeros_like(b)
+        rep = lpcg.plan_pcg(plan, vals, b, x, restart=restart, inner_rel_tol=inner)
+        xh = x.cpu().numpy()
+        r = bh - H @ xh
+        r[pin] = 0.0
+        rel = np.linalg.norm(r) / np.linalg.norm(bh)
+        assert rep.converged and rel <= 1.001e-8, (restart, rel, rep.rel_residual)
+        assert abs(rel - rep.rel_residual) <= 1e-3 * rel + 1e-15, (restart, rel, rep.rel_residual)
+
+
 def test_residual_probe_training_step_runs():
     torch = _torch()
     plan, vals, g, A = _system(4)
