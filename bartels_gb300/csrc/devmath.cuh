@@ -279,6 +279,47 @@ BT_HD void svd3(const T *F, T *U, T *S, T *V) {
     for (int j = 0; j < 3; ++j)
       A[i + 3 * j] = F[0 + 3 * i] * F[0 + 3 * j] + F[1 + 3 * i] * F[1 + 3 * j] + F[2 + 3 * i] * F[2 + 3 * j];
   for (int i = 0; i < 9; ++i) V[i] = (i % 4 == 0) ? T(1) : T(0);
+  if constexpr (sizeof(T) == 8) {
+    // Warm start for the FP64 path (FP64 runs at a small fraction of the FP32
+    // rate on this GPU): FP32 sweeps give V diagonalising F^T F to ~1e-7, two
+    // Newton-Schulz steps V <- V (3 I - V^T V) / 2 in FP64 make it orthonormal
+    // to rounding, and A = V^T (F^T F) V is then diagonal to ~1e-7, so the FP64
+    // sweeps below (same stopping test) need one or two passes instead of ~5.
+    float Af[9], Vf[9];
+    for (int i = 0; i < 9; ++i) {
+      Af[i] = (float)A[i];
+      Vf[i] = (i % 4 == 0) ? 1.f : 0.f;
+    }
+    for (int s = 0; s < 6; ++s) {
+      const float off = Af[3] * Af[3] + Af[6] * Af[6] + Af[7] * Af[7];
+      const float dia = Af[0] * Af[0] + Af[4] * Af[4] + Af[8] * Af[8];
+      if (off <= 1e-14f * dia) break;
+      jacobi_rot(Af, Vf, 0, 1);
+      jacobi_rot(Af, Vf, 0, 2);
+      jacobi_rot(Af, Vf, 1, 2);
+    }
+    for (int i = 0; i < 9; ++i) V[i] = (T)Vf[i];
+    for (int it = 0; it < 2; ++it) {
+      T M[9], W[9], Vn[9];
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+          M[i + 3 * j] = V[3 * i] * V[3 * j] + V[1 + 3 * i] * V[1 + 3 * j] + V[2 + 3 * i] * V[2 + 3 * j];
+      for (int i = 0; i < 9; ++i) W[i] = ((i % 4 == 0) ? T(1.5) : T(0)) - T(0.5) * M[i];
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) Vn[i + 3 * j] = V[i] * W[3 * j] + V[i + 3] * W[1 + 3 * j] + V[i + 6] * W[2 + 3 * j];
+      for (int i = 0; i < 9; ++i) V[i] = Vn[i];
+    }
+    T AV[9];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        AV[i + 3 * j] = A[i] * V[3 * j] + A[i + 3] * V[1 + 3 * j] + A[i + 6] * V[2 + 3 * j];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j <= i; ++j) {
+        const T a = V[3 * i] * AV[3 * j] + V[1 + 3 * i] * AV[1 + 3 * j] + V[2 + 3 * i] * AV[2 + 3 * j];
+        const T b = V[3 * j] * AV[3 * i] + V[1 + 3 * j] * AV[1 + 3 * i] + V[2 + 3 * j] * AV[2 + 3 * i];
+        A[i + 3 * j] = A[j + 3 * i] = T(0.5) * (a + b);
+      }
+  }
   const int sweeps = sizeof(T) == 4 ? 6 : 12;
   for (int s = 0; s < sweeps; ++s) {
     T off = A[3] * A[3] + A[6] * A[6] + A[7] * A[7];
@@ -420,8 +461,17 @@ BT_HD void arap_pv(const T *pv, T *out) {
 // ----------------------------------------------------------------------------
 // FP64 energy and first Piola-Kirchhoff stress (scaled by vol via pv)
 // ----------------------------------------------------------------------------
+// ARAP maps its parameters and continues in the corotational branch (no
+// recursive call: device recursion leaves the stack size undetermined).
 template <class T>
-BT_HD T psi_model(int model, const T *F, const T *pv) {
+BT_HD T psi_model(int model, const T *F, const T *pv_in) {
+  T pa[2];
+  const T *pv = pv_in;
+  if (model == MODEL_ARAP) {
+    arap_pv(pv_in, pa);
+    pv = pa;
+    model = MODEL_COROT;
+  }
   if (model == MODEL_LE) {
     // mu e:e + lambda/2 tr(e)^2, e = sym(F) (the reference's strain of q as given)
     T ee = T(0);
@@ -432,11 +482,6 @@ BT_HD T psi_model(int model, const T *F, const T *pv) {
       }
     const T tr = F[0] + F[4] + F[8];
     return pv[1] * ee + T(0.5) * pv[0] * tr * tr;
-  }
-  if (model == MODEL_ARAP) {
-    T pa[2];
-    arap_pv(pv, pa);
-    return psi_model(MODEL_COROT, F, pa);
   }
   if (model == MODEL_NH || model == MODEL_NH_ISO) {
     T J = det3(F), I1 = T(0);
@@ -464,18 +509,19 @@ BT_HD T psi_model(int model, const T *F, const T *pv) {
 }
 
 template <class T>
-BT_HD void pk1_model(int model, const T *F, const T *pv, T *P) {
+BT_HD void pk1_model(int model, const T *F, const T *pv_in, T *P) {
+  T pa[2];
+  const T *pv = pv_in;
+  if (model == MODEL_ARAP) {
+    arap_pv(pv_in, pa);
+    pv = pa;
+    model = MODEL_COROT;
+  }
   if (model == MODEL_LE) {
     const T tr = F[0] + F[4] + F[8];
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j)
         P[i + 3 * j] = pv[1] * (F[i + 3 * j] + F[j + 3 * i]) + (i == j ? pv[0] * tr : T(0));
-    return;
-  }
-  if (model == MODEL_ARAP) {
-    T pa[2];
-    arap_pv(pv, pa);
-    pk1_model(MODEL_COROT, F, pa, P);
     return;
   }
   if (model == MODEL_NH || model == MODEL_NH_ISO) {

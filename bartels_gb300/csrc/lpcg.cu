@@ -978,7 +978,7 @@ static int lp_state(bartels_mesh_plan plan, bool train, int nprobe, LpcgPlanStat
   plan->lpcg = nullptr;
   s = new LpcgPlanState();
   plan->lpcg = s;
-  const size_t nV = plan->nV, nnzb = plan->nnzb, nnzl = fp->nnzl, nnzu = fp->nnzu;
+  const size_t nV = plan->nV, nnzb = plan->nnzb, nnzl = fp->nnzl;
   s->nV = plan->nV;
   s->nnzb = plan->nnzb;
   s->nnzl = fp->nnzl;

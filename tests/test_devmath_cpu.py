@@ -164,6 +164,40 @@ def test_svd3_float_and_double(oracle):
         assert np.linalg.norm(Um @ np.diag(S32.astype(float)) @ Vm.T - F) <= 1e-5 * np.linalg.norm(F)
 
 
+def test_svd3_double_hard_cases():
+    """The FP64 SVD (FP32 warm start, Newton-Schulz re-orthonormalisation, FP64
+    sweeps) at machine precision on near-rest, rotated, repeated, nearly
+    repeated and inverted deformation gradients."""
+    L = devmath()
+    rng = np.random.default_rng(17)
+
+    def rot():
+        q, _ = np.linalg.qr(rng.standard_normal((3, 3)))
+        return q * np.sign(np.linalg.det(q))
+    for k in range(100):
+        t = k % 5
+        if t == 0:
+            F = np.eye(3) + 1e-6 * rng.standard_normal((3, 3))
+        elif t == 1:
+            F = rot()
+        elif t == 2:
+            F = rot() @ np.diag([1.0, 1.0, 2.0]) @ rot()
+        elif t == 3:
+            F = rot() @ np.diag([1.5, 0.7, -0.3]) @ rot()
+        else:
+            F = rot() @ np.diag([1.0, 1.0 + 1e-9, 1.0 - 1e-9]) @ rot()
+        fv = np.ascontiguousarray(F.ravel(order="F"))
+        U, S, V = np.zeros(9), np.zeros(3), np.zeros(9)
+        L.dm_svd3_d(dp(fv), dp(U), dp(S), dp(V))
+        Um, Vm = U.reshape(3, 3, order="F"), V.reshape(3, 3, order="F")
+        assert np.linalg.norm(Um @ np.diag(S) @ Vm.T - F) <= 1e-14 * np.linalg.norm(F), (k, t)
+        assert np.linalg.norm(Vm.T @ Vm - np.eye(3)) <= 1e-14 and np.linalg.norm(Um.T @ Um - np.eye(3)) <= 1e-14
+        assert np.linalg.det(Um) > 0 and np.linalg.det(Vm) > 0
+        sv = np.sort(np.abs(S))[::-1]
+        assert np.abs(sv - np.linalg.svd(F, compute_uv=False)).max() <= 1e-14 * sv[0], (k, t)
+        assert (S[2] < 0) == (np.linalg.det(F) < 0)
+
+
 @pytest.mark.parametrize("model", ["neohookean", "neohookean_isochoric", "stvk"])
 def test_cancellation_free_energy_accuracy(oracle, model):
     """psi from the displacement gradient H = F - I (used by the GPU energy and
