@@ -388,10 +388,11 @@ __device__ __forceinline__ void with_law(const float *F, const float *pv, int co
 // changes the element matrix beyond its translation modes (the exact test
 // psd_fast_ok) and flag the tet; flagged tets are appended to a list (the
 // order of the list does not matter: each entry writes only its own tet).
+// F and the flag are stored per tet (12 floats) for the assembly kernel.
 template <int MODEL>
 __global__ void __launch_bounds__(128)
 k_psd_test(int nT, const TetRec32 *__restrict__ rec, const float4 *__restrict__ u, int add_identity, float tol,
-           int corot_exact, unsigned char *__restrict__ slow, int *__restrict__ list, int *__restrict__ count) {
+           int corot_exact, float4 *__restrict__ fslot, int *__restrict__ list, int *__restrict__ count) {
   for (int t0 = blockIdx.x * blockDim.x; t0 < nT; t0 += gridDim.x * blockDim.x) {
     const int t = t0 + threadIdx.x;
     bool flag = false;
@@ -403,7 +404,11 @@ k_psd_test(int nT, const TetRec32 *__restrict__ rec, const float4 *__restrict__ 
       float F[9];
       elem_F<MODEL>(r, u, add_identity, F);
       with_law<MODEL>(F, r.pv, corot_exact, [&](const auto &law) { flag = !psd_fast_ok(law, phi, tol); });
-      slow[t] = flag ? 1 : 0;
+      // the assembly reads F and the flag from here instead of gathering the vertices again
+      float4 *o = fslot + 3ll * t;
+      o[0] = make_float4(F[0], F[1], F[2], F[3]);
+      o[1] = make_float4(F[4], F[5], F[6], F[7]);
+      o[2] = make_float4(F[8], flag ? 1.f : 0.f, 0.f, 0.f);
     }
     // warp-aggregated append
     const unsigned m = __ballot_sync(0xffffffffu, flag);
@@ -452,9 +457,12 @@ struct HessInc {
   bool slow;
 };
 
-template <bool PSD>
+// With the PSD pre-pass (PRE) the tet's F and projection flag come from its
+// 12-float slot (x[0..2]) together with the record; otherwise the four vertex
+// positions are gathered (x[0..3]) after the record.
+template <bool PRE>
 __device__ __forceinline__ void load_inc_head(const int *__restrict__ inc_tet, const uint32_t *__restrict__ inc_pos,
-                                              const TetRec32 *__restrict__ rec, const unsigned char *__restrict__ slow,
+                                              const TetRec32 *__restrict__ rec, const float4 *__restrict__ fslot,
                                               int k, HessInc &h) {
   const int ta = __ldg(inc_tet + k);
   h.t = ta >> 2;
@@ -462,14 +470,23 @@ __device__ __forceinline__ void load_inc_head(const int *__restrict__ inc_tet, c
   h.pos = __ldg(inc_pos + k);
   load_rec32(rec, ta >> 2, h.r);
   h.slow = false;
-  if constexpr (PSD) h.slow = __ldg(slow + (ta >> 2)) != 0;
+  if constexpr (PRE) {
+    const float4 *f = fslot + 3ll * h.t;
+    h.x[0] = __ldg(f);
+    h.x[1] = __ldg(f + 1);
+    h.x[2] = __ldg(f + 2);
+    h.slow = h.x[2].y != 0.f;
+  }
 }
 
+template <bool PRE>
 __device__ __forceinline__ void load_inc_x(const float4 *__restrict__ u, HessInc &h) {
-  h.x[0] = __ldg(u + h.r.idx.x);
-  h.x[1] = __ldg(u + h.r.idx.y);
-  h.x[2] = __ldg(u + h.r.idx.z);
-  h.x[3] = __ldg(u + h.r.idx.w);
+  if constexpr (!PRE) {
+    h.x[0] = __ldg(u + h.r.idx.x);
+    h.x[1] = __ldg(u + h.r.idx.y);
+    h.x[2] = __ldg(u + h.r.idx.z);
+    h.x[3] = __ldg(u + h.r.idx.w);
+  }
 }
 
 // Row block a of one element Hessian: the off-diagonal blocks (b != a) are
@@ -499,7 +516,13 @@ __device__ __forceinline__ void hess_inc(const HessInc &h, float *row, int rs, f
         for (int i = 0; i < 9; ++i) K[b][i] *= cK;
     } else {
       float F[9];
-      elem_F_from<MODEL>(h.r, h.x[0], h.x[1], h.x[2], h.x[3], add_identity, F);
+      if constexpr (PSD) {
+        F[0] = h.x[0].x; F[1] = h.x[0].y; F[2] = h.x[0].z; F[3] = h.x[0].w;
+        F[4] = h.x[1].x; F[5] = h.x[1].y; F[6] = h.x[1].z; F[7] = h.x[1].w;
+        F[8] = h.x[2].x;
+      } else {
+        elem_F_from<MODEL>(h.r, h.x[0], h.x[1], h.x[2], h.x[3], add_identity, F);
+      }
       const float pv[2] = {cK * h.r.pv[0], cK * h.r.pv[1]};
       float pa[3];
 #pragma unroll
@@ -563,7 +586,8 @@ __global__ void __launch_bounds__(kChunkMaxVerts)
 k_hess(const int *__restrict__ chunk_v, const int *__restrict__ brp, const int *__restrict__ inc_ptr,
        const int *__restrict__ inc_tet, const uint32_t *__restrict__ inc_pos, const TetRec32 *__restrict__ rec,
        const float4 *__restrict__ u, int add_identity, float cK, float cM, float tol, int corot_exact,
-       const unsigned char *__restrict__ slow, const float *__restrict__ Nbuf, float *__restrict__ values) {
+       const float4 *__restrict__ fslot, const float *__restrict__ Nbuf, float *__restrict__ values) {
+  constexpr bool PRE = PSD && MODEL >= 0;
   extern __shared__ float sbuf[];
   const int v0 = chunk_v[blockIdx.x], v1 = chunk_v[blockIdx.x + 1];
   const int b0 = brp[v0];
@@ -583,10 +607,10 @@ k_hess(const int *__restrict__ chunk_v, const int *__restrict__ brp, const int *
     for (int k = k0; k < k1; k += 2) {
       const bool two = k + 1 < k1;
       HessInc h0, h1;
-      load_inc_head<PSD>(inc_tet, inc_pos, rec, slow, k, h0);
-      load_inc_head<PSD>(inc_tet, inc_pos, rec, slow, two ? k + 1 : k, h1);
-      load_inc_x(u, h0);
-      load_inc_x(u, h1);
+      load_inc_head<PRE>(inc_tet, inc_pos, rec, fslot, k, h0);
+      load_inc_head<PRE>(inc_tet, inc_pos, rec, fslot, two ? k + 1 : k, h1);
+      load_inc_x<PRE>(u, h0);
+      load_inc_x<PRE>(u, h1);
       jd = (h0.pos >> (8 * h0.a)) & 255;
       hess_inc<MODEL, PSD>(h0, row, rs, D, add_identity, cK, cM, tol, corot_exact, Nbuf);
       if (two) hess_inc<MODEL, PSD>(h1, row, rs, D, add_identity, cK, cM, tol, corot_exact, Nbuf);
@@ -800,24 +824,24 @@ static int launch_hess_t(bartels_ctx ctx, bartels_mesh_plan plan, const float4 *
     BT_CUDA(cudaFuncSetAttribute(k_hess<MODEL, PSD>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     attr_set = true;
   }
-  unsigned char *slow = nullptr;
+  float4 *fslot = nullptr;
   float *nbuf = nullptr;
   if constexpr (PSD && MODEL >= 0) {
     const size_t nT = (size_t)plan->nT;
-    // N (45 floats per tet), the slow-tet list and its count, the flags
-    BT_CHECK(plan->w_psd.ensure(nT * (45 * sizeof(float) + sizeof(int) + 1) + 512));
-    nbuf = plan->w_psd.as<float>();
+    // F + flag slots (12 floats per tet), N (45 floats per tet), the slow-tet list and its count
+    BT_CHECK(plan->w_psd.ensure(nT * (57 * sizeof(float) + sizeof(int)) + 512));
+    fslot = plan->w_psd.as<float4>();
+    nbuf = reinterpret_cast<float *>(fslot + 3 * nT);
     int *list = reinterpret_cast<int *>(nbuf + 45 * nT);
     int *count = list + nT;
-    slow = reinterpret_cast<unsigned char *>(count + 32);
     BT_CUDA(cudaMemsetAsync(count, 0, sizeof(int), ctx->stream));
     BT_LAUNCH(ctx, k_psd_test<MODEL>, grid_for(ctx, plan->nT, 128), 128, 0, plan->nT, plan->rec32, u, add_identity,
-              tol, corot_exact, slow, list, count);
+              tol, corot_exact, fslot, list, count);
     BT_LAUNCH(ctx, k_psd_eig<MODEL>, grid_for(ctx, plan->nT, 128), 128, 0, list, count, plan->rec32, u,
               add_identity, tol, corot_exact, nbuf);
   }
   BT_LAUNCH(ctx, (k_hess<MODEL, PSD>), plan->nchunks, kChunkMaxVerts, smem, plan->chunk_v, plan->brp, plan->inc_ptr,
-            plan->inc_tet, plan->inc_pos, plan->rec32, u, add_identity, cK, cM, tol, corot_exact, slow, nbuf, values);
+            plan->inc_tet, plan->inc_pos, plan->rec32, u, add_identity, cK, cM, tol, corot_exact, fslot, nbuf, values);
   return BARTELS_OK;
 }
 
