@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--precond", default="learned", choices=["learned", "jacobi"])
     ap.add_argument("--weights", default=os.path.join(ROOT, "bartels_gb300", "weights", "lpcg_neohookean.npz"))
     ap.add_argument("--no-jacobi-arm", action="store_true", help="skip the block-Jacobi comparison run")
+    ap.add_argument("--no-autotune", action="store_true", help="default lane counts instead of the autotuner's")
     return ap.parse_args()
 
 
@@ -177,6 +178,20 @@ def run_gpu(args, rank, world):
                            mass_coeff=1.0, scale=pb["dt"], force_scale=pb["dt"], max_iterations=100)
     x = torch.zeros(3 * nV, dtype=torch.float64, device=f"cuda:{dev}")
     xp = C.c_void_p(x.data_ptr())
+    # lane counts of the SpMV and factor passes from the library's autotuner (plan setup,
+    # outside the timed region), on the Hessian of the rest state
+    lanes = None
+    if not args.no_autotune:
+        hv = torch.empty(plan.nnz, dtype=torch.float32, device=f"cuda:{dev}")
+        q0 = torch.from_numpy(qt).to(f"cuda:{dev}")
+        _lib.check(L.bartels_plan_hessian_d(ctx.handle, plan.handle, bg.api.MODELS[args.model], psd, 1e-6, 0,
+                                            pb["dt"] ** 2, 1.0, C.c_void_p(q0.data_ptr()), C.c_void_p(hv.data_ptr())),
+                   "hessian")
+        a_l, b_l = C.c_int(), C.c_int()
+        _lib.check(L.bartels_plan_autotune(ctx.handle, plan.handle, C.c_void_p(hv.data_ptr()), 0, C.byref(a_l),
+                                           C.byref(b_l)), "autotune")
+        lanes = {"spmv": a_l.value, "factor": b_l.value}
+        del hv, q0
     net = None
     if args.precond == "learned":
         from bartels_gb300 import lpcg
@@ -321,6 +336,7 @@ def run_gpu(args, rank, world):
         jv = replica_value(jac["newton_its"], world, jac["ms"])
         jacobi_pcg = {"value": jv, "unit": UNIT, "ms_per_step": jac["ms"] / max(jac["newton_its"], 1),
                       "pcg_iters_per_newton": jac["pcg_its"] / max(jac["newton_its"], 1),
+                      "ls_backtracks_per_newton": jac["ls_its"] / max(jac["newton_its"], 1),
                       "newton_iterations": jac["newton_its"], "clocks": jac["clocks"],
                       "learned_over_jacobi": value / jv if jv > 0 else None}
     out = {
@@ -333,7 +349,7 @@ def run_gpu(args, rank, world):
                                f"{'off' if args.no_psd else 'simple_psd_fix 1e-6'}, {precond_name} PCG 1e-8, "
                                "Newton 1e-8 relative", "preconditioner": precond_name,
                    "learned_pcg_weights": os.path.relpath(args.weights, ROOT) if net is not None else None,
-                   "parallelism": f"replicas x{world}",
+                   "parallelism": f"replicas x{world}", "lanes_per_row": lanes,
                    "l2": "inputs larger than L2 (CSR values %.0f MB)" % (4 * nnz / 1e6)},
         "newton_iterations": newton_its, "pcg_iterations": pcg_its,
         "pcg_iters_per_newton": pcg_its / max(newton_its, 1),
