@@ -3,8 +3,9 @@
 Workload (one "step" = one Newton iteration): implicit Euler in velocity form
 (dt = 0.01) from rest under gravity, z = 0 face pinned, Neo-Hookean E = 2e6 Pa,
 nu = 0.45, rho = 1000, Hessians PSD-projected (simple_psd_fix, tol 1e-6), each
-Newton system solved by PCG to 1e-8 relative residual (FP32 PCG, FP64 residual
-refinement), Newton to 1e-8 relative gradient norm; when a time step converges
+Newton system solved by PCG to 1e-8 relative residual (FP32 PCG; the residual
+b - A x is recomputed to ~2^-48 (float-float) after every 10x reduction and CG
+continues against it), Newton to 1e-8 relative gradient norm; when a time step converges
 the next one starts. Synthetic, seeded inputs (no dataset).
 
 The headline value uses the learned preconditioner (the network's factor G is

@@ -214,7 +214,8 @@ typedef struct {
   double rel_tol;       /* relative residual target ||b - A x|| / ||b|| (default 1e-8) */
   int max_iters;        /* total PCG iterations cap (default 20000) */
   double inner_rel_tol; /* FP32 inner PCG: reduction of the residual per refinement pass (default 0.1) */
-  int max_refinements;  /* FP64 residual refinement passes (default 40) */
+  int max_refinements;  /* residual refinement passes (default 40); the refinement residual is
+                           float-float (~2^-48 relative) on the block layout, FP64 on a CSR */
   int restart;          /* 0 (default): each refinement pass replaces the FP32 residual by the FP64 one
                            b - A x and continues the previous pass's search direction (reliable update,
                            one replacement per 10x reduction by default); 1: each pass restarts the inner
