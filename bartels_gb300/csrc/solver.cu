@@ -112,7 +112,7 @@ k_spmv_csr(int n, const int *__restrict__ rp, const int *__restrict__ ci, const 
 __global__ void __launch_bounds__(256)
 k_resid_csr64(int n, const int *__restrict__ rp, const int *__restrict__ ci, const float *__restrict__ val,
               const double *__restrict__ val64, const double *__restrict__ x, const double *__restrict__ b,
-              double *__restrict__ r, double *__restrict__ partial) {
+              float *__restrict__ r, double *__restrict__ partial) {
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -123,7 +123,7 @@ k_resid_csr64(int n, const int *__restrict__ rp, const int *__restrict__ ci, con
     s = warp_sum(s);
     if (lane == 0) {
       double q = b[i] - s;
-      r[i] = q;
+      r[i] = (float)q;
       acc += q * q;
     }
   }
@@ -248,12 +248,12 @@ __device__ __forceinline__ double sum_partials(const double *a, int n) {
   return cta_sum(acc);
 }
 
-// start of an inner solve: x = 0, r = (float) r64, z = M^-1 r. A fresh solve
+// start of an inner solve: x = 0, r = rres (the refinement residual), z = M^-1 r. A fresh solve
 // (cont = 0) clears p and the iteration count; a continued one (cont = 1, the
 // reliable update) keeps the previous pass's last direction and iteration
 // count, and takes beta = r'.z' / r_k.z_k against the replaced residual r'
 // (r_k.z_k = r.z / beta of the previous pass's last update).
-__global__ void k_pcg_init(int nb, int n, const double *__restrict__ r64, const float *__restrict__ minv,
+__global__ void k_pcg_init(int nb, int n, const float *__restrict__ rres, const float *__restrict__ minv,
                            float *__restrict__ x, float *__restrict__ r, float *__restrict__ z,
                            float *__restrict__ p0, float *__restrict__ p1, double *__restrict__ part_a,
                            double *__restrict__ part_b, PcgState *__restrict__ st, double inner_rel2, double abs_tol2,
@@ -261,7 +261,7 @@ __global__ void k_pcg_init(int nb, int n, const double *__restrict__ r64, const 
   float arz = 0.f, arr = 0.f;
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nb; v += gridDim.x * blockDim.x) {
     float rv[3], zv[3];
-    for (int k = 0; k < 3; ++k) rv[k] = (3 * v + k < n) ? (float)r64[3 * v + k] : 0.f;
+    for (int k = 0; k < 3; ++k) rv[k] = (3 * v + k < n) ? rres[3 * v + k] : 0.f;
     apply_minv(minv, v, rv, zv);
     for (int k = 0; k < 3; ++k) {
       const int i = 3 * v + k;
@@ -583,6 +583,16 @@ __global__ void k_axpy64(int n, const float *__restrict__ dx, double *__restrict
   }
 }
 
+// b split into two floats, b = bh + bl to ~2^-48 relative (once per solve)
+__global__ void k_split64(int n, const double *__restrict__ b, float *__restrict__ bh, float *__restrict__ bl) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double v = b[i];
+    const float h = (float)v;
+    bh[i] = h;
+    bl[i] = (float)(v - (double)h);
+  }
+}
+
 // ---------------------------------------------- float-float residual -------
 // GB300 runs FP64 at a small fraction of its FP32 rate, so the refinement
 // residual r = b - A x works in float-float arithmetic (Dekker / Knuth
@@ -619,15 +629,18 @@ __device__ __forceinline__ void ff_group_reduce(float &h, float &l) {
   }
 }
 
-// r = b - A x (block layout, x = xh + xl), partial sums of r.r per block
+// r = b - A x (block layout, x = xh + xl, b = bh + bl), rounded to FP32 (the
+// inner solve's residual); partial sums of r.r per block. No FP64 work: on
+// this GPU one FP64 warp instruction costs about as much as 64 FP32 ones.
 template <int G>
 __global__ void __launch_bounds__(256)
 k_resid_blk_ff(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, const float *__restrict__ val,
-               const float *__restrict__ xh, const float *__restrict__ xl, const double *__restrict__ b,
-               double *__restrict__ r, const unsigned char *__restrict__ pinned, double *__restrict__ partial) {
-  double acc = 0.0;
+               const float *__restrict__ xh, const float *__restrict__ xl, const float *__restrict__ bh,
+               const float *__restrict__ bl, float *__restrict__ r, const unsigned char *__restrict__ pinned,
+               double *__restrict__ partial) {
+  float acc = 0.f;
   BT_ROW_LOOP_BEGIN(G)
-  float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f, h2 = 0.f, l2 = 0.f;
+  float h[3] = {0.f, 0.f, 0.f}, l[3] = {0.f, 0.f, 0.f};
   if (active) {
     const int rb = __ldg(brp + v);
     const int rs = 3 * (__ldg(brp + v + 1) - rb);
@@ -635,26 +648,27 @@ k_resid_blk_ff(int nV, const int *__restrict__ brp, const int *__restrict__ bcol
     for (int e = sl; e < rs; e += G) {
       const int j = e / 3, c = 3 * __ldg(bcol + rb + j) + (e - 3 * j);
       const float a = __ldg(xh + c), al = __ldg(xl + c);
-      ff_mac(__ldcs(r0 + e), a, al, h0, l0);
-      ff_mac(__ldcs(r0 + rs + e), a, al, h1, l1);
-      ff_mac(__ldcs(r0 + 2 * rs + e), a, al, h2, l2);
+      ff_mac(__ldcs(r0 + e), a, al, h[0], l[0]);
+      ff_mac(__ldcs(r0 + rs + e), a, al, h[1], l[1]);
+      ff_mac(__ldcs(r0 + 2 * rs + e), a, al, h[2], l[2]);
     }
   }
-  ff_group_reduce<G>(h0, l0);
-  ff_group_reduce<G>(h1, l1);
-  ff_group_reduce<G>(h2, l2);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) ff_group_reduce<G>(h[k], l[k]);
   if (active && sl == 0) {
-    double q0 = b[3 * v] - ((double)h0 + (double)l0);
-    double q1 = b[3 * v + 1] - ((double)h1 + (double)l1);
-    double q2 = b[3 * v + 2] - ((double)h2 + (double)l2);
-    if (pinned && pinned[v]) q0 = q1 = q2 = 0.0;
-    r[3 * v] = q0;
-    r[3 * v + 1] = q1;
-    r[3 * v + 2] = q2;
-    acc += q0 * q0 + q1 * q1 + q2 * q2;
+    const bool pin = pinned && pinned[v];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      // (bh + bl) - (h + l) in float-float, rounded once
+      float t, e;
+      two_sum(__ldg(bh + 3 * v + k), -h[k], t, e);
+      const float q = pin ? 0.f : __fadd_rn(t, __fadd_rn(e, __fsub_rn(__ldg(bl + 3 * v + k), l[k])));
+      r[3 * v + k] = q;
+      acc += q * q;
+    }
   }
   BT_ROW_LOOP_END
-  double s = cta_sum(acc);
+  double s = cta_sum_f(acc);
   if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
 
@@ -821,17 +835,17 @@ k_pcg_update_f(int n, const float *__restrict__ pa, const float *__restrict__ pb
   }
 }
 
-// start of an inner solve with the factor preconditioner: x = 0, r = (float) r64;
+// start of an inner solve with the factor preconditioner: x = 0, r = rres;
 // r.r and the tolerance. A fresh solve (cont = 0) clears p and the iteration
 // count (r.z = 1 stands for the previous r.z; beta multiplies p = 0); a
 // continued one keeps p, the iteration count and r_k.z_k, so the following
 // k_pcg_prec_lower takes beta = r'.z' / r_k.z_k against the replaced residual.
-__global__ void k_pcg_init_f(int n, const double *__restrict__ r64, float *__restrict__ x, float *__restrict__ r,
+__global__ void k_pcg_init_f(int n, const float *__restrict__ rres, float *__restrict__ x, float *__restrict__ r,
                              float *__restrict__ p0, float *__restrict__ p1, double *__restrict__ part,
                              PcgState *__restrict__ st, double inner_rel2, double abs_tol2, int max_it, int cont) {
   float arr = 0.f;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const float rv = (float)r64[i];
+    const float rv = rres[i];
     x[i] = 0.f;
     r[i] = rv;
     if (!cont) {
@@ -877,8 +891,9 @@ struct PcgOperator {
 };
 
 struct PcgWork {
-  float *x, *r, *z, *pa, *pb, *ap, *minv, *xh, *xl;
-  double *r64, *part_a, *part_b;
+  float *x, *r, *z, *pa, *pb, *ap, *minv, *xh, *xl, *bh, *bl;
+  float *rres;  // the refinement residual b - A x (FP32)
+  double *part_a, *part_b;
   PcgState *st;
 };
 
@@ -970,8 +985,8 @@ static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double
     return o;
   };
   const size_t o_x = take(4ull * n), o_r = take(4ull * n), o_z = take(4ull * n), o_pa = take(4ull * n),
-               o_pb = take(4ull * n), o_ap = take(4ull * n), o_minv = take(24ull * nb), o_r64 = take(8ull * n),
-               o_xh = take(4ull * n), o_xl = take(4ull * n),
+               o_pb = take(4ull * n), o_ap = take(4ull * n), o_minv = take(24ull * nb), o_rres = take(4ull * n),
+               o_xh = take(4ull * n), o_xl = take(4ull * n), o_bh = take(4ull * n), o_bl = take(4ull * n),
                o_pa8 = take(8ull * nparts), o_pb8 = take(8ull * nparts), o_st = take(sizeof(PcgState));
   BT_CHECK(wbuf.ensure(off));
   char *base = wbuf.as<char>();
@@ -983,7 +998,9 @@ static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double
   w.pb = (float *)(base + o_pb);
   w.ap = (float *)(base + o_ap);
   w.minv = (float *)(base + o_minv);
-  w.r64 = (double *)(base + o_r64);
+  w.rres = (float *)(base + o_rres);
+  w.bh = (float *)(base + o_bh);
+  w.bl = (float *)(base + o_bl);
   w.xh = (float *)(base + o_xh);
   w.xl = (float *)(base + o_xl);
   w.part_a = (double *)(base + o_pa8);
@@ -1033,13 +1050,16 @@ static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double
   double rel = 0.0;
   PcgState hs{};
   for (int pass = 0; pass <= prm.max_refinements; ++pass) {
-    // r64 = b - A x (FP64)
+    // rres = b - A x (float-float on the block layout, FP64 on a CSR)
     if (blk) {
-      if (pass == 0) BT_LAUNCH(ctx, k_axpy64, grid_vec(ctx, n), 256, 0, n, nullptr, x, w.xh, w.xl);
+      if (pass == 0) {
+        BT_LAUNCH(ctx, k_axpy64, grid_vec(ctx, n), 256, 0, n, nullptr, x, w.xh, w.xl);
+        BT_LAUNCH(ctx, k_split64, grid_vec(ctx, n), 256, 0, n, b, w.bh, w.bl);
+      }
       BT_LAUNCH(ctx, k_resid_blk_ff<16>, gs, 256, 0, op.plan->nV, op.plan->brp, op.plan->bcol, op.values, w.xh, w.xl,
-                b, w.r64, op.pinned, w.part_a);
+                w.bh, w.bl, w.rres, op.pinned, w.part_a);
     } else {
-      BT_LAUNCH(ctx, k_resid_csr64, gs, 256, 0, n, op.rp, op.ci, op.values, op.values64, x, b, w.r64, w.part_a);
+      BT_LAUNCH(ctx, k_resid_csr64, gs, 256, 0, n, op.rp, op.ci, op.values, op.values64, x, b, w.rres, w.part_a);
     }
     BT_CHECK(reduce_sum(ctx, w.part_a, gs, &w.st->rr));
     double rr = 0.0;
@@ -1060,17 +1080,17 @@ static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double
       break;
     }
     rep->refinements = pass + 1;
-    // inner FP32 PCG on r64: a fresh solve in the first pass, later passes
+    // inner FP32 PCG on rres: a fresh solve in the first pass, later passes
     // continue the direction against the replaced residual unless restart is set
     const double abs2 = (0.5 * target) * (0.5 * target);
     const int cont = (pass > 0 && !prm.restart) ? 1 : 0;
     const int it0 = cont ? hs.it : 0;
     if (op.gl) {
-      BT_LAUNCH(ctx, k_pcg_init_f, gv, 256, 0, n, w.r64, w.x, w.r, w.pa, w.pb, w.part_a, w.st,
+      BT_LAUNCH(ctx, k_pcg_init_f, gv, 256, 0, n, w.rres, w.x, w.r, w.pa, w.pb, w.part_a, w.st,
                 prm.inner_rel_tol * prm.inner_rel_tol, abs2, prm.max_iters - rep->iterations, cont);
       BT_CHECK(pcg_enqueue_prec(ctx, op, w));
     } else {
-      BT_LAUNCH(ctx, k_pcg_init, gv, 256, 0, nb, n, w.r64, w.minv, w.x, w.r, w.z, w.pa, w.pb, w.part_a, w.part_b,
+      BT_LAUNCH(ctx, k_pcg_init, gv, 256, 0, nb, n, w.rres, w.minv, w.x, w.r, w.z, w.pa, w.pb, w.part_a, w.part_b,
                 w.st, prm.inner_rel_tol * prm.inner_rel_tol, abs2, prm.max_iters - rep->iterations, cont);
     }
     for (;;) {
