@@ -155,8 +155,6 @@ namespace bartels {
 constexpr int kChunkFloats = 16384;  // 64 KB of shared memory per assembly CTA
 constexpr int kChunkMaxVerts = 128;
 
-// value offset of block row v (first value of row 3v)
-__host__ __device__ inline int64_t row_value_base(const int *brp, int v) { return 9ll * brp[v]; }
 
 // Kernel-side entry points implemented in the .cu files.
 int plan_build(bartels_mesh_plan plan, const double *V_host, const int *E_host);

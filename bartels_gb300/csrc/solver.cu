@@ -69,46 +69,10 @@ __device__ __forceinline__ double cta_sum(double v) {
   return s;
 }
 
-// every block: deterministic sum of n partials, broadcast to all threads
-__device__ __forceinline__ double cta_sum_array(const double *__restrict__ a, int n) {
-  __shared__ double bcast;
-  double acc = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) acc += a[i];
-  double s = cta_sum(acc);
-  if (threadIdx.x == 0) bcast = s;
-  __syncthreads();
-  s = bcast;
-  __syncthreads();
-  return s;
-}
-
 // ------------------------------------------------------------------ SpMV ---
-// generic scalar CSR (drop-in search direction): one warp per row
-template <bool DOT>
-__global__ void __launch_bounds__(256)
-k_spmv_csr(int n, const int *__restrict__ rp, const int *__restrict__ ci, const float *__restrict__ val,
-           const float *__restrict__ x, float *__restrict__ y, double *__restrict__ partial,
-           const PcgState *__restrict__ st) {
-  if (st && st->done) return;
-  const int lane = threadIdx.x & 31;
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  double acc = 0.0;
-  for (int i = warp; i < n; i += nwarps) {
-    float s = 0.f;
-    for (int k = rp[i] + lane; k < rp[i + 1]; k += 32) s += val[k] * __ldg(x + ci[k]);
-    s = warp_sumf(s);
-    if (lane == 0) {
-      y[i] = s;
-      if (DOT) acc += (double)(x[i] * s);
-    }
-  }
-  if (DOT) {
-    double s = cta_sum(acc);
-    if (threadIdx.x == 0) partial[blockIdx.x] = s;
-  }
-}
-
+// refinement residual r = b - A x of a generic scalar CSR (the drop-in search
+// direction): FP64 products (with the exact FP64 values when given), one warp
+// per row, rounded to the FP32 residual the inner solve takes; partial sums of r.r
 __global__ void __launch_bounds__(256)
 k_resid_csr64(int n, const int *__restrict__ rp, const int *__restrict__ ci, const float *__restrict__ val,
               const double *__restrict__ val64, const double *__restrict__ x, const double *__restrict__ b,
