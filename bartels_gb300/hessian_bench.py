@@ -7,9 +7,11 @@ States (seeded): "rest" (q = X: every element passes the exact PSD test),
 elements are projected) and "gravity_like" (a small sag in z plus vertex noise
 0.002 h: a fraction of the elements is projected). E = 2e6 Pa, nu = 0.45,
 simple_psd_fix tol 1e-6. Each line gives milliseconds per assembly (device
-time of `reps` back-to-back calls on the library's stream, CUDA events) and the
-compulsory-bytes rate: per-tet record (64 B) + per-vertex input (16 B) + the
-CSR values written (4 B each) + the incidence map (8 B per incidence).
+time of `reps` back-to-back calls on the library's stream, CUDA events) and two
+byte rates: compulsory (tet inputs 64 B + vertex positions 12 B + CSR values
+written 4 B each) and algorithmic (the traffic of the two-kernel formulation:
+element kernel 64 T + 12 V + 576 T written, reduction kernel 576 T read + 4 nnz
+written + 576 T of scatter map).
 """
 from __future__ import annotations
 
@@ -46,7 +48,8 @@ def main(argv=None):
     plan.set_element_data(params=material_params(args.model, len(E), 2e6, 0.45))
     model = bg.api.MODELS[args.model]
     nT, nV, nnz = len(E), len(V), plan.nnz
-    compulsory = 64 * nT + 16 * nV + 4 * nnz + 8 * 4 * nT
+    compulsory = 64 * nT + 12 * nV + 4 * nnz
+    algorithmic = 64 * nT + 12 * nV + 576 * nT + 576 * nT + 4 * nnz + 4 * 144 * nT
     # CUDA events on the library's own stream
     stream = torch.cuda.ExternalStream(int(L.bartels_ctx_stream(ctx.handle)), device=f"cuda:{ctx.device}")
     out = {}
@@ -66,8 +69,10 @@ def main(argv=None):
         b.record(stream)
         ctx.synchronize()
         ms = a.elapsed_time(b) / args.reps
-        out[name] = dict(ms=round(ms, 4), compulsory_gbs=round(compulsory / ms / 1e6, 1))
-    line = dict(n=args.n, model=args.model, tets=nT, vertices=nV, compulsory_bytes=compulsory, states=out)
+        out[name] = dict(ms=round(ms, 4), compulsory_gbs=round(compulsory / ms / 1e6, 1),
+                         algorithmic_gbs=round(algorithmic / ms / 1e6, 1))
+    line = dict(n=args.n, model=args.model, tets=nT, vertices=nV, compulsory_bytes=compulsory,
+                algorithmic_bytes=algorithmic, states=out)
     print(json.dumps(line), flush=True)
     plan.close()
     return line
