@@ -315,6 +315,163 @@ linear_tetmesh_linear_elasticity_q, linear_tetmesh_linear_elasticity_dq, linear_
     _make("linear_elasticity")
 
 
+# ------------------------------------------------------- 2D triangle meshes --
+class Tri2DPlan:
+    """A plan for a triangle mesh in the plane (bartels_tri2d_plan): the CSR
+    pattern with 2x2 vertex blocks and the incidence lists, from (nV, E)."""
+
+    def __init__(self, nV, E, ctx: Context | None = None):
+        self.ctx = ctx or Context.default()
+        self.E = np.ascontiguousarray(E, dtype=np.int32)
+        if self.E.ndim != 2 or self.E.shape[1] != 3:
+            raise BartelsError(_lib.E_INVALID_ARG, "Tri2DPlan", "E must be (nT,3)")
+        self.nV, self.nT = int(nV), len(self.E)
+        ecm = _colmajor(self.E, np.int32)
+        h = C.c_void_p()
+        check(lib().bartels_tri2d_plan_create(self.ctx.handle, self.nV, self.nT, _iptr(ecm), C.byref(h)),
+              "bartels_tri2d_plan_create")
+        self.handle = h
+        self.ctx._plans.add(self)
+        n = C.c_int()
+        nnz = C.c_int64()
+        check(lib().bartels_tri2d_plan_csr_size(h, C.byref(n), C.byref(nnz)), "bartels_tri2d_plan_csr_size")
+        self.n, self.nnz = n.value, nnz.value
+        rp = np.zeros(self.n + 1, np.int32)
+        ci = np.zeros(self.nnz, np.int32)
+        check(lib().bartels_tri2d_plan_csr_pattern(h, _iptr(rp), _iptr(ci)), "bartels_tri2d_plan_csr_pattern")
+        self._pattern = (rp, ci)
+
+    def pattern(self):
+        return self._pattern
+
+    def csr(self, values):
+        rp, ci = self._pattern
+        return sp.csr_matrix((values, ci.copy(), rp.copy()), shape=(self.n, self.n))
+
+    def _args(self, q, dphidX, area, params):
+        qa = _f64(np.ravel(q))
+        if qa.size != 2 * self.nV:
+            raise BartelsError(_lib.E_INVALID_ARG, "Tri2DPlan", "q must hold 2 nV values")
+        keep = [qa, _colmajor(np.asarray(dphidX, np.float64).reshape(self.nT, 6), np.float64),
+                _f64(np.ravel(area)), _colmajor(np.asarray(params, np.float64).reshape(self.nT, 2), np.float64)]
+        return keep, [_dptr(a) for a in keep]
+
+    def q(self, model, q, dphidX, area, params) -> float:
+        keep, (qp, d, a, p) = self._args(q, dphidX, area, params)
+        e = C.c_double()
+        check(lib().bartels_tri2dmesh_q(self.ctx.handle, self.handle, MODELS[model], qp, d, a, p, C.byref(e)),
+              "bartels_tri2dmesh_q")
+        return e.value
+
+    def dq(self, model, q, dphidX, area, params):
+        keep, (qp, d, a, p) = self._args(q, dphidX, area, params)
+        g = np.zeros(2 * self.nV)
+        check(lib().bartels_tri2dmesh_dq(self.ctx.handle, self.handle, MODELS[model], qp, d, a, p, _dptr(g)),
+              "bartels_tri2dmesh_dq")
+        return g
+
+    def dq2(self, model, q, dphidX, area, params, psd_tol=None):
+        keep, (qp, d, a, p) = self._args(q, dphidX, area, params)
+        vals = np.zeros(self.nnz)
+        psd = _lib.PSD_NONE if psd_tol is None else _lib.PSD_SIMPLE_FIX
+        check(lib().bartels_tri2dmesh_dq2(self.ctx.handle, self.handle, MODELS[model], qp, d, a, p, psd,
+                                          0.0 if psd_tol is None else float(psd_tol), _dptr(vals)),
+              "bartels_tri2dmesh_dq2")
+        return self.csr(vals)
+
+    def mass_matrix(self, density, area):
+        dens = _f64(np.broadcast_to(np.asarray(density, np.float64), (self.nT,)))
+        ar = _f64(np.ravel(area))
+        vals = np.zeros(self.nnz)
+        check(lib().bartels_tri2dmesh_mass_matrix(self.ctx.handle, self.handle, _dptr(dens), _dptr(ar), _dptr(vals)),
+              "bartels_tri2dmesh_mass_matrix")
+        return self.csr(vals)
+
+    def close(self):
+        if getattr(self, "handle", None) and getattr(self.ctx, "handle", None):
+            lib().bartels_tri2d_plan_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        if sys.is_finalizing():
+            return
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_tri_plans: "OrderedDict[str, Tri2DPlan]" = OrderedDict()
+
+
+def _tri_plan_for(V, E) -> Tri2DPlan:
+    E = np.ascontiguousarray(E, dtype=np.int32)
+    nV = len(V)
+    key = hashlib.sha1(str(nV).encode() + b"|" + E.tobytes()).hexdigest()
+    p = _tri_plans.get(key)
+    if p is None:
+        p = Tri2DPlan(nV, E)
+        _tri_plans[key] = p
+        while len(_tri_plans) > 4:
+            _tri_plans.popitem(last=False)[1].close()
+    else:
+        _tri_plans.move_to_end(key)
+    return p
+
+
+def _tri_geometry(V, E):
+    V = np.asarray(V, np.float64)
+    E = np.asarray(E, np.int32)
+    vcm = _colmajor(V, np.float64)
+    ecm = _colmajor(E, np.int32)
+    d = np.zeros(6 * len(E))
+    a = np.zeros(len(E))
+    check(lib().bartels_tri2dmesh_dphi_dX(Context.default().handle, len(V), _dptr(vcm), len(E), _iptr(ecm),
+                                          _dptr(d), _dptr(a)), "bartels_tri2dmesh_dphi_dX")
+    return d.reshape(6, len(E)).T.copy(), a
+
+
+def linear_tri2dmesh_dphi_dX(V, E):
+    """src/linear_tri2dmesh_dphi_dX.cpp:5-18 -> (nT, 6), the column-major flatten
+    of each 3x2 gradient matrix."""
+    return _tri_geometry(V, E)[0]
+
+
+def triangle_areas(V, E):
+    """Unsigned areas |det [x1 - x0, x2 - x0]| / 2 of a planar triangle mesh."""
+    return _tri_geometry(V, E)[1]
+
+
+def _make_tri(model):
+    def q_fn(V, E, q, dphidX, area, params):
+        return _tri_plan_for(V, E).q(model, q, dphidX, area, params)
+
+    def dq_fn(V, E, q, dphidX, area, params):
+        return _tri_plan_for(V, E).dq(model, q, dphidX, area, params)
+
+    def dq2_fn(V, E, q, dphidX, area, params, psd_tol=None):
+        return _tri_plan_for(V, E).dq2(model, q, dphidX, area, params, psd_tol)
+
+    q_fn.__name__ = f"linear_tri2dmesh_{model}_q"
+    dq_fn.__name__ = f"linear_tri2dmesh_{model}_dq"
+    dq2_fn.__name__ = f"linear_tri2dmesh_{model}_dq2"
+    return q_fn, dq_fn, dq2_fn
+
+
+linear_tri2dmesh_neohookean_q, linear_tri2dmesh_neohookean_dq, linear_tri2dmesh_neohookean_dq2 = \
+    _make_tri("neohookean")
+linear_tri2dmesh_stvk_q, linear_tri2dmesh_stvk_dq, linear_tri2dmesh_stvk_dq2 = _make_tri("stvk")
+linear_tri2dmesh_corotational_q, linear_tri2dmesh_corotational_dq, linear_tri2dmesh_corotational_dq2 = \
+    _make_tri("corotational")
+linear_tri2dmesh_arap_q, linear_tri2dmesh_arap_dq, linear_tri2dmesh_arap_dq2 = _make_tri("arap")
+linear_tri2dmesh_linear_elasticity_dq2 = _make_tri("linear_elasticity")[2]
+
+
+def linear_tri2dmesh_mass_matrix(V, E, density, area):
+    """src/linear_tri2dmesh_mass_matrix.cpp."""
+    return _tri_plan_for(V, E).mass_matrix(density, area)
+
+
 def linear_tetmesh_mass_matrix(V, E, density, volume):
     """src/linear_tetmesh_mass_matrix.cpp:7-24."""
     return _plan_for(V, E).mass_matrix(density, volume)
