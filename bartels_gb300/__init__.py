@@ -20,7 +20,9 @@ from .api import (Context, MeshPlan, newton_params, linear_tetmesh_dphi_dX, volu
                   linear_tri2dmesh_stvk_q, linear_tri2dmesh_stvk_dq, linear_tri2dmesh_stvk_dq2,
                   linear_tri2dmesh_corotational_q, linear_tri2dmesh_corotational_dq,
                   linear_tri2dmesh_corotational_dq2, linear_tri2dmesh_arap_q, linear_tri2dmesh_arap_dq,
-                  linear_tri2dmesh_arap_dq2, linear_tri2dmesh_linear_elasticity_dq2, linear_tri2dmesh_mass_matrix)
+                  linear_tri2dmesh_arap_dq2, linear_tri2dmesh_linear_elasticity_dq2, linear_tri2dmesh_mass_matrix,
+                  Tri3DPlan, linear_tri3dmesh_dphi_dX, triangle_areas_3d, triangle_normals,
+                  linear_tri3dmesh_stvk_dq2)
 from . import meshes
 
 __all__ = [n for n in dir() if not n.startswith("_")]

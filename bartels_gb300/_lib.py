@@ -113,15 +113,17 @@ SIGNATURES = [
     ("bartels_gemm_bf16_d", C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, C.c_int, _P, _P, C.c_int, _P, C.c_int]),
     ("bartels_newton_iterate_d", C.c_int,
      [_P, _P, C.POINTER(NewtonParams), _P, C.c_double, _I, C.POINTER(NewtonReport)]),
-    ("bartels_tri2d_plan_create", C.c_int, [_P, C.c_int, C.c_int, _I, C.POINTER(_P)]),
-    ("bartels_tri2d_plan_destroy", None, [_P]),
-    ("bartels_tri2d_plan_csr_size", C.c_int, [_P, _I, C.POINTER(C.c_int64)]),
-    ("bartels_tri2d_plan_csr_pattern", C.c_int, [_P, _I, _I]),
+    ("bartels_tri_plan_create", C.c_int, [_P, C.c_int, C.c_int, _I, C.c_int, C.POINTER(_P)]),
+    ("bartels_tri_plan_destroy", None, [_P]),
+    ("bartels_tri_plan_csr_size", C.c_int, [_P, _I, C.POINTER(C.c_int64)]),
+    ("bartels_tri_plan_csr_pattern", C.c_int, [_P, _I, _I]),
     ("bartels_tri2dmesh_dphi_dX", C.c_int, [_P, C.c_int, _D, C.c_int, _I, _D, _D]),
     ("bartels_tri2dmesh_q", C.c_int, [_P, _P, C.c_int, _D, _D, _D, _D, _D]),
     ("bartels_tri2dmesh_dq", C.c_int, [_P, _P, C.c_int, _D, _D, _D, _D, _D]),
     ("bartels_tri2dmesh_dq2", C.c_int, [_P, _P, C.c_int, _D, _D, _D, _D, C.c_int, C.c_double, _D]),
     ("bartels_tri2dmesh_mass_matrix", C.c_int, [_P, _P, _D, _D, _D]),
+    ("bartels_tri3dmesh_dphi_dX", C.c_int, [_P, C.c_int, _D, C.c_int, _I, _D, _D]),
+    ("bartels_tri3dmesh_stvk_dq2", C.c_int, [_P, _P, _D, _D, _D, _D, _D, _D, _D, C.c_int, C.c_double, _D]),
 ]
 
 _lib = None

@@ -317,8 +317,10 @@ linear_tetmesh_linear_elasticity_q, linear_tetmesh_linear_elasticity_dq, linear_
 
 # ------------------------------------------------------- 2D triangle meshes --
 class Tri2DPlan:
-    """A plan for a triangle mesh in the plane (bartels_tri2d_plan): the CSR
-    pattern with 2x2 vertex blocks and the incidence lists, from (nV, E)."""
+    """A plan for a triangle mesh in the plane (bartels_tri_plan, 2 DOFs per
+    vertex): the CSR pattern with 2x2 vertex blocks and the incidence lists."""
+
+    DIM = 2
 
     def __init__(self, nV, E, ctx: Context | None = None):
         self.ctx = ctx or Context.default()
@@ -328,17 +330,17 @@ class Tri2DPlan:
         self.nV, self.nT = int(nV), len(self.E)
         ecm = _colmajor(self.E, np.int32)
         h = C.c_void_p()
-        check(lib().bartels_tri2d_plan_create(self.ctx.handle, self.nV, self.nT, _iptr(ecm), C.byref(h)),
-              "bartels_tri2d_plan_create")
+        check(lib().bartels_tri_plan_create(self.ctx.handle, self.nV, self.nT, _iptr(ecm), self.DIM, C.byref(h)),
+              "bartels_tri_plan_create")
         self.handle = h
         self.ctx._plans.add(self)
         n = C.c_int()
         nnz = C.c_int64()
-        check(lib().bartels_tri2d_plan_csr_size(h, C.byref(n), C.byref(nnz)), "bartels_tri2d_plan_csr_size")
+        check(lib().bartels_tri_plan_csr_size(h, C.byref(n), C.byref(nnz)), "bartels_tri_plan_csr_size")
         self.n, self.nnz = n.value, nnz.value
         rp = np.zeros(self.n + 1, np.int32)
         ci = np.zeros(self.nnz, np.int32)
-        check(lib().bartels_tri2d_plan_csr_pattern(h, _iptr(rp), _iptr(ci)), "bartels_tri2d_plan_csr_pattern")
+        check(lib().bartels_tri_plan_csr_pattern(h, _iptr(rp), _iptr(ci)), "bartels_tri_plan_csr_pattern")
         self._pattern = (rp, ci)
 
     def pattern(self):
@@ -389,7 +391,7 @@ class Tri2DPlan:
 
     def close(self):
         if getattr(self, "handle", None) and getattr(self.ctx, "handle", None):
-            lib().bartels_tri2d_plan_destroy(self.handle)
+            lib().bartels_tri_plan_destroy(self.handle)
         self.handle = None
 
     def __del__(self):
@@ -470,6 +472,101 @@ linear_tri2dmesh_linear_elasticity_dq2 = _make_tri("linear_elasticity")[2]
 def linear_tri2dmesh_mass_matrix(V, E, density, area):
     """src/linear_tri2dmesh_mass_matrix.cpp."""
     return _tri_plan_for(V, E).mass_matrix(density, area)
+
+
+# ---------------------------------------------------- triangles in space (3D) --
+class Tri3DPlan(Tri2DPlan):
+    """A plan for a triangle mesh in space (bartels_tri_plan, 3 DOFs per vertex)."""
+
+    DIM = 3
+
+    def stvk_dq2(self, q, dphidX, N, n, dndq, area, params, psd_tol=None):
+        """linear_tri3dmesh_stvk_dq2: q (3 nV), dphidX (nT, 9), N and n (nT, 3),
+        dndq (nT, 27), area (nT), params (nT, 2) = (lambda, mu)."""
+        nT = self.nT
+        keep = [_f64(np.ravel(q)), _colmajor(np.asarray(dphidX, np.float64).reshape(nT, 9), np.float64),
+                _colmajor(np.asarray(N, np.float64).reshape(nT, 3), np.float64),
+                _colmajor(np.asarray(n, np.float64).reshape(nT, 3), np.float64),
+                _colmajor(np.asarray(dndq, np.float64).reshape(nT, 27), np.float64), _f64(np.ravel(area)),
+                _colmajor(np.asarray(params, np.float64).reshape(nT, 2), np.float64)]
+        if keep[0].size != 3 * self.nV:
+            raise BartelsError(_lib.E_INVALID_ARG, "Tri3DPlan", "q must hold 3 nV values")
+        vals = np.zeros(self.nnz)
+        psd = _lib.PSD_NONE if psd_tol is None else _lib.PSD_SIMPLE_FIX
+        check(lib().bartels_tri3dmesh_stvk_dq2(self.ctx.handle, self.handle, *[_dptr(a) for a in keep], psd,
+                                               0.0 if psd_tol is None else float(psd_tol), _dptr(vals)),
+              "bartels_tri3dmesh_stvk_dq2")
+        return self.csr(vals)
+
+
+_tri3_plans: "OrderedDict[str, Tri3DPlan]" = OrderedDict()
+
+
+def _tri3_plan_for(V, E) -> Tri3DPlan:
+    E = np.ascontiguousarray(E, dtype=np.int32)
+    nV = len(V)
+    key = hashlib.sha1(str(nV).encode() + b"|" + E.tobytes()).hexdigest()
+    p = _tri3_plans.get(key)
+    if p is None:
+        p = Tri3DPlan(nV, E)
+        _tri3_plans[key] = p
+        while len(_tri3_plans) > 4:
+            _tri3_plans.popitem(last=False)[1].close()
+    else:
+        _tri3_plans.move_to_end(key)
+    return p
+
+
+def _tri3_geometry(V, E):
+    V = np.asarray(V, np.float64)
+    E = np.asarray(E, np.int32)
+    vcm = _colmajor(V, np.float64)
+    ecm = _colmajor(E, np.int32)
+    d = np.zeros(9 * len(E))
+    a = np.zeros(len(E))
+    check(lib().bartels_tri3dmesh_dphi_dX(Context.default().handle, len(V), _dptr(vcm), len(E), _iptr(ecm),
+                                          _dptr(d), _dptr(a)), "bartels_tri3dmesh_dphi_dX")
+    return d.reshape(9, len(E)).T.copy(), a
+
+
+def linear_tri3dmesh_dphi_dX(V, E):
+    """src/linear_tri3dmesh_dphi_dX.cpp -> (nT, 9), the column-major flatten of each 3x3."""
+    return _tri3_geometry(V, E)[0]
+
+
+def triangle_areas_3d(V, E):
+    """|e1 x e2| / 2 of the triangles of a mesh in space."""
+    return _tri3_geometry(V, E)[1]
+
+
+def triangle_normals(x, E):
+    """Unit normals n = (x1 - x0) x (x2 - x0) / |.| of the triangles at positions x
+    (nV x 3) and their derivatives with respect to the element DOFs [x0 x1 x2]:
+    (n (nT, 3), dndq (nT, 27) as the column-major flatten of the 3x9 Jacobian),
+    the per-element inputs of linear_tri3dmesh_stvk_dq2."""
+    x = np.asarray(x, np.float64).reshape(-1, 3)
+    E = np.asarray(E)
+    e1, e2 = x[E[:, 1]] - x[E[:, 0]], x[E[:, 2]] - x[E[:, 0]]
+    c = np.cross(e1, e2)
+    r = np.linalg.norm(c, axis=1)
+    n = c / r[:, None]
+
+    def skew(v):
+        z = np.zeros(len(v))
+        return np.stack([np.stack([z, -v[:, 2], v[:, 1]], 1), np.stack([v[:, 2], z, -v[:, 0]], 1),
+                         np.stack([-v[:, 1], v[:, 0], z], 1)], 1)
+    P = (np.eye(3)[None] - n[:, :, None] * n[:, None, :]) / r[:, None, None]  # dn/dc
+    dc1, dc2 = -skew(e2), skew(e1)  # dc/de1 = -[e2]x, dc/de2 = [e1]x
+    J = np.zeros((len(E), 3, 9))
+    J[:, :, 3:6] = P @ dc1
+    J[:, :, 6:9] = P @ dc2
+    J[:, :, 0:3] = -(J[:, :, 3:6] + J[:, :, 6:9])
+    return n, J.transpose(0, 2, 1).reshape(len(E), 27)
+
+
+def linear_tri3dmesh_stvk_dq2(V, E, q, dphidX, N, n, dndq, area, params, psd_tol=None):
+    """src/linear_tri3dmesh_stvk_dq2.cpp: StVK membrane Hessian (scipy CSR)."""
+    return _tri3_plan_for(V, E).stvk_dq2(q, dphidX, N, n, dndq, area, params, psd_tol)
 
 
 def linear_tetmesh_mass_matrix(V, E, density, volume):

@@ -426,15 +426,17 @@ int bartels_tetmesh_dq_noalloc_d(bartels_ctx ctx, bartels_mesh_plan plan, int mo
  * conventions: Neo-Hookean (C, D), StVK and corotational (lambda, mu), ARAP
  * column 0 = k, linear elasticity (Young's modulus, Poisson ratio)). The 2D
  * deformation gradient is embedded in 3D with F33 = 1, as the reference does.
- * The plan holds the CSR pattern (2x2 vertex blocks; rows 2v, 2v+1 with the
- * sorted columns of v's neighbours, as the reference's assemble); all
+ * The plan holds the CSR pattern (dim x dim vertex blocks; rows dim v .. dim v +
+ * dim - 1 with the sorted columns of v's neighbours, as the reference's assemble); all
  * arithmetic is FP64 and every entry is summed over its triangles in triangle
  * order. */
-typedef struct bartels_tri2d_plan_s *bartels_tri2d_plan;
-int bartels_tri2d_plan_create(bartels_ctx ctx, int nV, int nT, const int *E, bartels_tri2d_plan *plan);
-void bartels_tri2d_plan_destroy(bartels_tri2d_plan plan);
-int bartels_tri2d_plan_csr_size(bartels_tri2d_plan plan, int *n, int64_t *nnz);
-int bartels_tri2d_plan_csr_pattern(bartels_tri2d_plan plan, int *row_ptr, int *col_idx);
+typedef struct bartels_tri_plan_s *bartels_tri_plan;
+/* dim: DOFs per vertex, 2 for the linear_tri2dmesh_* functions, 3 for
+ * linear_tri3dmesh_* (triangles in space). */
+int bartels_tri_plan_create(bartels_ctx ctx, int nV, int nT, const int *E, int dim, bartels_tri_plan *plan);
+void bartels_tri_plan_destroy(bartels_tri_plan plan);
+int bartels_tri_plan_csr_size(bartels_tri_plan plan, int *n, int64_t *nnz);
+int bartels_tri_plan_csr_pattern(bartels_tri_plan plan, int *row_ptr, int *col_idx);
 /* linear_tri2dmesh_dphi_dX (src/linear_tri2dmesh_dphi_dX.cpp:5-18,
  * src/linear_tri2d_dphi_dX.cpp:10-16); V nV x 2 column-major; area (optional)
  * = |det| / 2 of the edge matrix. */
@@ -445,51 +447,68 @@ int bartels_tri2dmesh_dphi_dX(bartels_ctx ctx, int nV, const double *V, int nT, 
  * BARTELS_LINEAR_ELASTICITY, src/linear_tri2d_linear_elasticity_dq2.cpp:9-44).
  * psd_mode BARTELS_PSD_SIMPLE_FIX applies simple_psd_fix (src/simple_psd_fix.cpp:5-21)
  * to each 6x6 element matrix. */
-int bartels_tri2dmesh_q(bartels_ctx ctx, bartels_tri2d_plan plan, int model, const double *q, const double *dphidX,
+int bartels_tri2dmesh_q(bartels_ctx ctx, bartels_tri_plan plan, int model, const double *q, const double *dphidX,
                         const double *area, const double *params, double *energy);
-int bartels_tri2dmesh_dq(bartels_ctx ctx, bartels_tri2d_plan plan, int model, const double *q, const double *dphidX,
+int bartels_tri2dmesh_dq(bartels_ctx ctx, bartels_tri_plan plan, int model, const double *q, const double *dphidX,
                          const double *area, const double *params, double *g);
-int bartels_tri2dmesh_dq2(bartels_ctx ctx, bartels_tri2d_plan plan, int model, const double *q, const double *dphidX,
+int bartels_tri2dmesh_dq2(bartels_ctx ctx, bartels_tri_plan plan, int model, const double *q, const double *dphidX,
                           const double *area, const double *params, int psd_mode, double psd_tol,
                           double *csr_values);
 /* linear_tri2dmesh_mass_matrix (src/linear_tri2dmesh_mass_matrix.cpp,
  * src/linear_tri2d_mass_matrix.cpp:10-32): density * area * (1/6, 1/12) x I2. */
-int bartels_tri2dmesh_mass_matrix(bartels_ctx ctx, bartels_tri2d_plan plan, const double *density,
+int bartels_tri2dmesh_mass_matrix(bartels_ctx ctx, bartels_tri_plan plan, const double *density,
                                   const double *area, double *csr_values);
 /* Named drop-ins: bartels_tri2dmesh_{neohookean,stvk,corotational,arap}_{q,dq,dq2}
  * (src/linear_tri2dmesh_<model>_{q,dq,dq2}.cpp) and
  * bartels_tri2dmesh_linear_elasticity_dq2. */
-int bartels_tri2dmesh_neohookean_q(bartels_ctx ctx, bartels_tri2d_plan plan, const double *q, const double *dphidX,
+int bartels_tri2dmesh_neohookean_q(bartels_ctx ctx, bartels_tri_plan plan, const double *q, const double *dphidX,
                                    const double *area, const double *params, double *energy);
-int bartels_tri2dmesh_neohookean_dq(bartels_ctx ctx, bartels_tri2d_plan plan, const double *q, const double *dphidX,
+int bartels_tri2dmesh_neohookean_dq(bartels_ctx ctx, bartels_tri_plan plan, const double *q, const double *dphidX,
                                     const double *area, const double *params, double *g);
-int bartels_tri2dmesh_neohookean_dq2(bartels_ctx ctx, bartels_tri2d_plan plan, const double *q, const double *dphidX,
+int bartels_tri2dmesh_neohookean_dq2(bartels_ctx ctx, bartels_tri_plan plan, const double *q, const double *dphidX,
                                      const double *area, const double *params, int psd_mode, double psd_tol,
                                      double *csr_values);
-int bartels_tri2dmesh_stvk_q(bartels_ctx ctx, bartels_tri2d_plan plan, const double *q, const double *dphidX,
+int bartels_tri2dmesh_stvk_q(bartels_ctx ctx, bartels_tri_plan plan, const double *q, const double *dphidX,
                              const double *area, const double *params, double *energy);
-int bartels_tri2dmesh_stvk_dq(bartels_ctx ctx, bartels_tri2d_plan plan, const double *q, const double *dphidX,
+int bartels_tri2dmesh_stvk_dq(bartels_ctx ctx, bartels_tri_plan plan, const double *q, const double *dphidX,
                               const double *area, const double *params, double *g);
-int bartels_tri2dmesh_stvk_dq2(bartels_ctx ctx, bartels_tri2d_plan plan, const double *q, const double *dphidX,
+int bartels_tri2dmesh_stvk_dq2(bartels_ctx ctx, bartels_tri_plan plan, const double *q, const double *dphidX,
                                const double *area, const double *params, int psd_mode, double psd_tol,
                                double *csr_values);
-int bartels_tri2dmesh_corotational_q(bartels_ctx ctx, bartels_tri2d_plan plan, const double *q, const double *dphidX,
+int bartels_tri2dmesh_corotational_q(bartels_ctx ctx, bartels_tri_plan plan, const double *q, const double *dphidX,
                                      const double *area, const double *params, double *energy);
-int bartels_tri2dmesh_corotational_dq(bartels_ctx ctx, bartels_tri2d_plan plan, const double *q, const double *dphidX,
+int bartels_tri2dmesh_corotational_dq(bartels_ctx ctx, bartels_tri_plan plan, const double *q, const double *dphidX,
                                       const double *area, const double *params, double *g);
-int bartels_tri2dmesh_corotational_dq2(bartels_ctx ctx, bartels_tri2d_plan plan, const double *q, const double *dphidX,
+int bartels_tri2dmesh_corotational_dq2(bartels_ctx ctx, bartels_tri_plan plan, const double *q, const double *dphidX,
                                        const double *area, const double *params, int psd_mode, double psd_tol,
                                        double *csr_values);
-int bartels_tri2dmesh_arap_q(bartels_ctx ctx, bartels_tri2d_plan plan, const double *q, const double *dphidX,
+int bartels_tri2dmesh_arap_q(bartels_ctx ctx, bartels_tri_plan plan, const double *q, const double *dphidX,
                              const double *area, const double *params, double *energy);
-int bartels_tri2dmesh_arap_dq(bartels_ctx ctx, bartels_tri2d_plan plan, const double *q, const double *dphidX,
+int bartels_tri2dmesh_arap_dq(bartels_ctx ctx, bartels_tri_plan plan, const double *q, const double *dphidX,
                               const double *area, const double *params, double *g);
-int bartels_tri2dmesh_arap_dq2(bartels_ctx ctx, bartels_tri2d_plan plan, const double *q, const double *dphidX,
+int bartels_tri2dmesh_arap_dq2(bartels_ctx ctx, bartels_tri_plan plan, const double *q, const double *dphidX,
                                const double *area, const double *params, int psd_mode, double psd_tol,
                                double *csr_values);
-int bartels_tri2dmesh_linear_elasticity_dq2(bartels_ctx ctx, bartels_tri2d_plan plan, const double *q,
+int bartels_tri2dmesh_linear_elasticity_dq2(bartels_ctx ctx, bartels_tri_plan plan, const double *q,
                                             const double *dphidX, const double *area, const double *params,
                                             int psd_mode, double psd_tol, double *csr_values);
+
+/* ------------------------------------------------- triangles in space (3D) -- */
+/* linear_tri3dmesh_dphi_dX (src/linear_tri3dmesh_dphi_dX.cpp,
+ * src/linear_tri3d_dphi_dX.cpp:10-16): V nV x 3 column-major; dphidX nT x 9, the
+ * column-major flatten of each 3x3 (rows 1, 2 = (T^T T)^-1 T^T, row 0 = minus
+ * their sum); area (optional) = |e1 x e2| / 2. */
+int bartels_tri3dmesh_dphi_dX(bartels_ctx ctx, int nV, const double *V, int nT, const int *E, double *dphidX,
+                              double *area);
+/* linear_tri3dmesh_stvk_dq2 (src/linear_tri3dmesh_stvk_dq2.cpp,
+ * src/linear_tri3d_stvk_dq2.cpp:15-42): StVK membrane Hessian of a triangle mesh
+ * in space, 3 DOFs per vertex (plan created with dim 3); per element the rest
+ * normal N (nT x 3), the deformed normal n (nT x 3) and its derivative dndq
+ * (nT x 27, the column-major flatten of dn/dqe 3x9), params (lambda, mu)
+ * nT x 2; optional simple_psd_fix on each 9x9 element matrix. FP64. */
+int bartels_tri3dmesh_stvk_dq2(bartels_ctx ctx, bartels_tri_plan plan, const double *q, const double *dphidX,
+                               const double *N, const double *n, const double *dndq, const double *area,
+                               const double *params, int psd_mode, double psd_tol, double *csr_values);
 
 #ifdef __cplusplus
 }

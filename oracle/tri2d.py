@@ -177,3 +177,64 @@ def square_mesh(n, seed=0, jitter=0.0):
             else:
                 E += [[a, b, c], [b, d, c]]
     return V, np.array(E, np.int32)
+
+
+# ------------------------------------------------------------ triangles in space
+def dphi_dX_3d(V, E):
+    """src/linear_tri3d_dphi_dX.cpp:10-16: T = [x1-x0, x2-x0] (3x2), rows 1, 2 =
+    (T^T T)^-1 T^T, row 0 = -(row 1 + row 2); (nT, 9) column-major flatten of 3x3."""
+    V = np.asarray(V, np.float64)
+    out = np.zeros((len(E), 9))
+    for t, e in enumerate(np.asarray(E)):
+        Tm = np.stack([V[e[1]] - V[e[0]], V[e[2]] - V[e[0]]], axis=1)
+        d = np.zeros((3, 3))
+        d[1:] = np.linalg.inv(Tm.T @ Tm) @ Tm.T
+        d[0] = -d[1:].sum(axis=0)
+        out[t] = d.ravel(order="F")
+    return out
+
+
+def area_3d(V, E):
+    V = np.asarray(V, np.float64)
+    E = np.asarray(E)
+    return 0.5 * np.linalg.norm(np.cross(V[E[:, 1]] - V[E[:, 0]], V[E[:, 2]] - V[E[:, 0]]), axis=1)
+
+
+def stvk_hessian_3d_elements(E, q, dphidX, N, n, dndq, area_, params, psd_tol=None):
+    """src/linear_tri3d_stvk_dq2.cpp:15-42, literally: B = flatten_multiply_right(dphidX)
+    + flatten_multiply_right(N) unflatten<3,9>(dndq), F = unflatten(B qe + vec(n N)),
+    K = B^T d2psi_stvk(F) B * area."""
+    q = np.asarray(q, np.float64)
+    out = []
+    for t, e in enumerate(np.asarray(E)):
+        qe = np.concatenate([q[3 * v:3 * v + 3] for v in e])
+        M = np.asarray(dphidX[t]).reshape(3, 3, order="F")
+        Na = np.asarray(N[t]).reshape(1, 3)
+        fmr_N = np.kron(Na.reshape(3, 1), np.eye(3))  # vec(y Na) = fmr_N y
+        B = np.kron(M.T, np.eye(3)) + fmr_N @ np.asarray(dndq[t]).reshape(3, 9, order="F")
+        F = (B @ qe + fmr_N @ np.asarray(n[t])).reshape(3, 3, order="F")
+        K = B.T @ O.d2psi("stvk", F, params[t]) @ B * area_[t]
+        if psd_tol is not None:
+            K = O.psd_fix(K, psd_tol)
+        out.append(K)
+    return np.array(out)
+
+
+def assemble_3(nV, E, Ke):
+    """src/assemble.cpp:57-94 with 3 DOFs per vertex."""
+    rows, cols, vals = [], [], []
+    for t, e in enumerate(np.asarray(E)):
+        dof = np.array([[3 * v, 3 * v + 1, 3 * v + 2] for v in e]).ravel()
+        for c in range(9):
+            for r in range(9):
+                rows.append(dof[r])
+                cols.append(dof[c])
+                vals.append(Ke[t][r, c])
+    H = sp.coo_matrix((vals, (rows, cols)), shape=(3 * nV, 3 * nV)).tocsr()
+    H.sum_duplicates()
+    H.sort_indices()
+    return H
+
+
+def stvk_hessian_3d(nV, E, q, dphidX, N, n, dndq, area_, params, psd_tol=None):
+    return assemble_3(nV, E, stvk_hessian_3d_elements(E, q, dphidX, N, n, dndq, area_, params, psd_tol))

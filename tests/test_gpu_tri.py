@@ -1,4 +1,4 @@
-"""Planar triangle meshes on the GPU (linear_tri2dmesh_*) against the FP64 CPU
+"""Triangle meshes on the GPU (linear_tri2dmesh_*, linear_tri3dmesh_*) against the FP64 CPU
 restatement (oracle/tri2d.py): shape gradients and areas, energy, gradient,
 Hessian (pattern bit-exact, values with and without simple_psd_fix), linear
 elasticity, the mass matrix, the named drop-ins and the reference's 2D case."""
@@ -97,3 +97,51 @@ def test_reference_2d_case_has_zero_gradient_at_rest():
     d = bg.linear_tri2dmesh_dphi_dX(V, E)
     g = bg.linear_tri2dmesh_corotational_dq(V, E, V.ravel(), d, np.array([68.002]), params)
     assert np.abs(g).max() <= 1e-6 * params.max()
+
+
+# ---------------------------------------------------------- triangles in space
+def curved_sheet(n=5, seed=6):
+    V2, E = T.square_mesh(n, seed=seed, jitter=0.2)
+    V = np.c_[V2, 0.2 * np.sin(2.0 * V2[:, 0]) * np.cos(1.5 * V2[:, 1])]
+    rng = np.random.default_rng(seed)
+    Rz = np.array([[0.96, -0.28, 0.0], [0.28, 0.96, 0.0], [0.0, 0.0, 1.0]])
+    x = V @ Rz.T * np.array([1.1, 0.9, 1.0]) + 0.03 / n * rng.uniform(-1, 1, V.shape)
+    return V, E, x
+
+
+def test_tri3d_dphi_and_area():
+    V, E, _ = curved_sheet()
+    d = bg.linear_tri3dmesh_dphi_dX(V, E)
+    d_ref = T.dphi_dX_3d(V, E)
+    assert np.abs(d - d_ref).max() <= 1e-10 * np.abs(d_ref).max()
+    assert np.allclose(bg.triangle_areas_3d(V, E), T.area_3d(V, E), rtol=1e-13, atol=0)
+
+
+@pytest.mark.parametrize("psd_tol", [None, 1e-6, 1e3])
+def test_tri3d_stvk_hessian(psd_tol):
+    V, E, x = curved_sheet()
+    d, ar = T.dphi_dX_3d(V, E), T.area_3d(V, E)
+    p = material_params("stvk", len(E), 2e6, 0.45)
+    N, _ = bg.triangle_normals(V, E)
+    for name, pos in (("rest", V), ("deformed", x)):
+        n, dndq = bg.triangle_normals(pos, E)
+        H = bg.linear_tri3dmesh_stvk_dq2(V, E, pos.ravel(), d, N, n, dndq, ar, p, psd_tol=psd_tol)
+        H_ref = T.stvk_hessian_3d(len(V), E, pos.ravel(), d, N, n, dndq, ar, p, psd_tol)
+        assert same_pattern(H, H_ref), name
+        assert rel_max(H, H_ref) <= 1e-10, (name, rel_max(H, H_ref))
+
+
+def test_flat_membrane_matches_planar_stvk_on_the_gpu():
+    V2, E = T.square_mesh(4, seed=4, jitter=0.2)
+    V3 = np.c_[V2, np.zeros(len(V2))]
+    x2 = V2 @ np.array([[1.1, 0.15], [-0.05, 0.95]]).T
+    x3 = np.c_[x2, np.zeros(len(V2))]
+    p = material_params("stvk", len(E), 1e5, 0.3)
+    N, _ = bg.triangle_normals(V3, E)
+    n, dndq = bg.triangle_normals(x3, E)
+    H3 = bg.linear_tri3dmesh_stvk_dq2(V3, E, x3.ravel(), bg.linear_tri3dmesh_dphi_dX(V3, E), N, n, dndq,
+                                      bg.triangle_areas_3d(V3, E), p).toarray()
+    H2 = bg.linear_tri2dmesh_stvk_dq2(V2, E, x2.ravel(), bg.linear_tri2dmesh_dphi_dX(V2, E),
+                                      bg.triangle_areas(V2, E), p).toarray()
+    inplane = np.array([3 * v + k for v in range(len(V2)) for k in range(2)])
+    assert np.abs(H3[np.ix_(inplane, inplane)] - H2).max() <= 1e-9 * np.abs(H2).max()

@@ -87,3 +87,23 @@ def test_mass_matrix_total_mass():
     # each translation direction carries the total mass
     ux = np.tile([1.0, 0.0], len(V))
     assert np.isclose(ux @ M @ ux, 7.0 * ar.sum(), rtol=1e-12)
+
+
+def test_flat_membrane_matches_the_planar_stvk_hessian():
+    """A flat mesh in the xy plane under in-plane motion: the in-plane blocks of the
+    3D membrane Hessian (src/linear_tri3d_stvk_dq2.cpp) are the planar StVK
+    Hessian (F is the same embedded matrix with n = N = e_z)."""
+    import bartels_gb300 as bg
+    V2, E = T.square_mesh(2, seed=4, jitter=0.2)
+    V3 = np.c_[V2, np.zeros(len(V2))]
+    A = np.array([[1.1, 0.15], [-0.05, 0.95]])
+    x2 = V2 @ A.T
+    x3 = np.c_[x2, np.zeros(len(V2))]
+    p = material_params("stvk", len(E), 1e5, 0.3)
+    N, _ = bg.triangle_normals(V3, E)
+    n, dndq = bg.triangle_normals(x3, E)
+    H3 = T.stvk_hessian_3d(len(V3), E, x3.ravel(), T.dphi_dX_3d(V3, E), N, n, dndq, T.area_3d(V3, E), p).toarray()
+    H2 = T.hessian("stvk", len(V2), E, x2.ravel(), T.dphi_dX(V2, E), T.area(V2, E), p).toarray()
+    inplane = np.array([3 * v + k for v in range(len(V2)) for k in range(2)])
+    assert np.abs(H3[np.ix_(inplane, inplane)] - H2).max() <= 1e-9 * np.abs(H2).max()
+    assert np.allclose(T.area_3d(V3, E), T.area(V2, E), rtol=1e-13)
