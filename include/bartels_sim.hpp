@@ -163,6 +163,131 @@ BARTELS_SIM_MODEL(arap, BARTELS_ARAP)
 BARTELS_SIM_MODEL(linear_elasticity, BARTELS_LINEAR_ELASTICITY)
 #undef BARTELS_SIM_MODEL
 
+// ----------------------------------------------------------- triangle meshes --
+namespace detail {
+template <class MV, class ME>
+bartels_tri_plan tri_plan_for(const MV &V, const ME &E, int dim) {
+  static std::map<std::tuple<const void *, const void *, int, int, int>, bartels_tri_plan> cache;
+  auto key = std::make_tuple((const void *)V.data(), (const void *)E.data(), (int)V.rows(), (int)E.rows(), dim);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  bartels_tri_plan p = nullptr;
+  check(bartels_tri_plan_create(context(), (int)V.rows(), (int)E.rows(), E.data(), dim, &p), "bartels_tri_plan_create");
+  cache[key] = p;
+  return p;
+}
+inline void tri_pattern(SparseMatrix &S, bartels_tri_plan p) {
+  int n = 0;
+  int64_t nnz = 0;
+  check(bartels_tri_plan_csr_size(p, &n, &nnz), "bartels_tri_plan_csr_size");
+  S.n_rows = S.n_cols = n;
+  S.outer_ptr.resize(n + 1);
+  S.inner_idx.resize(nnz);
+  S.values.resize(nnz);
+  check(bartels_tri_plan_csr_pattern(p, S.outer_ptr.data(), S.inner_idx.data()), "bartels_tri_plan_csr_pattern");
+}
+template <class CB>
+void psd_of(const CB &cb, int &psd, double &tol) {
+  psd = BARTELS_PSD_NONE;
+  tol = 0.0;
+  if constexpr (std::is_same<CB, simple_psd_fix_t>::value) {
+    psd = BARTELS_PSD_SIMPLE_FIX;
+    tol = cb.tol;
+  }
+}
+}  // namespace detail
+
+// linear_tri2dmesh_dphi_dX, include/linear_tri2dmesh_dphi_dX.h (dX: nT x 6)
+template <class MR, class MV, class ME>
+void linear_tri2dmesh_dphi_dX(MR &dX, const MV &V, const ME &E) {
+  dX.resize((int)E.rows(), 6);
+  check(bartels_tri2dmesh_dphi_dX(context(), (int)V.rows(), V.data(), (int)E.rows(), E.data(), dX.data(), nullptr),
+        "bartels_tri2dmesh_dphi_dX");
+}
+
+#define BARTELS_SIM_TRI_MODEL(name, id)                                                                            \
+  template <class MV, class ME, class MQ, class MD, class MA, class MP>                                            \
+  double linear_tri2dmesh_##name##_q(const MV &V, const ME &E, const MQ &q, const MD &dphidX, const MA &area,     \
+                                     const MP &params) {                                                           \
+    double e = 0;                                                                                                  \
+    check(bartels_tri2dmesh_q(context(), detail::tri_plan_for(V, E, 2), id, q.data(), dphidX.data(), area.data(),  \
+                              params.data(), &e),                                                                  \
+          "linear_tri2dmesh_" #name "_q");                                                                         \
+    return e;                                                                                                      \
+  }                                                                                                                \
+  template <class MG, class MV, class ME, class MQ, class MD, class MA, class MP>                                  \
+  void linear_tri2dmesh_##name##_dq(MG &g, const MV &V, const ME &E, const MQ &q, const MD &dphidX,                \
+                                    const MA &area, const MP &params) {                                            \
+    g.resize(2 * (int)V.rows(), 1);                                                                                \
+    check(bartels_tri2dmesh_dq(context(), detail::tri_plan_for(V, E, 2), id, q.data(), dphidX.data(), area.data(), \
+                               params.data(), g.data()),                                                           \
+          "linear_tri2dmesh_" #name "_dq");                                                                        \
+  }                                                                                                                \
+  template <class MV, class ME, class MQ, class MD, class MA, class MP, class CB = default_callback_t>              \
+  void linear_tri2dmesh_##name##_dq2(SparseMatrix &H, const MV &V, const ME &E, const MQ &q, const MD &dphidX,     \
+                                     const MA &area, const MP &params, const CB &cb = CB()) {                      \
+    bartels_tri_plan p = detail::tri_plan_for(V, E, 2);                                                            \
+    detail::tri_pattern(H, p);                                                                                     \
+    int psd;                                                                                                       \
+    double tol;                                                                                                    \
+    detail::psd_of(cb, psd, tol);                                                                                  \
+    check(bartels_tri2dmesh_dq2(context(), p, id, q.data(), dphidX.data(), area.data(), params.data(), psd, tol,   \
+                                H.values.data()),                                                                  \
+          "linear_tri2dmesh_" #name "_dq2");                                                                       \
+  }
+
+BARTELS_SIM_TRI_MODEL(neohookean, BARTELS_NEOHOOKEAN)
+BARTELS_SIM_TRI_MODEL(stvk, BARTELS_STVK)
+BARTELS_SIM_TRI_MODEL(corotational, BARTELS_COROTATIONAL)
+BARTELS_SIM_TRI_MODEL(arap, BARTELS_ARAP)
+#undef BARTELS_SIM_TRI_MODEL
+
+// linear_tri2dmesh_linear_elasticity_dq2 (the reference has only the Hessian)
+template <class MV, class ME, class MQ, class MD, class MA, class MP, class CB = default_callback_t>
+void linear_tri2dmesh_linear_elasticity_dq2(SparseMatrix &H, const MV &V, const ME &E, const MQ &q, const MD &dphidX,
+                                            const MA &area, const MP &params, const CB &cb = CB()) {
+  bartels_tri_plan p = detail::tri_plan_for(V, E, 2);
+  detail::tri_pattern(H, p);
+  int psd;
+  double tol;
+  detail::psd_of(cb, psd, tol);
+  check(bartels_tri2dmesh_dq2(context(), p, BARTELS_LINEAR_ELASTICITY, q.data(), dphidX.data(), area.data(),
+                              params.data(), psd, tol, H.values.data()),
+        "linear_tri2dmesh_linear_elasticity_dq2");
+}
+
+// linear_tri2dmesh_mass_matrix, include/linear_tri2dmesh_mass_matrix.h
+template <class MV, class ME, class MD, class MA>
+void linear_tri2dmesh_mass_matrix(SparseMatrix &M, const MV &V, const ME &E, const MD &density, const MA &area) {
+  bartels_tri_plan p = detail::tri_plan_for(V, E, 2);
+  detail::tri_pattern(M, p);
+  check(bartels_tri2dmesh_mass_matrix(context(), p, density.data(), area.data(), M.values.data()),
+        "linear_tri2dmesh_mass_matrix");
+}
+
+// linear_tri3dmesh_dphi_dX, include/linear_tri3dmesh_dphi_dX.h (dX: nT x 9)
+template <class MR, class MV, class ME>
+void linear_tri3dmesh_dphi_dX(MR &dX, const MV &V, const ME &E) {
+  dX.resize((int)E.rows(), 9);
+  check(bartels_tri3dmesh_dphi_dX(context(), (int)V.rows(), V.data(), (int)E.rows(), E.data(), dX.data(), nullptr),
+        "bartels_tri3dmesh_dphi_dX");
+}
+
+// linear_tri3dmesh_stvk_dq2, include/linear_tri3dmesh_stvk_dq2.h:14-25
+template <class MV, class ME, class MQ, class MD, class MN, class Mn, class MdN, class MA, class MP,
+          class CB = default_callback_t>
+void linear_tri3dmesh_stvk_dq2(SparseMatrix &H, const MV &V, const ME &E, const MQ &q, const MD &dphidX, const MN &N,
+                               const Mn &n, const MdN &dndq, const MA &area, const MP &params, const CB &cb = CB()) {
+  bartels_tri_plan p = detail::tri_plan_for(V, E, 3);
+  detail::tri_pattern(H, p);
+  int psd;
+  double tol;
+  detail::psd_of(cb, psd, tol);
+  check(bartels_tri3dmesh_stvk_dq2(context(), p, q.data(), dphidX.data(), N.data(), n.data(), dndq.data(),
+                                   area.data(), params.data(), psd, tol, H.values.data()),
+        "linear_tri3dmesh_stvk_dq2");
+}
+
 // linear_tetmesh_mass_matrix, include/linear_tetmesh_mass_matrix.h
 template <class MV, class ME, class MD, class MVol>
 void linear_tetmesh_mass_matrix(SparseMatrix &M, const MV &V, const ME &E, const MD &density, const MVol &volume) {

@@ -133,6 +133,33 @@ int main() {
   }
   REQUIRE(sim::linesearch_backtracking_bisection(x, dx, quad, gx, 100, 1.0, 1e-4, 0.5) == sim::CONVERGED);
   REQUIRE(std::fabs(x(0) - (1.0 - 1.5)) < 1e-12);
+  // the reference's 2D case (tests/test_constitutive_model.cpp:107-135): one triangle at rest
+  {
+    sim::MatrixXd V2(3, 2);
+    V2(0, 0) = 96.921; V2(0, 1) = 44.047;
+    V2(1, 0) = 81.5;   V2(1, 1) = 37.5;
+    V2(2, 0) = 87.452; V2(2, 1) = 31.207;
+    sim::MatrixXi E2(1, 3);
+    E2(0, 0) = 0; E2(0, 1) = 1; E2(0, 2) = 2;
+    sim::MatrixXd params2(1, 2);
+    params2(0, 0) = 6.2069e+06;
+    params2(0, 1) = 6.8966e+05;
+    sim::VectorXd area(1, 1);
+    area(0) = 68.002;
+    sim::VectorXd q2(6, 1);
+    for (int v = 0; v < 3; ++v) {
+      q2(2 * v) = V2(v, 0);
+      q2(2 * v + 1) = V2(v, 1);
+    }
+    sim::MatrixXd dX2;
+    sim::linear_tri2dmesh_dphi_dX(dX2, V2, E2);
+    sim::VectorXd f2;
+    sim::linear_tri2dmesh_corotational_dq(f2, V2, E2, q2, dX2, area, params2);
+    for (int i = 0; i < 6; ++i) REQUIRE(std::fabs(f2(i)) <= 1e-6 * 6.2069e+06);
+    sim::SparseMatrix H2;
+    sim::linear_tri2dmesh_neohookean_dq2(H2, V2, E2, q2, dX2, area, params2, sim::simple_psd_fix(1e-6));
+    REQUIRE(H2.rows() == 6 && H2.nonZeros() == 36);
+  }
   std::printf("sim shim ok: energy %.6e, nnz %lld, pcg iterations %d\n", e0, (long long)H.nonZeros(),
               solver.report.iterations);
   return 0;
