@@ -259,7 +259,7 @@ int bartels_linesearch_backtracking_bisection(int n, double *x, const double *d,
  *   q(x)  = q_base + scale * x
  *   f(x)  = mass_coeff * (1/2 x^T M x - x^T M x_hat) + Psi(q(x)) - force_scale * x^T f_ext
  * restricted to the free vertices (pinned vertices keep x = 0).
- * Quasi-static (config: Newton under gravity): mass_coeff 0, scale 1, q_base 0.
+ * Quasi-static (Newton under gravity): mass_coeff 0, scale 1, q_base 0.
  * Implicit Euler in velocity form (matlab/examples/implicit_integration.m:69-83):
  *   x = v, q_base = q_t, scale = dt, x_hat = v_t, force_scale = dt, mass_coeff 1.
  * M is the consistent mass matrix of the plan's density. */

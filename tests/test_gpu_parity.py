@@ -207,7 +207,7 @@ def _gravity_problem(n, model, nu=0.45):
 
 @pytest.mark.parametrize("model", ["neohookean", "stvk"])
 def test_newton_quasistatic_vs_oracle(oracle, model):
-    """Config-1 style quasi-static solve (n=4 here), relative 1e-8."""
+    """Quasi-static solve of a gravity-loaded cube with z = 0 pinned (n=4), relative 1e-8."""
     from oracle import newton as on
     V, E, q, params, rho, pinned = _gravity_problem(4, model)
     vol = oracle.volume(V, E)
