@@ -197,10 +197,12 @@ class System:
 
 
 def sample_configs(count: int, seed: int = 0, n_range=(8, 20), models=("neohookean",), ratio_range=(30.0, 3e4),
-                   nu_range=(0.30, 0.48), stretch=0.15):
+                   nu_range=(0.30, 0.48), stretch=0.15, hetero=0.0, hetero_frac=0.5):
     """Implicit-Euler cubes with a spread of stiffness-to-inertia ratios
     E dt^2 / (rho h^2) around the n=96 benchmark's (1.8e3), Poisson ratios,
-    initial stretches and (optionally) material models."""
+    initial stretches and (optionally) material models. With hetero > 0 a
+    fraction hetero_frac of the cubes gets per-tet stiffness exp(hetero N(0, 1))
+    times the cube's E (log-normal heterogeneity)."""
     rng = np.random.default_rng(seed)
     out = []
     for _ in range(count):
@@ -212,8 +214,25 @@ def sample_configs(count: int, seed: int = 0, n_range=(8, 20), models=("neohooke
         dt = math.sqrt(ratio * rho * h * h / young)
         st = rng.uniform(1.0 - stretch, 1.0 + stretch, size=3)
         model = models[int(rng.integers(len(models)))]
-        out.append(dict(n=n, young=young, nu=nu, rho=rho, dt=dt, ratio=ratio, stretch=st.tolist(), model=model))
+        sigma = hetero if (hetero > 0 and rng.uniform() < hetero_frac) else 0.0
+        out.append(dict(n=n, young=young, nu=nu, rho=rho, dt=dt, ratio=ratio, stretch=st.tolist(), model=model,
+                        hetero=sigma))
     return out
+
+
+def _cube_params(model, nT, cfg):
+    """Per-tet params of a training cube: the cube's (E, nu), times a seeded
+    log-normal per-tet factor when cfg["hetero"] > 0 (every law's parameters
+    scale with E at fixed nu)."""
+    params = material_params(model, nT, cfg["young"], cfg["nu"])
+    sigma = cfg.get("hetero", 0.0)
+    if sigma > 0:
+        f = np.exp(sigma * np.random.default_rng(cfg.get("seed", 0) + 7919).standard_normal(nT))
+        if model == "linear_elasticity":
+            params[:, 0] *= f
+        else:
+            params *= f[:, None]
+    return params
 
 
 def newton_systems(ctx: Context, cfg: dict, newton_iters: int = 3, model: str | None = None):
@@ -223,7 +242,7 @@ def newton_systems(ctx: Context, cfg: dict, newton_iters: int = 3, model: str | 
     dev = torch.device(f"cuda:{ctx.device}")
     V, E = kuhn_cube(cfg["n"])
     plan = MeshPlan(V, E, ctx)
-    params = material_params(model, len(E), cfg["young"], cfg["nu"])
+    params = _cube_params(model, len(E), cfg)
     rho = np.full(len(E), cfg["rho"])
     plan.set_element_data(params=params, density=rho)
     vol = None
@@ -270,8 +289,7 @@ def perturbed_systems(ctx: Context, cfg: dict, count: int = 1, noise: float = 0.
     dev = torch.device(f"cuda:{ctx.device}")
     V, E = kuhn_cube(cfg["n"])
     plan = MeshPlan(V, E, ctx)
-    plan.set_element_data(params=material_params(model, len(E), cfg["young"], cfg["nu"]),
-                          density=np.full(len(E), cfg["rho"]))
+    plan.set_element_data(params=_cube_params(model, len(E), cfg), density=np.full(len(E), cfg["rho"]))
     plan.set_problem(pinned=(np.abs(V[:, 2]) <= 1e-12).astype(np.uint8))
     rng = np.random.default_rng(cfg.get("seed", 0))
     out = []

@@ -1,7 +1,9 @@
 """Train the learned PCG preconditioner on the GPU and write its weights.
 
-    python -m bartels_gb300.train_lpcg --systems 32 --steps 4000 --nmin 24 --nmax 48 --probes 8 \
-        --models neohookean,stvk,corotational --eval 32 --out bartels_gb300/weights/lpcg_neohookean.npz
+    python -m bartels_gb300.train_lpcg --kind rest --no-residual --models neohookean,stvk,corotational \
+        --probes 8 --seed 0 --newton-iters 2 --systems 48 --nmin 12 --nmax 40 --steps 12000 \
+        --hetero 1.0 --hetero-frac 0.5 --lr 3e-3 --eval 40,96 --out bartels_gb300/weights/lpcg_neohookean.npz
+        (the recipe of the shipped weights)
     python -m bartels_gb300.train_lpcg --systems 0 --steps 0 --init bartels_gb300/weights/lpcg_neohookean.npz --eval 96
         (evaluation only: PCG iterations and seconds, learned vs block-Jacobi)
 
@@ -76,6 +78,9 @@ def main(argv=None):
     ap.add_argument("--kind", default="newton", choices=["newton", "rest"],
                     help="newton: Newton-iteration Hessians with residuals; rest: Hessians at perturbed rest states")
     ap.add_argument("--no-residual", action="store_true", help="train with Rademacher probes only")
+    ap.add_argument("--hetero", type=float, default=0.0,
+                    help="sigma of a log-normal per-tet stiffness factor on a fraction of the cubes")
+    ap.add_argument("--hetero-frac", type=float, default=0.5, help="fraction of the cubes made heterogeneous")
     args = ap.parse_args(argv)
     import bartels_gb300 as bg
     from . import lpcg
@@ -86,7 +91,8 @@ def main(argv=None):
     rr = tuple(float(v) for v in args.ratio.split(","))
     nr = tuple(float(v) for v in args.nu.split(","))
     for cfg in lpcg.sample_configs(args.systems, seed=args.seed, n_range=(args.nmin, args.nmax), models=models,
-                                   ratio_range=rr, nu_range=nr, stretch=args.stretch):
+                                   ratio_range=rr, nu_range=nr, stretch=args.stretch, hetero=args.hetero,
+                                   hetero_frac=args.hetero_frac):
         cfg["seed"] = len(systems)
         if args.kind == "newton":
             systems += lpcg.newton_systems(ctx, cfg, newton_iters=args.newton_iters)

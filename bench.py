@@ -10,8 +10,8 @@ the next one starts. Synthetic, seeded inputs (no dataset).
 
 The headline value uses the learned preconditioner (the network's factor G is
 rebuilt from each Newton Hessian inside the timed region; M^-1 = G^T G), with
-weights trained by bartels_gb300/train_lpcg.py on other cubes (n = 5..24,
-three material models). The same workload is then timed with block-Jacobi PCG
+weights trained by bartels_gb300/train_lpcg.py on other cubes (n = 12..40,
+three material models, half of them with log-normal per-tet stiffness). The same workload is then timed with block-Jacobi PCG
 on the same GPU ("jacobi_pcg" in the JSON line).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--precond jacobi]
