@@ -124,7 +124,19 @@ SIGNATURES = [
     ("bartels_tri2dmesh_mass_matrix", C.c_int, [_P, _P, _D, _D, _D]),
     ("bartels_tri3dmesh_dphi_dX", C.c_int, [_P, C.c_int, _D, C.c_int, _I, _D, _D]),
     ("bartels_tri3dmesh_stvk_dq2", C.c_int, [_P, _P, _D, _D, _D, _D, _D, _D, _D, C.c_int, C.c_double, _D]),
+    ("bartels_mex_routine_count", C.c_int, []),
+    ("bartels_mex_routine_name", C.c_char_p, [C.c_int]),
+    ("bartels_mex_release", None, []),
 ]
+
+
+class MxArray(C.Structure):
+    """bartels_mx of include/bartels_mex.h: an m x n column-major double matrix."""
+    _fields_ = [("m", C.c_int64), ("n", C.c_int64), ("pr", _D)]
+
+
+MX_ALLOC = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.POINTER(_D),
+                       C.POINTER(C.POINTER(C.c_uint64)), C.POINTER(C.POINTER(C.c_uint64)))
 
 _lib = None
 

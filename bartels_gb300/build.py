@@ -19,7 +19,7 @@ CSRC = os.path.join(PKG, "csrc")
 OBJ = os.path.join(PKG, "_build")
 LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libbartels_gpu.so")
-SOURCES = ["elements.cu", "plan.cu", "solver.cu", "capi.cu", "lpcg.cu", "gemm_tc.cu", "tri.cu"]
+SOURCES = ["elements.cu", "plan.cu", "solver.cu", "capi.cu", "lpcg.cu", "gemm_tc.cu", "tri.cu", "mex.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -55,7 +55,8 @@ def _stale() -> bool:
     if not os.path.exists(LIB):
         return True
     t = os.path.getmtime(LIB)
-    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(ROOT, "include", "bartels_gpu.h")]
+    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [
+        os.path.join(ROOT, "include", h) for h in ("bartels_gpu.h", "bartels_mex.h")]
     return any(os.path.getmtime(p) > t for p in deps)
 
 

@@ -1,5 +1,5 @@
 """C ABI checks that need no GPU: the library loads, exports every function
-declared in include/bartels_gpu.h, and its host-only entry points (integer
+declared in include/*.h, and its host-only entry points (integer
 bookkeeping, the host line search) agree with the oracle. Also the Kuhn cube
 generator's counts against the assembled pattern."""
 import ctypes as C
@@ -17,7 +17,8 @@ from bartels_gb300.meshes import cube_counts, kuhn_cube
 
 
 def declared_functions():
-    text = open(os.path.join(ROOT, "include", "bartels_gpu.h")).read()
+    inc = os.path.join(ROOT, "include")
+    text = "".join(open(os.path.join(inc, h)).read() for h in sorted(os.listdir(inc)) if h.endswith(".h"))
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return sorted(set(re.findall(r"\b(bartels_[A-Za-z0-9_]+)\s*\(", text)) - {"bartels_objective_fn"})
 
