@@ -9,14 +9,16 @@
 // so outer_ptr/inner_idx read as CSR or CSC) and can be wrapped with
 // Eigen::Map<Eigen::SparseMatrix<double>>.
 //
-// A mesh plan is cached per (V, E) data pointer pair and size, so repeated
-// calls on the same mesh reuse the pattern; element data is uploaded per call
-// as in the reference. Errors throw sim::Error (the reference asserts or
+// Mesh plans are cached by content (E, and V for tets, compared exactly; the
+// four most recently used are kept), so repeated calls on one mesh reuse its
+// pattern and a buffer reused for another mesh never meets a stale plan;
+// element data is uploaded per call as in the reference. Errors throw sim::Error (the reference asserts or
 // exits).
 #pragma once
 
+#include <algorithm>
 #include <cstdint>
-#include <map>
+#include <list>
 #include <stdexcept>
 #include <string>
 #include <tuple>
@@ -58,6 +60,7 @@ struct Dense {
   T &operator()(int i, int j) { return v[i + (size_t)r * j]; }
   const T &operator()(int i, int j) const { return v[i + (size_t)r * j]; }
   T &operator()(int i) { return v[i]; }
+  const T &operator()(int i) const { return v[i]; }
 };
 using MatrixXd = Dense<double>;
 using MatrixXi = Dense<int>;
@@ -83,16 +86,45 @@ inline bartels_ctx context() {
 }
 
 namespace detail {
+// Most-recently-used list of plans keyed by (tag, nV, V values, E values).
+template <class Plan>
+struct PlanCache {
+  struct Item {
+    int tag, nV;
+    std::vector<double> V;
+    std::vector<int> E;
+    Plan plan;
+  };
+  std::list<Item> items;
+  template <class Make, class Destroy>
+  Plan get(int tag, int nV, const double *V, size_t nVvals, const int *E, size_t nE, Make make, Destroy destroy) {
+    for (auto it = items.begin(); it != items.end(); ++it) {
+      if (it->tag != tag || it->nV != nV || it->V.size() != nVvals || it->E.size() != nE) continue;
+      if (!std::equal(E, E + nE, it->E.begin()) || !std::equal(V, V + nVvals, it->V.begin())) continue;
+      items.splice(items.begin(), items, it);
+      return items.front().plan;
+    }
+    Plan p = make();
+    items.push_front(Item{tag, nV, std::vector<double>(V, V + nVvals), std::vector<int>(E, E + nE), p});
+    while (items.size() > 4) {
+      destroy(items.back().plan);
+      items.pop_back();
+    }
+    return p;
+  }
+};
+
 template <class MV, class ME>
 bartels_mesh_plan plan_for(const MV &V, const ME &E) {
-  static std::map<std::tuple<const void *, const void *, int, int>, bartels_mesh_plan> cache;
-  auto key = std::make_tuple((const void *)V.data(), (const void *)E.data(), (int)V.rows(), (int)E.rows());
-  auto it = cache.find(key);
-  if (it != cache.end()) return it->second;
-  bartels_mesh_plan p = nullptr;
-  check(bartels_plan_create(context(), (int)V.rows(), V.data(), (int)E.rows(), E.data(), &p), "bartels_plan_create");
-  cache[key] = p;
-  return p;
+  static PlanCache<bartels_mesh_plan> cache;
+  const int nV = (int)V.rows(), nT = (int)E.rows();
+  return cache.get(0, nV, V.data(), 3 * (size_t)nV, E.data(), 4 * (size_t)nT,
+                   [&] {
+                     bartels_mesh_plan p = nullptr;
+                     check(bartels_plan_create(context(), nV, V.data(), nT, E.data(), &p), "bartels_plan_create");
+                     return p;
+                   },
+                   [](bartels_mesh_plan p) { bartels_plan_destroy(p); });
 }
 template <class Out>
 void copy_pattern(SparseMatrix &S, bartels_mesh_plan p, int n, int64_t nnz) {
@@ -167,14 +199,15 @@ BARTELS_SIM_MODEL(linear_elasticity, BARTELS_LINEAR_ELASTICITY)
 namespace detail {
 template <class MV, class ME>
 bartels_tri_plan tri_plan_for(const MV &V, const ME &E, int dim) {
-  static std::map<std::tuple<const void *, const void *, int, int, int>, bartels_tri_plan> cache;
-  auto key = std::make_tuple((const void *)V.data(), (const void *)E.data(), (int)V.rows(), (int)E.rows(), dim);
-  auto it = cache.find(key);
-  if (it != cache.end()) return it->second;
-  bartels_tri_plan p = nullptr;
-  check(bartels_tri_plan_create(context(), (int)V.rows(), (int)E.rows(), E.data(), dim, &p), "bartels_tri_plan_create");
-  cache[key] = p;
-  return p;
+  static PlanCache<bartels_tri_plan> cache;
+  const int nV = (int)V.rows(), nT = (int)E.rows();
+  return cache.get(dim, nV, nullptr, 0, E.data(), 3 * (size_t)nT,
+                   [&] {
+                     bartels_tri_plan p = nullptr;
+                     check(bartels_tri_plan_create(context(), nV, nT, E.data(), dim, &p), "bartels_tri_plan_create");
+                     return p;
+                   },
+                   [](bartels_tri_plan p) { bartels_tri_plan_destroy(p); });
 }
 inline void tri_pattern(SparseMatrix &S, bartels_tri_plan p) {
   int n = 0;

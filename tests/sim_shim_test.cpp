@@ -133,6 +133,26 @@ int main() {
   }
   REQUIRE(sim::linesearch_backtracking_bisection(x, dx, quad, gx, 100, 1.0, 1e-4, 0.5) == sim::CONVERGED);
   REQUIRE(std::fabs(x(0) - (1.0 - 1.5)) < 1e-12);
+  // the same V / E buffers rewritten in place with the vertices relabelled
+  // v -> nV - 1 - v: a new mesh at the old addresses, the same physical state
+  {
+    const sim::MatrixXd V0 = V;
+    const sim::VectorXd q0 = q;
+    for (int v = 0; v < nV; ++v)
+      for (int d = 0; d < 3; ++d) {
+        V(nV - 1 - v, d) = V0(v, d);
+        q(3 * (nV - 1 - v) + d) = q0(3 * v + d);
+      }
+    for (int e = 0; e < nT; ++e)
+      for (int a = 0; a < 4; ++a) E(e, a) = nV - 1 - E(e, a);
+    const double e1 = sim::linear_tetmesh_neohookean_q(V, E, q, dphidX, vol, params);
+    REQUIRE(std::fabs(e1 - e0) <= 1e-10 * e0);
+    sim::VectorXd g1;
+    sim::linear_tetmesh_neohookean_dq(g1, V, E, q, dphidX, vol, params);
+    for (int v = 0; v < nV; ++v)
+      for (int d = 0; d < 3; ++d)
+        REQUIRE(std::fabs(g1(3 * (nV - 1 - v) + d) - g(3 * v + d)) <= 1e-9 * (std::fabs(g(3 * v + d)) + 1.0));
+  }
   // the reference's 2D case (tests/test_constitutive_model.cpp:107-135): one triangle at rest
   {
     sim::MatrixXd V2(3, 2);
