@@ -255,7 +255,7 @@ _plans: "OrderedDict[str, MeshPlan]" = OrderedDict()
 def _plan_for(V, E) -> MeshPlan:
     V = _f64(V)
     E = np.ascontiguousarray(E, dtype=np.int32)
-    key = hashlib.sha1(V.tobytes() + b"|" + E.tobytes()).hexdigest()
+    key = hashlib.sha1(f"{V.shape}{E.shape}".encode() + V.tobytes() + E.tobytes()).hexdigest()
     p = _plans.get(key)
     if p is None:
         p = MeshPlan(V, E)
@@ -409,7 +409,7 @@ _tri_plans: "OrderedDict[str, Tri2DPlan]" = OrderedDict()
 def _tri_plan_for(V, E) -> Tri2DPlan:
     E = np.ascontiguousarray(E, dtype=np.int32)
     nV = len(V)
-    key = hashlib.sha1(str(nV).encode() + b"|" + E.tobytes()).hexdigest()
+    key = hashlib.sha1(f"{nV}{E.shape}".encode() + E.tobytes()).hexdigest()
     p = _tri_plans.get(key)
     if p is None:
         p = Tri2DPlan(nV, E)
@@ -505,7 +505,7 @@ _tri3_plans: "OrderedDict[str, Tri3DPlan]" = OrderedDict()
 def _tri3_plan_for(V, E) -> Tri3DPlan:
     E = np.ascontiguousarray(E, dtype=np.int32)
     nV = len(V)
-    key = hashlib.sha1(str(nV).encode() + b"|" + E.tobytes()).hexdigest()
+    key = hashlib.sha1(f"{nV}{E.shape}".encode() + E.tobytes()).hexdigest()
     p = _tri3_plans.get(key)
     if p is None:
         p = Tri3DPlan(nV, E)
