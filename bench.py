@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--no-psd", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-faithful-baseline", action="store_true",
+                    help="skip the 1-thread reference-structured CPU sample beside the OpenMP baseline")
     ap.add_argument("--precond", default="learned", choices=["learned", "jacobi"])
     ap.add_argument("--weights", default=os.path.join(ROOT, "bartels_gb300", "weights", "lpcg_neohookean.npz"))
     ap.add_argument("--no-jacobi-arm", action="store_true", help="skip the block-Jacobi comparison run")
@@ -332,6 +334,10 @@ def run_gpu(args, rank, world):
         cpu = {"value": 1.0 / est[0], "unit": UNIT, "cores": threads, "kind": "port",
                "sample": cpu_sample_text(counts, args.n).replace("from the GPU run of the same workload", "from this run"),
                "components": parts}
+        if not args.no_faithful_baseline:
+            f_est, f_parts = cpu_faithful_sample(pb, args, counts)
+            cpu["reference_faithful_1thread"] = {"value": 1.0 / f_est, "unit": UNIT, "cores": 1,
+                                                 "sample": cpu_faithful_text(counts, args.n), "components": f_parts}
 
     precond_name = "learned factor G^T G" if net is not None else "block-Jacobi"
     value = replica_value(newton_its, world, ms)
@@ -414,6 +420,60 @@ def cpu_newton_sample(pb, args, counts, reps=1):
         parts = {"gradient_s": t_g, "hessian_s": t_h, "pcg_iter_s": t_p, "energy_s": t_e}
     cb.close()
     return est, parts, cb.threads, t_setup
+
+
+def cpu_faithful_sample(pb, args, counts):
+    """The reference's own structure on one host thread, timed on bounded
+    samples of this workload: per-tet dense B^T d2psi B with simple_psd_fix, a
+    triplet list and a sort / compress into CSR (src/assemble.cpp:57-94), serial
+    gradient and energy sums (oracle/oracle_baseline.cpp, oracle/oracle_capi.cpp),
+    simple_psd_fix by tridiagonal QL as Eigen's solver does, over 1/64 of the tets
+    (scaled x64); the line search's two energy evaluations per trial
+    (src/linesearch_backtracking_bisection.cpp:21); block-Jacobi PCG
+    iterations on the full system with one OpenMP thread (scaled to the PCG
+    iteration count per Newton iteration; the reference's SparseLU cannot
+    factor 2.7M DOF here). Returns (seconds per Newton iteration, components)."""
+    from oracle import oracle as o
+    from oracle.baseline import CpuNewton, faithful_dq2
+    V, E = pb["V"], pb["E"]
+    nV, nT = len(V), len(E)
+    sub = E[: max(1, nT // 64)]
+    scale = nT / len(sub)
+    q = V.ravel().copy()
+    dphi, vol = o.dphi_dX(V, sub), o.volume(V, sub)
+    params = pb["params"][: len(sub)]
+    psd = None if args.no_psd else 1e-6
+    t = time.perf_counter(); faithful_dq2(args.model, nV, sub, q, dphi, vol, params, psd)
+    t_h = (time.perf_counter() - t) * scale
+    t = time.perf_counter(); o.tetmesh_dq(args.model, nV, sub, q, dphi, vol, params)
+    t_g = (time.perf_counter() - t) * scale
+    t = time.perf_counter(); o.tetmesh_q(args.model, sub, q, dphi, vol, params)
+    t_e = (time.perf_counter() - t) * scale
+    cb = CpuNewton(V, E)
+    full_vol = o.volume(V, E)
+    cb.set(args.model, pb["params"], np.full(nT, pb["rho"]), q, np.zeros(3 * nV),
+           o.const_ext_force(nV, E, full_vol, pb["rho"] * pb["gravity"]), pb["pinned"], 1.0, pb["dt"], pb["dt"], psd)
+    threads = cb.threads
+    x = np.zeros(3 * nV)
+    g = cb.gradient(x)
+    cb.hessian_range(x, 0, len(sub), True)  # PCG cost per iteration does not depend on the values
+    cb.set_threads(1)
+    try:
+        d = np.zeros(3 * nV)
+        t = time.perf_counter(); it, _ = cb.pcg(-g, d, 1e-30, 3); t_p = (time.perf_counter() - t) / max(it, 1)
+    finally:
+        cb.set_threads(threads)
+        cb.close()
+    n_pcg, n_ls = counts["pcg_per_newton"], counts["ls_per_newton"]
+    est = t_g + t_h + n_pcg * t_p + 2.0 * (1.0 + n_ls) * t_e
+    return est, {"gradient_s": t_g, "hessian_s": t_h, "pcg_iter_s": t_p, "energy_s": t_e}
+
+
+def cpu_faithful_text(counts, n=96):
+    return (f"one Newton iteration of the n={n} workload in the reference's structure on 1 thread: dense per-tet "
+            "B^T d2psi B + simple_psd_fix, triplets + sort/compress, serial gradient and energy, over 1/64 of the "
+            f"tets x64; 3 block-Jacobi PCG iterations on the full system (1 thread) x {counts['pcg_per_newton']:.0f} "
+            "per Newton; 2 energy evaluations per line-search trial")
 
 
 def cpu_sample_text(counts, n=96):

@@ -794,6 +794,113 @@ inline void psd_fix(double *A, int n, double tol) {
     }
 }
 
+// The same projection with the method class of Eigen's SelfAdjointEigenSolver
+// (Householder tridiagonalisation, then implicit-shift QL iterations on the
+// tridiagonal matrix with the rotations accumulated into the eigenvectors;
+// Golub & Van Loan, Matrix Computations, 8.3; Wilkinson & Reinsch's tred2 /
+// tql2): O(n^3) with a small constant where cyclic Jacobi takes many sweeps.
+// Used by the timed CPU baseline so that its cost per element is that of a
+// production eigen-solver; the parity checks keep psd_fix above. n <= 12.
+// Returns false if the QL iteration did not converge (A left unchanged).
+inline bool psd_fix_ql(double *A, int n, double tol) {
+  double Z[144], d[12], e[12];
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) Z[i + n * j] = (i >= j) ? A[i + n * j] : A[j + n * i];
+  // Householder reflections H_k = I - 2 v v^T zero column k below the
+  // subdiagonal; Q = H_0 H_1 ... is accumulated separately.
+  double Q[144];
+  for (int i = 0; i < n * n; ++i) Q[i] = 0.0;
+  for (int i = 0; i < n; ++i) Q[i + n * i] = 1.0;
+  for (int k = 0; k + 2 < n; ++k) {
+    double v[12], nx = 0.0;
+    for (int i = k + 1; i < n; ++i) nx += Z[i + n * k] * Z[i + n * k];
+    nx = std::sqrt(nx);
+    if (nx == 0.0) continue;
+    const double x0 = Z[(k + 1) + n * k];
+    const double alpha = x0 >= 0.0 ? -nx : nx;
+    double nv = 0.0;
+    for (int i = k + 1; i < n; ++i) {
+      v[i] = Z[i + n * k] - (i == k + 1 ? alpha : 0.0);
+      nv += v[i] * v[i];
+    }
+    nv = std::sqrt(nv);
+    if (nv == 0.0) continue;
+    for (int i = k + 1; i < n; ++i) v[i] /= nv;
+    // trailing block: A22 <- A22 - 2 v w^T - 2 w v^T, w = p - (v^T p) v, p = A22 v
+    double p[12], vp = 0.0;
+    for (int i = k + 1; i < n; ++i) {
+      double s = 0.0;
+      for (int j = k + 1; j < n; ++j) s += Z[i + n * j] * v[j];
+      p[i] = s;
+      vp += v[i] * s;
+    }
+    for (int i = k + 1; i < n; ++i) p[i] -= vp * v[i];
+    for (int i = k + 1; i < n; ++i)
+      for (int j = k + 1; j < n; ++j) Z[i + n * j] -= 2.0 * (v[i] * p[j] + p[i] * v[j]);
+    Z[(k + 1) + n * k] = Z[k + n * (k + 1)] = alpha;
+    for (int i = k + 2; i < n; ++i) Z[i + n * k] = Z[k + n * i] = 0.0;
+    for (int r = 0; r < n; ++r) {  // Q <- Q H_k
+      double s = 0.0;
+      for (int i = k + 1; i < n; ++i) s += Q[r + n * i] * v[i];
+      for (int i = k + 1; i < n; ++i) Q[r + n * i] -= 2.0 * s * v[i];
+    }
+  }
+  for (int i = 0; i < n; ++i) d[i] = Z[i + n * i];
+  for (int i = 0; i + 1 < n; ++i) e[i] = Z[(i + 1) + n * i];
+  e[n - 1] = 0.0;
+  // implicit QL with Wilkinson-type shifts; rotations applied to Q's columns
+  for (int l = 0; l < n; ++l) {
+    for (int iter = 0;; ++iter) {
+      int m = l;
+      for (; m + 1 < n; ++m) {
+        const double dd = std::fabs(d[m]) + std::fabs(d[m + 1]);
+        if (std::fabs(e[m]) + dd == dd) break;  // e[m] below the rounding of d
+      }
+      if (m == l) break;
+      if (iter == 60) return false;
+      double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+      double r = std::hypot(g, 1.0);
+      g = d[m] - d[l] + e[l] / (g + (g >= 0.0 ? r : -r));
+      double s = 1.0, c = 1.0, pp = 0.0;
+      int i = m - 1;
+      for (; i >= l; --i) {
+        const double f = s * e[i], b = c * e[i];
+        r = std::hypot(f, g);
+        e[i + 1] = r;
+        if (r == 0.0) {  // split: restart the sweep on the smaller block
+          d[i + 1] -= pp;
+          e[m] = 0.0;
+          break;
+        }
+        s = f / r;
+        c = g / r;
+        g = d[i + 1] - pp;
+        r = (d[i] - g) * s + 2.0 * c * b;
+        pp = s * r;
+        d[i + 1] = g + pp;
+        g = c * r - b;
+        for (int k = 0; k < n; ++k) {
+          const double zi = Q[k + n * i], zi1 = Q[k + n * (i + 1)];
+          Q[k + n * (i + 1)] = s * zi + c * zi1;
+          Q[k + n * i] = c * zi - s * zi1;
+        }
+      }
+      if (r == 0.0 && i >= l) continue;
+      d[l] -= pp;
+      e[l] = g;
+      e[m] = 0.0;
+    }
+  }
+  for (int i = 0; i < n; ++i) d[i] = std::max(d[i], tol);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j <= i; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < n; ++k) s += Q[i + n * k] * d[k] * Q[j + n * k];
+      A[i + n * j] = A[j + n * i] = s;
+    }
+  return true;
+}
+
 // ----------------------------------------------------------------------------
 // assembly, src/assemble.cpp
 // ----------------------------------------------------------------------------

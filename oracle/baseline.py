@@ -32,6 +32,9 @@ def _lib():
         L.ob_pcg.argtypes = [C.c_void_p, D, D, C.c_double, C.c_int, D]
         L.ob_newton_iteration.argtypes = [C.c_void_p, D, C.c_double, C.c_int, C.c_int, D]
         L.ob_threads.restype = C.c_int
+        L.ob_set_threads.argtypes = [C.c_int]
+        L.ob_faithful_dq2.restype = C.c_longlong
+        L.ob_faithful_dq2.argtypes = [C.c_int, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_int), D, D, D, D, D]
         L.ob_wtime.restype = C.c_double
         L._ob_ready = True
     return L
@@ -39,6 +42,20 @@ def _lib():
 
 def _p(a):
     return a.ctypes.data_as(D)
+
+
+def faithful_dq2(model, nV, E, q, dphidX, vol, params, psd_tol):
+    """linear_tetmesh_{model}_dq2 in the reference's structure on one thread
+    (per-tet dense blocks, simple_psd_fix, triplets, sort / compress).
+    Returns (nnz, sum of values, sum of |values|)."""
+    L = _lib()
+    Ec = np.asfortranarray(E, np.int32).ravel(order="F")
+    arrs = [np.ascontiguousarray(q, np.float64), np.asfortranarray(dphidX, np.float64).ravel(order="F"),
+            np.ascontiguousarray(vol, np.float64), np.asfortranarray(params, np.float64).ravel(order="F")]
+    sums = np.zeros(2)
+    nnz = L.ob_faithful_dq2(o.MODELS[model], -1.0 if psd_tol is None else psd_tol, nV, len(E),
+                            Ec.ctypes.data_as(C.POINTER(C.c_int)), *[_p(a) for a in arrs], _p(sums))
+    return int(nnz), float(sums[0]), float(sums[1])
 
 
 class CpuNewton:
@@ -85,6 +102,9 @@ class CpuNewton:
     @property
     def threads(self):
         return self.L.ob_threads()
+
+    def set_threads(self, n):
+        self.L.ob_set_threads(int(n))
 
     def wtime(self):
         return self.L.ob_wtime()

@@ -247,6 +247,15 @@ def psd_fix(A, tol=1e-6):
     return np.array(A)
 
 
+def psd_fix_ql(A, tol=1e-6):
+    """simple_psd_fix with the tridiagonal-QL eigen-solver of the timed CPU baseline."""
+    A = np.asfortranarray(np.array(A, np.float64))
+    ok = lib().or_psd_fix_ql(A.ctypes.data_as(C.POINTER(C.c_double)), A.shape[0], C.c_double(tol))
+    if not ok:
+        raise RuntimeError("QL iteration did not converge")
+    return np.array(A)
+
+
 def build_B(dphi12):
     da, dp = _d(np.asarray(dphi12, np.float64))
     out = np.zeros(108)

@@ -5,6 +5,9 @@
 // and vertices and a precomputed CSR pattern + scatter positions instead of a
 // triplet sort (the "optimised CPU" variant), and block-Jacobi PCG in FP64 in
 // place of Eigen::SparseLU (a direct factorisation of 2.7M DOF is impractical).
+// simple_psd_fix uses the tridiagonal-QL eigen-solver (psd_fix_ql), the method
+// class of the reference's Eigen::SelfAdjointEigenSolver. ob_faithful_dq2 is the
+// reference's own structure on one thread (triplets, sort / compress).
 //
 // TEST / BASELINE INFRASTRUCTURE ONLY: timed by bench.py on the host cores and
 // never used by the GPU library.
@@ -237,7 +240,7 @@ void ob_hessian(void *h, const double *x, int t0, int t1, int clear) {
     double qe[12], K[144];
     element_qe(*B, x, t, qe);
     element_dq2(B->model, K, qe, &B->dphi[12 * (size_t)t], &B->params[2 * (size_t)t], B->vol[t], fl);
-    if (B->psd_tol >= 0) psd_fix(K, 12, B->psd_tol);
+    if (B->psd_tol >= 0) psd_fix_ql(K, 12, B->psd_tol);
     const double m = B->density[t] * B->vol[t];
     for (int a = 0; a < 4; ++a) {
       const int v = B->E[4 * (size_t)t + a];
@@ -375,7 +378,39 @@ void ob_newton_iteration(void *h, double *x, double pcg_rel_tol, int pcg_max_it,
   }
 }
 
+// linear_tetmesh_{model}_dq2 with the simple_psd_fix callback in the
+// reference's structure (src/linear_tetmesh_neohookean_dq2.cpp:17-27,
+// src/assemble.cpp:57-94): per tet the dense 12x12, the projection, 144
+// triplets; then setFromTriplets' sort / compress. Serial. Returns nnz and the
+// sum and absolute sum of the values (for checking).
+long long ob_faithful_dq2(int model, double psd_tol, int nV, int nT, const int *E, const double *q,
+                          const double *dphidX, const double *vol, const double *params, double *sums) {
+  CSR H;
+  ElementFlags fl;
+  assemble_matrix(H, nV, nT, E, [&](int t, double *K) {
+    double qe[12], dphi[12], p[2];
+    gather_qe(qe, q, E, nT, t);
+    row_of(dphi, dphidX, nT, 12, t);
+    row_of(p, params, nT, 2, t);
+    element_dq2(model, K, qe, dphi, p, vol[t], fl);
+    if (psd_tol >= 0) psd_fix_ql(K, 12, psd_tol);
+  });
+  double s = 0, a = 0;
+  for (double v : H.val) {
+    s += v;
+    a += std::fabs(v);
+  }
+  if (sums) {
+    sums[0] = s;
+    sums[1] = a;
+  }
+  return (long long)H.val.size();
+}
+
 int ob_threads() { return omp_get_max_threads(); }
+// Thread count of the parallel regions that follow on the calling thread
+// (the reference-faithful variant times the PCG on one thread).
+void ob_set_threads(int n) { omp_set_num_threads(n > 0 ? n : omp_get_num_procs()); }
 double ob_wtime() { return now(); }
 
 }  // extern "C"

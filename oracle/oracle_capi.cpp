@@ -194,6 +194,7 @@ void or_d2psi_corot_dsvd_literal(const double *F, const double *p, double *H) {
 }
 void or_svd3(const double *F, double *U, double *S, double *V) { svd3(F, U, S, V); }
 void or_psd_fix(double *A, int n, double tol) { psd_fix(A, n, tol); }
+int or_psd_fix_ql(double *A, int n, double tol) { return psd_fix_ql(A, n, tol) ? 1 : 0; }
 void or_build_B(const double *dphi12, double *B) { build_B(B, dphi12); }
 
 }  // extern "C"
