@@ -22,7 +22,8 @@ from .api import (Context, MeshPlan, newton_params, linear_tetmesh_dphi_dX, volu
                   linear_tri2dmesh_corotational_dq2, linear_tri2dmesh_arap_q, linear_tri2dmesh_arap_dq,
                   linear_tri2dmesh_arap_dq2, linear_tri2dmesh_linear_elasticity_dq2, linear_tri2dmesh_mass_matrix,
                   Tri3DPlan, linear_tri3dmesh_dphi_dX, triangle_areas_3d, triangle_normals,
-                  linear_tri3dmesh_stvk_dq2)
+                  linear_tri3dmesh_stvk_dq2, pointwise_laws, psi_neohookean_F, dpsi_neohookean_dF,
+                  d2psi_neohookean_dF2, psi_stvk_F, dpsi_stvk_dF, d2psi_stvk_dF2)
 from . import meshes
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -645,3 +645,59 @@ def linesearch_backtracking_bisection(x, d, f, g, max_iterations, alpha, c, p):
                                                           max_iterations, alpha, c, p, C.byref(status), C.byref(a)),
           "bartels_linesearch_backtracking_bisection")
     return status.value
+
+
+# ------------------------------------------------------------- pointwise laws --
+def _flat_F(F):
+    """(3, 3), (n, 3, 3) or (n, 9) rows of column-major flattens -> (n, 9), single?"""
+    F = np.asarray(F, np.float64)
+    if F.shape == (3, 3):
+        return F.T.reshape(1, 9), True
+    if F.ndim == 3 and F.shape[1:] == (3, 3):
+        return F.transpose(0, 2, 1).reshape(len(F), 9), False
+    if F.ndim == 2 and F.shape[1] == 9:
+        return F, False
+    raise BartelsError(_lib.E_INVALID_ARG, "pointwise_laws", "F must be (3,3), (n,3,3) or (n,9)")
+
+
+def pointwise_laws(model, F, params, psi=True, dpsi=True, d2psi=True, ctx: Context | None = None):
+    """psi(F), dpsi/dF and d2psi/dF2 of `model` at each F (bartels_pointwise_laws):
+    psi (n,), dpsi (n, 9) in the column-major flatten of F, d2psi (n, 9, 9);
+    params one (2,) row per F (ARAP: k, optionally alone). A single (3, 3) F
+    gives unbatched results."""
+    ctx = ctx or Context.default()
+    Fm, single = _flat_F(F)
+    n = len(Fm)
+    P = np.asarray(params, np.float64).reshape(n, -1)
+    if P.shape[1] == 1:
+        P = np.c_[P, np.zeros(n)]
+    Fc, Pc = _colmajor(Fm, np.float64), _colmajor(P[:, :2], np.float64)
+    o_psi = np.zeros(n) if psi else None
+    o_dpsi = np.zeros((9, n)) if dpsi else None      # n x 9 column-major
+    o_d2 = np.zeros((n, 9, 9)) if d2psi else None    # block t column-major: [t, c, r]
+    check(lib().bartels_pointwise_laws(ctx.handle, MODELS[model], n, _dptr(Fc), _dptr(Pc),
+                                       None if o_psi is None else _dptr(o_psi),
+                                       None if o_dpsi is None else _dptr(o_dpsi),
+                                       None if o_d2 is None else _dptr(o_d2)), "bartels_pointwise_laws")
+    out = (o_psi, None if o_dpsi is None else o_dpsi.T.copy(),
+           None if o_d2 is None else o_d2.transpose(0, 2, 1).copy())
+    if single:
+        out = tuple(None if a is None else a[0] for a in out)
+    return out
+
+
+def _named_law(model):
+    def psi_F(F, params):
+        return pointwise_laws(model, F, params, dpsi=False, d2psi=False)[0]
+
+    def dpsi_dF(F, params):
+        return pointwise_laws(model, F, params, psi=False, d2psi=False)[1]
+
+    def d2psi_dF2(F, params):
+        return pointwise_laws(model, F, params, psi=False, dpsi=False)[2]
+    return psi_F, dpsi_dF, d2psi_dF2
+
+
+# src/psi_neohookean_F.cpp, src/dpsi_neohookean_dF.cpp, src/d2psi_neohookean_dF2.cpp and the StVK files
+psi_neohookean_F, dpsi_neohookean_dF, d2psi_neohookean_dF2 = _named_law("neohookean")
+psi_stvk_F, dpsi_stvk_dF, d2psi_stvk_dF2 = _named_law("stvk")

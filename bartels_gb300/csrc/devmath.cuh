@@ -458,6 +458,28 @@ BT_HD void arap_pv(const T *pv, T *out) {
   out[1] = pv[0];
 }
 
+#ifdef __CUDACC__
+// The block law of `model` in FP64 handed to fn (a device lambda). ARAP maps
+// its parameter onto the corotational law; the corotational law takes the
+// reference's layout.
+template <class Fn>
+__device__ __forceinline__ void with_law64(int model, const double *F, const double *pv, Fn &&fn) {
+  switch (model) {
+    case MODEL_NH: fn(LawNH<double>(F, pv)); break;
+    case MODEL_NH_ISO: fn(LawNHIso<double>(F, pv)); break;
+    case MODEL_STVK: fn(LawStVK<double>(F, pv)); break;
+    case MODEL_LE: fn(LawLE<double>(F, pv)); break;
+    case MODEL_ARAP: {
+      double pa[2];
+      arap_pv(pv, pa);
+      fn(LawCorot<double>(F, pa, false));
+      break;
+    }
+    default: fn(LawCorot<double>(F, pv, false)); break;
+  }
+}
+#endif
+
 // ----------------------------------------------------------------------------
 // FP64 energy and first Piola-Kirchhoff stress (scaled by vol via pv)
 // ----------------------------------------------------------------------------

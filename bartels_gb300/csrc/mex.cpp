@@ -21,7 +21,7 @@ namespace {
 using bartels::fail;
 
 enum Family { TET, TRI2, TRI3, ANY };
-enum Op { DPHI, MASS, FIXED, Q, DQ, DQ2 };
+enum Op { DPHI, MASS, FIXED, Q, DQ, DQ2, LAW_DPSI, LAW_D2PSI };
 
 struct Routine {
   const char *name;
@@ -63,6 +63,11 @@ const Routine kRoutines[] = {
     {"linear_tri2dmesh_linear_elasticity_dq2", TRI2, DQ2, BARTELS_LINEAR_ELASTICITY, 6, false},
     {"linear_tri3dmesh_dphi_dX", TRI3, DPHI, -1, 2, false},
     {"linear_tri3dmesh_stvk_dq2", TRI3, DQ2, BARTELS_STVK, 9, true},
+    // matlab/dpsi_neohookean_dF.cpp, matlab/d2psi_neohookean_dF2.cpp, matlab/d2psi_stvk_dF2.cpp:
+    // (E, F, params), one row of F and params per element of E
+    {"dpsi_neohookean_dF", ANY, LAW_DPSI, BARTELS_NEOHOOKEAN, 3, false},
+    {"d2psi_neohookean_dF2", ANY, LAW_D2PSI, BARTELS_NEOHOOKEAN, 3, false},
+    {"d2psi_stvk_dF2", ANY, LAW_D2PSI, BARTELS_STVK, 3, false},
 };
 #undef TET_MODEL
 #undef TRI_MODEL
@@ -284,8 +289,54 @@ int fixed_point(int nrhs, const bartels_mx *prhs, bartels_mx_alloc alloc, void *
   return BARTELS_OK;
 }
 
+// The gateways loop over the rows of E (only its row count is used) and hand
+// back dpsi as one 9 nT vector (element after element) and d2psi as the
+// 9 nT x 9 nT block-diagonal sparse matrix with every block entry stored.
+int pointwise(const Routine &R, const bartels_mx *prhs, bartels_mx_alloc alloc, void *user) {
+  const int64_t nT = prhs[0].m;
+  if (nT < 0 || nT > INT32_MAX / 81) return fail(BARTELS_E_UNSUPPORTED, "E: too many elements");
+  int st = check_shape(prhs[1], "F", nT, 9);
+  if (st != BARTELS_OK) return st;
+  std::vector<double> pbuf;
+  if ((st = params2(prhs[2], (int)nT, R.model, pbuf)) != BARTELS_OK) return st;
+  bartels_ctx ctx;
+  if ((st = get_ctx(&ctx)) != BARTELS_OK) return st;
+  const size_t n = (size_t)nT;
+  if (R.op == LAW_DPSI) {
+    std::vector<double> d(9 * n);
+    if (n && (st = bartels_pointwise_laws(ctx, R.model, (int)nT, prhs[1].pr, pbuf.data(), nullptr, d.data(),
+                                          nullptr)) != BARTELS_OK)
+      return st;
+    double *out;
+    if ((st = alloc_dense(alloc, user, 9 * nT, 1, &out)) != BARTELS_OK) return st;
+    for (size_t t = 0; t < n; ++t)
+      for (int r = 0; r < 9; ++r) out[9 * t + r] = d[t + n * r];
+    return BARTELS_OK;
+  }
+  std::vector<double> H(81 * n);
+  if (n && (st = bartels_pointwise_laws(ctx, R.model, (int)nT, prhs[1].pr, pbuf.data(), nullptr, nullptr,
+                                        H.data())) != BARTELS_OK)
+    return st;
+  double *pr = nullptr;
+  uint64_t *ir = nullptr, *jc = nullptr;
+  const int64_t nnz = 81 * nT;
+  if (alloc(user, 9 * nT, 9 * nT, nnz, &pr, &ir, &jc) != 0 || !jc || (nnz > 0 && (!pr || !ir)))
+    return fail(BARTELS_E_INVALID_ARG, "output allocation failed");
+  for (size_t t = 0; t < n; ++t)
+    for (int c = 0; c < 9; ++c) {
+      jc[9 * t + c] = 81 * t + 9 * c;
+      for (int r = 0; r < 9; ++r) {
+        ir[81 * t + 9 * c + r] = 9 * t + r;
+        pr[81 * t + 9 * c + r] = H[81 * t + r + 9 * c];
+      }
+    }
+  jc[9 * n] = (uint64_t)nnz;
+  return BARTELS_OK;
+}
+
 int run(const Routine &R, int nrhs, const bartels_mx *prhs, bartels_mx_alloc alloc, void *user) {
   if (R.op == FIXED) return fixed_point(nrhs, prhs, alloc, user);
+  if (R.op == LAW_DPSI || R.op == LAW_D2PSI) return pointwise(R, prhs, alloc, user);
   // ---- validation (host only, before any device work)
   const int vdim = R.fam == TRI2 ? 2 : 3;                 // columns of V
   const int nodes = R.fam == TET ? 4 : 3;                  // columns of E

@@ -92,23 +92,6 @@ __device__ __forceinline__ void tri_load(int t, int nT, const int4 *__restrict__
   el.pv[1] = A * params[t + (size_t)nT];
 }
 
-template <class Fn>
-__device__ __forceinline__ void tri_law(int model, const double *F, const double *pv, Fn &&fn) {
-  switch (model) {
-    case MODEL_NH: fn(LawNH<double>(F, pv)); break;
-    case MODEL_NH_ISO: fn(LawNHIso<double>(F, pv)); break;
-    case MODEL_STVK: fn(LawStVK<double>(F, pv)); break;
-    case MODEL_LE: fn(LawLE<double>(F, pv)); break;
-    case MODEL_ARAP: {
-      double pa[2];
-      arap_pv(pv, pa);
-      fn(LawCorot<double>(F, pa, false));
-      break;
-    }
-    default: fn(LawCorot<double>(F, pv, false)); break;
-  }
-}
-
 // Symmetric N x N (row-major, in place) -> W max(L, tol) W^T: cyclic Jacobi
 // until the off-diagonal mass is at rounding level (at most 40 sweeps).
 template <int N>
@@ -172,7 +155,7 @@ __global__ void k_tri2d_elem(int what, int model, int nT, const int4 *__restrict
         for (int k = 0; k < 2; ++k) out[6ll * t + 2 * a + k] = P[k] * el.phi[a][0] + P[k + 3] * el.phi[a][1];
     } else {
       double K[36];
-      tri_law(model, el.F, el.pv, [&](const auto &law) {
+      with_law64(model, el.F, el.pv, [&](const auto &law) {
         for (int a = 0; a < 3; ++a)
           for (int b = 0; b < 3; ++b) {
             double B3[9];

@@ -190,6 +190,21 @@ int bartels_tetmesh_linear_elasticity_dq2(bartels_ctx, bartels_mesh_plan, const 
                                           const double *vol, const double *params, int psd_mode, double psd_tol,
                                           double *csr_values);
 
+/* --------------------------------------------------------- pointwise laws -- */
+/* The laws themselves over n deformation gradients: psi_<law>_F,
+ * dpsi_<law>_dF and d2psi_<law>_dF2 of the reference (src/psi_neohookean_F.cpp:31,
+ * src/dpsi_neohookean_dF.cpp:58-66, src/d2psi_neohookean_dF2.cpp:185-283,
+ * src/psi_stvk_F.cpp, src/dpsi_stvk_dF.cpp, src/d2psi_stvk_dF2.cpp; the
+ * corotational and ARAP laws through src/psi_stretch_F.cpp, src/dpsi_stretch_dF.cpp
+ * and src/d2psi_stretch_dF2.cpp, in the reference's layout). F: n x 9
+ * column-major, row t the column-major flatten [F11 F21 F31 F12 ...] of F_t;
+ * params n x 2 column-major (the mesh entry points' per-tet rows, volume 1).
+ * Outputs (any may be NULL): psi n; dpsi n x 9 column-major, row t = dpsi/dF in
+ * the same flatten; d2psi n blocks of 81, block t the column-major 9 x 9 with
+ * entry (r, c) = d2psi / dvec(F)_r dvec(F)_c. FP64 on the device. */
+int bartels_pointwise_laws(bartels_ctx ctx, int model, int n, const double *F, const double *params, double *psi,
+                           double *dpsi, double *d2psi);
+
 /* --------------------------------------------------- mass, loads, bounds --- */
 /* linear_tetmesh_mass_matrix, src/linear_tetmesh_mass_matrix.cpp:7-24 (per tet
  * src/linear_tet_mass_matrix.cpp:12-42): values in the plan's CSR order. */

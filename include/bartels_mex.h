@@ -41,6 +41,8 @@
  *   linear_tri2dmesh_<m>_{q,dq,dq2}(V, E, q, dphidX, areas, params[, psd]), linear_tri2dmesh_linear_elasticity_dq2
  *   linear_tri3dmesh_dphi_dX(V, E)                        -> nT x 9
  *   linear_tri3dmesh_stvk_dq2(V, E, q, dphidX, N, n, dndq, areas, params[, psd])  -> sparse 3nV x 3nV
+ *   dpsi_neohookean_dF(E, F, params)                      -> 9nT x 1 (F nT x 9, row t = flatten of F_t)
+ *   d2psi_neohookean_dF2(E, F, params), d2psi_stvk_dF2    -> sparse 9nT x 9nT, block diagonal
  *
  * E and fixed are 1-based doubles as MATLAB passes them; they must be integral
  * and in range (the reference's gateways do not check). q is used as given: the

@@ -11,14 +11,15 @@ import bartels_gb300 as bg
 from bartels_gb300 import _lib, mex
 
 MODELS = ["neohookean", "stvk", "corotational", "arap"]
-# matlab/<name>.cpp gateways of the tet and triangle families (the muscle model,
-# linear_*_B / _F and the pointwise dpsi / d2psi gateways are outside this library)
+# matlab/<name>.cpp gateways of the tet and triangle families and the pointwise
+# laws (the muscle model and linear_*_B / _F are outside this library)
 GATEWAYS = (
     ["linear_tetmesh_dphi_dX", "linear_tetmesh_mass_matrix", "fixed_point_constraint_matrix",
      "linear_tetmesh_linear_elasticity_dq2", "linear_tri2dmesh_dphi_dX", "linear_tri2dmesh_mass_matrix",
      "linear_tri2dmesh_linear_elasticity_dq2", "linear_tri3dmesh_dphi_dX", "linear_tri3dmesh_stvk_dq2"]
     + [f"linear_tetmesh_{m}_{w}" for m in MODELS for w in ("q", "dq", "dq2")]
     + [f"linear_tri2dmesh_{m}_{w}" for m in MODELS for w in ("q", "dq", "dq2")]
+    + ["dpsi_neohookean_dF", "d2psi_neohookean_dF2", "d2psi_stvk_dF2"]
 )
 
 
@@ -83,3 +84,13 @@ def test_valid_call_without_gpu_reports_no_device():
     with pytest.raises(bg.BartelsError) as ei:
         mex.call("linear_tetmesh_arap_q", *_tet_args()[:5], _tet_args()[5][:, :1])  # ARAP: one column is fine
     assert ei.value.status == _lib.E_NO_DEVICE
+
+
+def test_pointwise_gateways_validate_shapes():
+    E = np.ones((4, 4))
+    with pytest.raises(bg.BartelsError) as ei:
+        mex.call("d2psi_neohookean_dF2", E, np.zeros((3, 9)), np.ones((4, 2)))
+    assert "F" in str(ei.value)
+    with pytest.raises(bg.BartelsError) as ei:
+        mex.call("dpsi_neohookean_dF", E, np.zeros((4, 9)), np.ones((4, 1)))
+    assert "params" in str(ei.value)
