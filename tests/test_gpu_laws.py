@@ -78,7 +78,7 @@ def test_hessian_gateways_block_diagonal(oracle, routine, model):
     E = np.arange(28, dtype=float).reshape(7, 4) + 1
     H = mex.call(routine, E, flat, p)
     assert isinstance(H, sp.csc_matrix) and H.shape == (63, 63) and H.nnz == 7 * 81
-    ref = sp.block_diag([oracle.d2psi(model, F[t], p[t]) for t in range(7)], format="csc")
+    ref = sp.block_diag([sp.coo_matrix(oracle.d2psi(model, F[t], p[t])) for t in range(7)], format="csc")
     assert np.array_equal(H.indptr, ref.indptr) and np.array_equal(H.indices, ref.indices)
     assert np.abs(H.data - ref.data).max() <= 1e-11 * np.abs(ref.data).max()
 
