@@ -195,6 +195,43 @@ BARTELS_SIM_MODEL(arap, BARTELS_ARAP)
 BARTELS_SIM_MODEL(linear_elasticity, BARTELS_LINEAR_ELASTICITY)
 #undef BARTELS_SIM_MODEL
 
+// ------------------------------------------------------------ pointwise laws --
+// psi_<law>_F, dpsi_<law>_dF, d2psi_<law>_dF2 (include/psi_neohookean_F.h,
+// include/dpsi_neohookean_dF.h, include/d2psi_neohookean_dF2.h and the StVK
+// siblings): F a 3x3 column-major dense type, params 2 contiguous values; dw
+// becomes 9 x 1 (dpsi/dF in the column-major flatten of F), ddw 9 x 9. Each
+// call is one device round trip; bartels_pointwise_laws takes a batch.
+namespace detail {
+template <class MF, class MP>
+void pointwise(int model, const MF &F, const MP &params, double *psi, double *dpsi, double *d2psi) {
+  if (F.rows() != 3 || F.cols() != 3 || (int)(params.rows() * params.cols()) < 2)
+    throw Error(BARTELS_E_INVALID_ARG, "pointwise law: F must be 3 x 3 and params hold 2 values");
+  check(bartels_pointwise_laws(context(), model, 1, F.data(), params.data(), psi, dpsi, d2psi),
+        "bartels_pointwise_laws");
+}
+}  // namespace detail
+
+#define BARTELS_SIM_LAW(name, id)                                                  \
+  template <class MF, class MP>                                                   \
+  double psi_##name##_F(const MF &F, const MP &params) {                          \
+    double e = 0.0;                                                               \
+    detail::pointwise(id, F, params, &e, nullptr, nullptr);                       \
+    return e;                                                                     \
+  }                                                                               \
+  template <class MG, class MF, class MP>                                         \
+  void dpsi_##name##_dF(MG &dw, const MF &F, const MP &params) {                  \
+    dw.resize(9, 1);                                                              \
+    detail::pointwise(id, F, params, nullptr, dw.data(), nullptr);                \
+  }                                                                               \
+  template <class MH, class MF, class MP>                                         \
+  void d2psi_##name##_dF2(MH &ddw, const MF &F, const MP &params) {               \
+    ddw.resize(9, 9);                                                             \
+    detail::pointwise(id, F, params, nullptr, nullptr, ddw.data());               \
+  }
+BARTELS_SIM_LAW(neohookean, BARTELS_NEOHOOKEAN)
+BARTELS_SIM_LAW(stvk, BARTELS_STVK)
+#undef BARTELS_SIM_LAW
+
 // ----------------------------------------------------------- triangle meshes --
 namespace detail {
 template <class MV, class ME>

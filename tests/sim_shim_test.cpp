@@ -1,7 +1,8 @@
 // C++ caller of the sim:: layer (include/bartels_sim.hpp) written the way a
 // user of the reference's headers would: builds a 2x2x2 Kuhn cube, evaluates
 // q / dq / dq2 (with simple_psd_fix), mass, force, the constraint matrix, a
-// search direction and a line search, and checks them against each other.
+// search direction, a line search and the pointwise laws, and checks them
+// against each other.
 // Prints "sim shim ok" and returns 0 on success.
 #include <cmath>
 #include <cstdio>
@@ -16,6 +17,13 @@
       return 1;                                                      \
     }                                                                \
   } while (0)
+
+static sim::VectorXd params2_stvk(double lam, double mu) {
+  sim::VectorXd p(2, 1);
+  p(0) = lam;
+  p(1) = mu;
+  return p;
+}
 
 int main() {
   const int n = 2, m = n + 1;
@@ -152,6 +160,33 @@ int main() {
     for (int v = 0; v < nV; ++v)
       for (int d = 0; d < 3; ++d)
         REQUIRE(std::fabs(g1(3 * (nV - 1 - v) + d) - g(3 * v + d)) <= 1e-9 * (std::fabs(g(3 * v + d)) + 1.0));
+  }
+  // pointwise laws (include/dpsi_neohookean_dF.h, include/d2psi_stvk_dF2.h):
+  // dpsi against central differences of psi, d2psi against those of dpsi
+  {
+    sim::MatrixXd F(3, 3);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) F(i, j) = (i == j ? 1.0 : 0.0) + 0.05 * std::sin(3.0 * i + 5.0 * j + 1.0);
+    sim::VectorXd p2(2, 1);
+    p2(0) = 0.5 * mu;
+    p2(1) = 0.5 * lam;
+    sim::VectorXd dw;
+    sim::dpsi_neohookean_dF(dw, F, p2);
+    sim::MatrixXd ddw;
+    sim::d2psi_stvk_dF2(ddw, F, params2_stvk(lam, mu));
+    REQUIRE(dw.rows() == 9 && ddw.rows() == 9 && ddw.cols() == 9);
+    const double h = 1e-6;
+    for (int r = 0; r < 9; ++r) {
+      sim::MatrixXd Fp = F, Fm = F;
+      Fp.data()[r] += h;
+      Fm.data()[r] -= h;
+      const double fd = (sim::psi_neohookean_F(Fp, p2) - sim::psi_neohookean_F(Fm, p2)) / (2 * h);
+      REQUIRE(std::fabs(fd - dw(r)) <= 1e-6 * mu);
+      sim::VectorXd gp, gm;
+      sim::dpsi_stvk_dF(gp, Fp, params2_stvk(lam, mu));
+      sim::dpsi_stvk_dF(gm, Fm, params2_stvk(lam, mu));
+      for (int c = 0; c < 9; ++c) REQUIRE(std::fabs((gp(c) - gm(c)) / (2 * h) - ddw(c, r)) <= 1e-6 * (lam + mu));
+    }
   }
   // the reference's 2D case (tests/test_constitutive_model.cpp:107-135): one triangle at rest
   {
