@@ -125,6 +125,8 @@ SIGNATURES = [
     ("bartels_tri3dmesh_dphi_dX", C.c_int, [_P, C.c_int, _D, C.c_int, _I, _D, _D]),
     ("bartels_tri3dmesh_stvk_dq2", C.c_int, [_P, _P, _D, _D, _D, _D, _D, _D, _D, C.c_int, C.c_double, _D]),
     ("bartels_pointwise_laws", C.c_int, [_P, C.c_int, C.c_int, _D, _D, _D, _D, _D]),
+    ("bartels_tetmesh_q_d", C.c_int, [_P, _P, C.c_int, _P, _P]),
+    ("bartels_tetmesh_dq_d", C.c_int, [_P, _P, C.c_int, _P, _P]),
     ("bartels_mex_routine_count", C.c_int, []),
     ("bartels_mex_routine_name", C.c_char_p, [C.c_int]),
     ("bartels_mex_release", None, []),

@@ -580,6 +580,20 @@ int bartels_newton_advance_implicit_euler_d(bartels_ctx ctx, bartels_mesh_plan p
   return advance_implicit_euler(ctx, plan, dt, v_d);
 }
 
+int bartels_tetmesh_q_d(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q_d, double *energy_d) {
+  BT_CHECK(check_plan(ctx, plan));
+  if (!valid_model(model) || !q_d || !energy_d) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  ObjectiveDev obj;
+  return energy(ctx, plan, model, obj, q_d, energy_d);
+}
+
+int bartels_tetmesh_dq_d(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q_d, double *g_d) {
+  BT_CHECK(check_plan(ctx, plan));
+  if (!valid_model(model) || !q_d || !g_d) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  ObjectiveDev obj;
+  return gradient(ctx, plan, model, obj, q_d, g_d);
+}
+
 int bartels_tetmesh_dq_noalloc_d(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q_d,
                                  double *g_d) {
   BT_CHECK(check_plan(ctx, plan));

@@ -418,6 +418,16 @@ int bartels_plan_spmv_d(bartels_ctx ctx, bartels_mesh_plan plan, const float *va
  * q_base += dt * v, x_hat = v (device v_d, 3nV). */
 int bartels_newton_advance_implicit_euler_d(bartels_ctx ctx, bartels_mesh_plan plan, double dt, const double *v_d);
 
+/* Device-pointer forms of bartels_tetmesh_q / bartels_tetmesh_dq with the
+ * plan's element data (bartels_plan_set_element_data; for LINEAR_ELASTICITY
+ * the stored params are the Lame pair): q_d 3nV device doubles; the energy goes
+ * to the device scalar energy_d, the gradient to device g_d (3nV). Enqueued on
+ * the context's stream without a host synchronisation, so no finiteness check
+ * (the host forms return BARTELS_E_NONFINITE). Same kernels and summation
+ * order as the host forms: identical results. */
+int bartels_tetmesh_q_d(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q_d, double *energy_d);
+int bartels_tetmesh_dq_d(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q_d, double *g_d);
+
 /* ------------------------------------------------- allocation-free variant -- */
 /* Gradient of the elastic energy (as bartels_tetmesh_dq, with the plan's
  * element data) at device positions q_d (3nV doubles) into device g_d (3nV),
