@@ -13,8 +13,8 @@ converges only linearly here: the PSD projection is active at the compressed
 equilibrium, so the tolerance and a 40-iteration cap are set for that). Each Newton system is solved by PCG to 1e-8
 relative residual with block-Jacobi and with the learned factor (block-Jacobi
 as fallback). Reported: Newton and PCG iteration counts, fallbacks, time, and
-the energy and gradient of the final state against the FP64 CPU restatement.
-Synthetic, seeded inputs.
+the energy of the final state (tests/test_gpu_stress.py checks the final
+state against the FP64 CPU restatement). Synthetic, seeded inputs.
 """
 from __future__ import annotations
 
@@ -93,17 +93,9 @@ def run(prob, precond, net=None, steps=10, compression=0.5, gradient_tol=1e-5, m
         tot["fallbacks"] += rep.precond_fallbacks
         tot["pcg_failures"] += rep.pcg_failures
         tot["seconds"] += dt
-    # final state: energy and gradient against the FP64 CPU restatement
-    from oracle import oracle as o
-    dphi, vol = o.dphi_dX(V, E), o.volume(V, E)
-    qf = q.ravel()
-    e_gpu = plan.q("neohookean", qf, dphi, vol, prob["params"])
-    g_gpu = plan.dq("neohookean", qf, dphi, vol, prob["params"])
-    e_ref = o.tetmesh_q("neohookean", E, qf, dphi, vol, prob["params"])
-    g_ref = o.tetmesh_dq("neohookean", len(V), E, qf, dphi, vol, prob["params"])
-    tot.update(energy=e_gpu, energy_rel_err=abs(e_gpu - e_ref) / abs(e_ref),
-               gradient_rel_err=float(np.linalg.norm(g_gpu - g_ref) / np.linalg.norm(g_ref)),
-               pcg_per_newton=tot["pcg"] / max(tot["newton"], 1))
+    # final state (FP64 energy; its check against the FP64 CPU restatement is
+    # tests/test_gpu_stress.py)
+    tot.update(energy=plan.q("neohookean", q.ravel()), pcg_per_newton=tot["pcg"] / max(tot["newton"], 1))
     plan.close()
     return rows, tot, q
 

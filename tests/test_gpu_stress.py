@@ -9,7 +9,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def test_stress_case_small():
+def test_stress_case_small(oracle):
     pytest.importorskip("torch")
     import bartels_gb300 as bg
     from bartels_gb300 import lpcg, stress_case
@@ -21,7 +21,16 @@ def test_stress_case_small():
         rows, tot, q = stress_case.run(prob, pc, net, steps=3, compression=0.15, gradient_tol=1e-5, max_newton=40,
                                        log=lambda s: None)
         assert all(r["converged"] for r in rows), rows
-        assert tot["energy_rel_err"] < 1e-10 and tot["gradient_rel_err"] < 1e-9, tot
+        # the final state's FP64 energy and gradient against the restatement
+        V, E, params, qf = prob["V"], prob["E"], prob["params"], q.ravel()
+        dphi, vol = oracle.dphi_dX(V, E), oracle.volume(V, E)
+        plan = bg.MeshPlan(V, E)
+        e, g = plan.q("neohookean", qf, dphi, vol, params), plan.dq("neohookean", qf, dphi, vol, params)
+        e_ref = oracle.tetmesh_q("neohookean", E, qf, dphi, vol, params)
+        g_ref = oracle.tetmesh_dq("neohookean", len(V), E, qf, dphi, vol, params)
+        assert abs(e - e_ref) < 1e-10 * abs(e_ref) and abs(tot["energy"] - e_ref) < 1e-10 * abs(e_ref)
+        assert np.linalg.norm(g - g_ref) < 1e-9 * np.linalg.norm(g_ref)
+        plan.close()
         res[pc] = (tot, q)
     # same equilibrium from both solvers
     qa, qb = res["jacobi"][1], res["learned"][1]
