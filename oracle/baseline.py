@@ -1,6 +1,6 @@
 """ctypes front end of the OpenMP FP64 CPU baseline (oracle_baseline.cpp).
 
-TEST / BASELINE INFRASTRUCTURE ONLY: bench.py times it on the host cores as
+Test infrastructure and CPU timing only: bench.py times it on the host cores as
 the reference arm and the cpu_baseline field; the GPU library never uses it.
 """
 from __future__ import annotations

@@ -9,7 +9,7 @@
 // class of the reference's Eigen::SelfAdjointEigenSolver. ob_faithful_dq2 is the
 // reference's own structure on one thread (triplets, sort / compress).
 //
-// TEST / BASELINE INFRASTRUCTURE ONLY: timed by bench.py on the host cores and
+// Test infrastructure and CPU timing only: timed by bench.py on the host cores and
 // never used by the GPU library.
 #include <omp.h>
 
