@@ -124,3 +124,15 @@ def build_sim_shim_test():
 
 def test_sim_shim_compiles():
     assert os.path.exists(build_sim_shim_test())
+
+
+def test_sim_plan_cache_keys_on_content_and_evicts():
+    """The sim:: layer's plan cache with stand-in plans (no device needed)."""
+    import subprocess
+    out_dir = os.path.join(ROOT, "tests", "_build")
+    os.makedirs(out_dir, exist_ok=True)
+    exe = os.path.join(out_dir, "sim_plan_cache_test")
+    subprocess.check_call(["g++", "-std=c++17", "-O1", "-Wall", os.path.join(ROOT, "tests", "sim_plan_cache_test.cpp"),
+                           "-I", os.path.join(ROOT, "include"), "-o", exe])
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "plan cache ok" in r.stdout, r.stderr
