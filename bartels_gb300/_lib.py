@@ -126,6 +126,8 @@ SIGNATURES = [
     ("bartels_tri3dmesh_stvk_dq2", C.c_int, [_P, _P, _D, _D, _D, _D, _D, _D, _D, C.c_int, C.c_double, _D]),
     ("bartels_pointwise_laws", C.c_int, [_P, C.c_int, C.c_int, _D, _D, _D, _D, _D]),
     ("bartels_tetmesh_q_d", C.c_int, [_P, _P, C.c_int, _P, _P]),
+    ("bartels_plan_assemble_matrix", C.c_int, [_P, _P, _D, _D]),
+    ("bartels_plan_assemble_vector", C.c_int, [_P, _P, _D, _D]),
     ("bartels_tetmesh_dq_d", C.c_int, [_P, _P, C.c_int, _P, _P]),
     ("bartels_mex_routine_count", C.c_int, []),
     ("bartels_mex_routine_name", C.c_char_p, [C.c_int]),

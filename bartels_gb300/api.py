@@ -198,6 +198,24 @@ class MeshPlan:
               "bartels_tetmesh_mass_matrix")
         return self.csr(vals)
 
+    def assemble_matrix(self, Ke):
+        """sim::assemble of caller-computed element matrices: Ke (nT, 12, 12),
+        rows / columns 3a + k -> scipy CSR in the plan's pattern (FP64, summed in
+        tet order as setFromTriplets sums the reference's triplets)."""
+        K = np.ascontiguousarray(np.asarray(Ke, np.float64).reshape(self.nT, 12, 12).transpose(0, 2, 1))
+        vals = np.zeros(self.nnz)
+        check(lib().bartels_plan_assemble_matrix(self.ctx.handle, self.handle, _dptr(K), _dptr(vals)),
+              "bartels_plan_assemble_matrix")
+        return self.csr(vals)
+
+    def assemble_vector(self, ge):
+        """sim::assemble of caller-computed element vectors ge (nT, 12) -> (3 nV,)."""
+        G = _f64(np.asarray(ge).reshape(self.nT, 12))
+        g = np.zeros(3 * self.nV)
+        check(lib().bartels_plan_assemble_vector(self.ctx.handle, self.handle, _dptr(G), _dptr(g)),
+              "bartels_plan_assemble_vector")
+        return g
+
     def const_ext_force(self, volume, traction):
         v = None if volume is None else _f64(np.ravel(volume))
         t = _f64(np.ravel(traction))

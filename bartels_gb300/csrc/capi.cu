@@ -17,6 +17,8 @@ int launch_prep_u(bartels_ctx ctx, bartels_mesh_plan plan, const double *x, cons
                   bool displacement, float4 *u);
 int launch_hess(bartels_ctx ctx, bartels_mesh_plan plan, int model, int psd_mode, const float4 *u, int add_identity,
                 float cK, float cM, float tol, int flags, float *values);
+int assemble_elements64(bartels_ctx ctx, bartels_mesh_plan plan, const double *Ke, double *values);
+int assemble_vector64(bartels_ctx ctx, bartels_mesh_plan plan, const double *ge, double *g);
 int launch_mass64(bartels_ctx ctx, bartels_mesh_plan plan, const double *density, const double *vol,
                   double *values);
 int newton_iterate(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params &p, double *x,
@@ -354,6 +356,32 @@ int bartels_tetmesh_mass_matrix(bartels_ctx ctx, bartels_mesh_plan plan, const d
   BT_CHECK(launch_mass64(ctx, plan, plan->density, plan->vol, ctx->stage_d.as<double>()));
   (void)nT;
   BT_CUDA(cudaMemcpyAsync(csr_values, ctx->stage_d.p, sizeof(double) * nnz, cudaMemcpyDeviceToHost, ctx->stream));
+  BT_CUDA(cudaStreamSynchronize(ctx->stream));
+  return BARTELS_OK;
+}
+
+int bartels_plan_assemble_matrix(bartels_ctx ctx, bartels_mesh_plan plan, const double *Ke, double *csr_values) {
+  BT_CHECK(check_plan(ctx, plan));
+  if (!Ke || !csr_values) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  const int64_t nnz = 9 * plan->nnzb;
+  double *dK;
+  BT_CHECK(stage_vec(ctx, ctx->stage_e, Ke, 144 * (size_t)plan->nT, &dK));
+  BT_CHECK(ctx->stage_d.ensure(sizeof(double) * nnz));
+  BT_CHECK(assemble_elements64(ctx, plan, dK, ctx->stage_d.as<double>()));
+  BT_CUDA(cudaMemcpyAsync(csr_values, ctx->stage_d.p, sizeof(double) * nnz, cudaMemcpyDeviceToHost, ctx->stream));
+  BT_CUDA(cudaStreamSynchronize(ctx->stream));
+  return BARTELS_OK;
+}
+
+int bartels_plan_assemble_vector(bartels_ctx ctx, bartels_mesh_plan plan, const double *ge, double *g) {
+  BT_CHECK(check_plan(ctx, plan));
+  if (!ge || !g) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  const size_t n = 3 * (size_t)plan->nV;
+  double *dge;
+  BT_CHECK(stage_vec(ctx, ctx->stage_e, ge, 12 * (size_t)plan->nT, &dge));
+  BT_CHECK(plan->w_vec.ensure(sizeof(double) * (n + 16)));
+  BT_CHECK(assemble_vector64(ctx, plan, dge, plan->w_vec.as<double>()));
+  BT_CUDA(cudaMemcpyAsync(g, plan->w_vec.p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
   BT_CUDA(cudaStreamSynchronize(ctx->stream));
   return BARTELS_OK;
 }

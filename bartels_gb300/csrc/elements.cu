@@ -657,6 +657,35 @@ __global__ void k_mass64(int nV, const int *__restrict__ brp, const int *__restr
   }
 }
 
+// assemble (src/assemble.cpp:57-94) of caller-supplied element matrices: Ke
+// holds 144 doubles per tet (column-major 12 x 12, row / column 3a + k for
+// local vertex a, coordinate k). Each entry of v's rows is summed over its
+// tets in tet order from zero, the order in which setFromTriplets sums the
+// reference's duplicate triplets, so the FP64 result is the reference's.
+__global__ void k_assemble_elem64(int nV, const int *__restrict__ brp, const int *__restrict__ inc_ptr,
+                                  const int *__restrict__ inc_tet, const uint32_t *__restrict__ inc_pos,
+                                  const double *__restrict__ Ke, double *__restrict__ values) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nV; v += gridDim.x * blockDim.x) {
+    const int rb = brp[v], rs = 3 * (brp[v + 1] - rb);
+    double *row = values + 9ll * rb;
+    for (int i = 0; i < 3 * rs; ++i) row[i] = 0.0;
+    for (int k = inc_ptr[v]; k < inc_ptr[v + 1]; ++k) {
+      const int ta = inc_tet[k];
+      const double *K = Ke + 144ll * (ta >> 2);
+      const int a = ta & 3;
+      const uint32_t pos = inc_pos[k];
+      for (int b = 0; b < 4; ++b) {
+        const int j = (pos >> (8 * b)) & 255;
+        for (int kk = 0; kk < 3; ++kk)
+          for (int ll = 0; ll < 3; ++ll) {
+            double *p = row + kk * rs + 3 * j + ll;
+            *p = __dadd_rn(*p, K[(3 * a + kk) + 12 * (3 * b + ll)]);
+          }
+      }
+    }
+  }
+}
+
 // linear_tetmesh_const_ext_force: f_v = sum over tets (tet order) of
 // traction * (0.25 vol), as src/linear_tet_const_ext_force.cpp:8-9 + :126.
 __global__ void k_force(int nV, const int *__restrict__ inc_ptr, const int *__restrict__ inc_tet,
@@ -869,6 +898,20 @@ int launch_mass64(bartels_ctx ctx, bartels_mesh_plan plan, const double *density
                   double *values) {
   BT_LAUNCH(ctx, k_mass64, grid_for(ctx, plan->nV, 128), 128, 0, plan->nV, plan->brp, plan->inc_ptr, plan->inc_tet,
             plan->inc_pos, density, vol, values);
+  return BARTELS_OK;
+}
+
+int assemble_elements64(bartels_ctx ctx, bartels_mesh_plan plan, const double *Ke, double *values) {
+  BT_LAUNCH(ctx, k_assemble_elem64, grid_for(ctx, plan->nV, 128), 128, 0, plan->nV, plan->brp, plan->inc_ptr,
+            plan->inc_tet, plan->inc_pos, Ke, values);
+  return BARTELS_OK;
+}
+
+// vector assemble (src/assemble.cpp:100-132): per-tet 12-vectors ge (entry
+// 3a + k) summed per vertex in tet order
+int assemble_vector64(bartels_ctx ctx, bartels_mesh_plan plan, const double *ge, double *g) {
+  BT_LAUNCH(ctx, k_grad_gather, grid_for(ctx, plan->nV, 256), 256, 0, plan->nV, plan->inc_ptr, plan->inc_tet, ge,
+            nullptr, 0.0, nullptr, g);
   return BARTELS_OK;
 }
 

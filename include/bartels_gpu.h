@@ -210,6 +210,17 @@ int bartels_pointwise_laws(bartels_ctx ctx, int model, int n, const double *F, c
  * src/linear_tet_mass_matrix.cpp:12-42): values in the plan's CSR order. */
 int bartels_tetmesh_mass_matrix(bartels_ctx ctx, bartels_mesh_plan plan, const double *density, const double *vol,
                                 double *csr_values);
+/* assemble (src/assemble.cpp:36-97), the reference's generic assembler, for
+ * element quantities the caller computed (its element functor cannot run on
+ * the device): Ke holds nT blocks of 144 doubles, block t the column-major
+ * 12 x 12 with row / column 3a + k for local vertex a and coordinate k; the
+ * values are summed per CSR entry in tet order, the order in which
+ * setFromTriplets sums the reference's duplicate triplets, so the FP64 result
+ * is the reference's bit for bit. Output in the plan's CSR order. */
+int bartels_plan_assemble_matrix(bartels_ctx ctx, bartels_mesh_plan plan, const double *Ke, double *csr_values);
+/* Vector form (src/assemble.cpp:100-132): ge nT x 12 element-major (entry
+ * 12 t + 3a + k), summed per vertex in tet order into g (3nV). */
+int bartels_plan_assemble_vector(bartels_ctx ctx, bartels_mesh_plan plan, const double *ge, double *g);
 /* linear_tetmesh_const_ext_force, src/linear_tetmesh_const_ext_force.cpp:5-18:
  * f_v = sum over tets of v of vol/4 * traction. */
 int bartels_tetmesh_const_ext_force(bartels_ctx ctx, bartels_mesh_plan plan, const double *vol,
