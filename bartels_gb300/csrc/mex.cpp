@@ -394,7 +394,7 @@ int run(const Routine &R, int nrhs, const bartels_mx *prhs, bartels_mx_alloc all
     return bartels_tri3dmesh_dphi_dX(ctx, nV, prhs[0].pr, nT, E.data(), out, nullptr);
   }
   if (nT == 0) return fail(BARTELS_E_INVALID_ARG, "E: empty mesh");
-  Entry *e;
+  Entry *e = nullptr;
   if ((st = get_plan(R.fam, nV, prhs[0], nT, E, &e)) != BARTELS_OK) return st;
   const int64_t nnz = e->rp[e->n];
   if (R.op == MASS) {

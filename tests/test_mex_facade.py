@@ -94,3 +94,21 @@ def test_pointwise_gateways_validate_shapes():
     with pytest.raises(bg.BartelsError) as ei:
         mex.call("dpsi_neohookean_dF", E, np.zeros((4, 9)), np.ones((4, 1)))
     assert "params" in str(ei.value)
+
+
+def test_facade_layout_with_a_stand_in_abi():
+    """mex.cpp linked against a stand-in C ABI with unsymmetric values
+    (tests/mex_fake_abi.cpp): compressed columns carry H(i, j), q reaches the
+    ABI unshifted, dense and block-diagonal layouts, index checks, the plan
+    cache and its eviction."""
+    import os
+    import subprocess
+    from conftest import ROOT
+    out_dir = os.path.join(ROOT, "tests", "_build")
+    os.makedirs(out_dir, exist_ok=True)
+    exe = os.path.join(out_dir, "mex_fake_abi")
+    subprocess.check_call(["g++", "-std=c++17", "-O1", os.path.join(ROOT, "tests", "mex_fake_abi.cpp"),
+                           os.path.join(ROOT, "bartels_gb300", "csrc", "mex.cpp"), "-I", os.path.join(ROOT, "include"),
+                           "-o", exe])
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "mex facade ok" in r.stdout, r.stderr
