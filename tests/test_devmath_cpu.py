@@ -252,3 +252,26 @@ def test_fp32_rest_and_rigid_elements_take_the_fast_path(oracle, model):
     K, slow = lib_element(model, x, dphi, vol, PARAMS[model], 1e-6, False, np.float32)
     assert slow == 1 or model == "stvk"
     assert np.linalg.norm(K - K_ref) <= 2e-5 * np.linalg.norm(K_ref)
+
+
+@pytest.mark.parametrize("model", ["neohookean", "neohookean_isochoric", "stvk", "corotational", "arap"])
+def test_known_answers_rest_and_rigid_rotations(oracle, model):
+    """psi = 0 and dpsi/dF = 0 at F = I and at any rotation F = R, for every
+    hyperelastic law, in the library's math (FP64, on the host) and the oracle."""
+    L = devmath()
+    p = PARAMS[model]
+    rng = np.random.default_rng(21)
+    rots = [np.eye(3)]
+    for _ in range(5):
+        Q, _ = np.linalg.qr(rng.standard_normal((3, 3)))
+        rots.append(Q * np.sign(np.linalg.det(Q)))  # proper rotation
+    scale = np.abs(p).max()
+    for R in rots:
+        fv = np.ascontiguousarray(R.ravel(order="F"))
+        pd = np.ascontiguousarray(p, np.float64)
+        e = L.dm_psi_d(MODEL_ID[model], dp(fv), dp(pd))
+        P = np.zeros(9)
+        L.dm_pk1_d(MODEL_ID[model], dp(fv), dp(pd), dp(P))
+        assert abs(e) <= 1e-12 * scale and np.abs(P).max() <= 1e-9 * scale, (model, e, np.abs(P).max())
+        assert abs(oracle.psi(model, R, p)) <= 1e-12 * scale
+        assert np.abs(oracle.dpsi(model, R, p)).max() <= 1e-9 * scale
