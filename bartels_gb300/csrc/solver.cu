@@ -10,6 +10,8 @@
 // reference's backtracking line search (src/linesearch_backtracking_bisection.cpp:17-30)
 // on the device-evaluated FP64 objective, following newtons_method_bisection
 // (include/optimization_gradient_based.h:77-106).
+#include <nvtx3/nvToolsExt.h>
+
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -1157,8 +1159,25 @@ static int read_scalar(bartels_ctx ctx, const double *d, double *h) {
   return BARTELS_OK;
 }
 
+// NVTX range per Newton stage (gradient, Hessian, PCG, line search) for
+// timeline profilers; the range open at a return is closed by the destructor.
+// Without a profiler attached each call is a check of one function pointer.
+struct NvtxStage {
+  bool open = false;
+  void to(const char *name) {
+    if (open) nvtxRangePop();
+    nvtxRangePushA(name);
+    open = true;
+  }
+  ~NvtxStage() {
+    if (open) nvtxRangePop();
+  }
+};
+
 int newton_iterate(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params &p, double *x,
                    double g0_norm, int *done, bartels_newton_report *rep) {
+  NvtxStage stage;
+  stage.to("bartels newton: gradient");
   NewtonWork w;
   BT_CHECK(newton_work(plan, w));
   const int n = 3 * plan->nV;
@@ -1180,6 +1199,7 @@ int newton_iterate(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton
     return BARTELS_OK;
   }
   *done = 0;
+  stage.to("bartels newton: hessian");
   // Hessian H = mass_coeff M + scale^2 K (fused assembly, FP32)
   BT_CHECK(launch_prep_u(ctx, plan, x, plan->q_base, p.scale, plan->dphi_matches_rest, w.u));
   BT_CHECK(launch_hess(ctx, plan, p.model, p.psd_mode, w.u, plan->dphi_matches_rest ? 1 : 0,
@@ -1187,6 +1207,7 @@ int newton_iterate(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton
   BT_CUDA(cudaStreamSynchronize(ctx->stream));
   double t2 = now_s();
   rep->t_hessian += t2 - t1;
+  stage.to("bartels newton: pcg");
   // search direction d = -H^-1 g (src/search_direction_newton_sparse.cpp:12-24)
   BT_LAUNCH(ctx, k_scale_copy, grid_vec(ctx, n), 256, 0, n, -1.0, w.g, w.xt);
   BT_CUDA(cudaMemsetAsync(w.d, 0, sizeof(double) * n, ctx->stream));
@@ -1202,6 +1223,7 @@ int newton_iterate(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton
   double t3 = now_s();
   rep->t_pcg += t3 - t2;
   if (s != BARTELS_OK && s != BARTELS_E_NOT_CONVERGED) return s;
+  stage.to("bartels newton: line search");
   // line search (src/linesearch_backtracking_bisection.cpp:17-30): while
   // f(x + alpha d) > f(x) + c g.d and it < max: alpha *= p. The difference
   // f(x + alpha d) - f(x) is evaluated element by element (energy_diff) so that

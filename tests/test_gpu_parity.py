@@ -362,3 +362,21 @@ def test_generic_assembly_matches_the_reference_bit_for_bit(oracle):
             g_ref[3 * E[t, a]:3 * E[t, a] + 3] += ge[t, 3 * a:3 * a + 3]
     assert np.array_equal(plan.assemble_vector(ge), g_ref)
     plan.close()
+
+
+def test_search_direction_reports_an_iteration_cap(oracle):
+    """A PCG solve stopped by max_iters returns the reference's `false`
+    (BARTELS_E_NOT_CONVERGED underneath) with its residual, not a wrong d."""
+    V, E, q = noisy_cube(4, amp=0.05, seed=8)
+    params = material_params("neohookean", len(E), 2e6, 0.45)
+    dphi, vol = oracle.dphi_dX(V, E), oracle.volume(V, E)
+    K = oracle.tetmesh_dq2("neohookean", len(V), E, q, dphi, vol, params, psd_tol=1e-6)
+    M = oracle.mass_matrix(len(V), E, np.full(len(E), 1000.0), vol)
+    P = oracle.fixed_point_constraint_matrix(len(V), oracle.find_min_vertices(V, 2))
+    H = (P @ (M + 1e-4 * K) @ P.T).tocsr()
+    g = np.random.default_rng(9).standard_normal(H.shape[0])
+    d, ok, rep = bg.search_direction_newton_sparse(g, H, max_iters=3)
+    assert not ok and not rep.converged
+    assert 0 < rep.iterations < 20 and rep.rel_residual > 1e-8
+    d, ok, rep = bg.search_direction_newton_sparse(g, H)
+    assert ok and rep.converged
