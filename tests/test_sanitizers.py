@@ -1,6 +1,7 @@
 """Host code under AddressSanitizer + UndefinedBehaviorSanitizer (leaks
 included): the MATLAB facade against a stand-in C ABI, the sim:: plan cache,
-and the CPU oracle and baseline through every entry point. Any out-of-bounds
+the CPU oracle and baseline through every entry point, and the kernels'
+element math (devmath.cuh) compiled for the host over hard deformations. Any out-of-bounds
 access, use after free, leak or undefined arithmetic fails the run. Skipped
 where the compiler has no sanitizer runtime."""
 import os
@@ -19,6 +20,8 @@ PROGRAMS = {
     "plan_cache": (["tests/sim_plan_cache_test.cpp"], ["-Iinclude"], "plan cache ok"),
     "oracle": (["tests/oracle_sanitize_driver.cpp", "oracle/oracle_capi.cpp", "oracle/oracle_baseline.cpp"],
                ["-Ioracle", "-fopenmp"], "oracle sanitize ok"),
+    "devmath": (["tests/devmath_sanitize_driver.cpp", "tests/devmath_harness.cpp"], ["-Ibartels_gb300/csrc"],
+                "devmath sanitize ok"),
 }
 
 
