@@ -107,3 +107,40 @@ def test_loss_of_block_jacobi_is_log_kaporin():
     nf = 3 * (~g.pinned).sum()
     assert abs(t / nf - 1.0) < 0.05
     assert abs(loss) < 0.05
+
+
+def _factor_matrix(g, G):
+    """Sparse 3nV x 3nV G from its pattern blocks (lower part incl. the diagonal)."""
+    import scipy.sparse as sp
+    rows, cols, vals = [], [], []
+    for p in np.nonzero(g.lower | (g.row == g.bcol))[0]:
+        v, j = g.row[p], g.bcol[p]
+        for k in range(3):
+            for l in range(3):
+                rows.append(3 * v + k)
+                cols.append(3 * j + l)
+                vals.append(G[p, k, l])
+    n = 3 * g.nV
+    return sp.csr_matrix((vals, (rows, cols)), shape=(n, n))
+
+
+def test_shipped_weights_beat_block_jacobi_on_an_unseen_system():
+    """The shipped network (bartels_gb300/weights), evaluated by the restatement
+    with the GPU's BF16 rounding on a cube it was not trained on, gives a factor
+    with a positive diagonal and fewer PCG iterations than block-Jacobi."""
+    from bartels_gb300 import lpcg
+    g, A, Hs, pinned = small_system(8, seed=3)
+    theta = np.load(lpcg.WEIGHTS)["params"].astype(np.float64)
+    assert theta.shape == (sum(int(np.prod(s)) for _, s in L.LAYOUT.values()),) and np.all(np.isfinite(theta))
+    free = np.repeat(~pinned, 3)
+    Hf = Hs[free][:, free]
+    b = np.random.default_rng(5).standard_normal(int(free.sum()))
+    its = {}
+    for name, th in (("learned", theta), ("block_jacobi", lpcg.init_params(0).astype(np.float64))):
+        c = L.forward(g, A, th, bf=True)
+        Gb = L.factor_blocks(g, c)
+        d = np.array([np.diag(Gb[g.dpos[v]]) for v in np.nonzero(~pinned)[0]])
+        assert np.all(d > 0)
+        Gm = _factor_matrix(g, Gb)[free][:, free]
+        its[name] = L.factor_pcg_iterations(Hf, Gm, b)
+    assert its["learned"] < 0.9 * its["block_jacobi"], its
