@@ -63,6 +63,8 @@ static int upload(bartels_ctx ctx, T **dst, const T *src, size_t n) {
 int plan_build(bartels_mesh_plan plan, const double *V, const int *E) {
   bartels_ctx ctx = plan->ctx;
   const int nV = plan->nV, nT = plan->nT;
+  // incidences pack 4 t + a into an int (and count 4 nT of them)
+  if ((int64_t)nT >= (1 << 29)) return fail(BARTELS_E_UNSUPPORTED, "more than 2^29 tets");
   // --- validate and convert layouts
   std::vector<double> X(3 * (size_t)nV);
   for (int v = 0; v < nV; ++v)

@@ -402,6 +402,8 @@ extern "C" {
 int bartels_tri_plan_create(bartels_ctx ctx, int nV, int nT, const int *E, int dim, bartels_tri_plan *out) {
   if (!ctx || !E || !out || nV <= 0 || nT <= 0 || (dim != 2 && dim != 3))
     return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  // incidences pack (tri << 2 | local index) into an int
+  if ((int64_t)nT >= (1 << 29)) return fail(BARTELS_E_UNSUPPORTED, "too many triangles");
   BT_CUDA(cudaSetDevice(ctx->device));
   std::vector<int4> E4(nT);
   for (int t = 0; t < nT; ++t) {
@@ -426,7 +428,6 @@ int bartels_tri_plan_create(bartels_ctx ctx, int nV, int nT, const int *E, int d
     const int id[3] = {E4[t].x, E4[t].y, E4[t].z};
     for (int a = 0; a < 3; ++a) inc[fillp[id[a]]++] = (t << 2) | a;
   }
-  if ((int64_t)nT >= (1 << 29)) return fail(BARTELS_E_UNSUPPORTED, "too many triangles");
   std::vector<int> brp(nV + 1, 0);
   for (int v = 0; v < nV; ++v) {
     std::vector<int> &r = rows[v];
