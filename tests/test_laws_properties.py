@@ -61,3 +61,39 @@ def test_oracle_derivatives_are_centred_differences(oracle, model, entries):
         assert abs(fd - P[r]) <= 1e-5 * (np.abs(P).max() + np.abs(p).max())
         gd = (oracle.dpsi(model, F + D, p) - oracle.dpsi(model, F - D, p)) / (2 * h)
         assert np.abs(gd - H[:, r]).max() <= 1e-5 * (np.abs(H).max() + np.abs(p).max())
+
+
+def _element(model, F, psd, dtype):
+    import ctypes as C
+    L = devmath()
+    dphi9 = np.array([1.0, 0.1, -0.2, 0.05, 1.1, 0.0, -0.1, 0.2, 0.9])
+    pv = PARAMS[model] * (1.0 / 6.0)
+    fv = np.ascontiguousarray(F.ravel(order="F"))
+    if dtype == np.float64:
+        out = np.zeros(144)
+        L.dm_element_hessian_d(MODEL_ID[model], dp(fv), dp(np.ascontiguousarray(pv)), dp(dphi9), 0, int(psd),
+                               C.c_double(1e-6), dp(out))
+    else:
+        Fp = C.POINTER(C.c_float)
+        f32, p32, d32 = (np.ascontiguousarray(a, np.float32) for a in (fv, pv, dphi9))
+        out = np.zeros(144, np.float32)
+        L.dm_element_hessian_f(MODEL_ID[model], f32.ctypes.data_as(Fp), p32.ctypes.data_as(Fp),
+                               d32.ctypes.data_as(Fp), 0, int(psd), C.c_float(1e-6), out.ctypes.data_as(Fp))
+    return out.astype(np.float64)
+
+
+@pytest.mark.parametrize("model", ["neohookean", "stvk", "corotational"])
+@pytest.mark.parametrize("psd", [0, 1])
+@settings(max_examples=60, deadline=None)
+@given(entries=F_ENTRIES)
+def test_fp32_element_hessian_within_the_kernel_bound(model, psd, entries):
+    """The FP32 element Hessian the kernels assemble stays within 1e-5 of the
+    largest entry of the FP64 one (projected or not)."""
+    F = as_F(entries)
+    assume(np.linalg.det(F) >= 0.2)
+    if model == "corotational":
+        s = np.linalg.svd(F, compute_uv=False)
+        assume(np.min(np.abs(np.diff(np.sort(s)))) > 1e-3)
+    K64 = _element(model, F, psd, np.float64)
+    K32 = _element(model, F, psd, np.float32)
+    assert np.abs(K32 - K64).max() <= 1e-5 * np.abs(K64).max()
