@@ -94,7 +94,9 @@ const char *bartels_last_error(void);
 
 /* ---------------------------------------------------------------- context -- */
 /* One context per host thread: a device, a stream, workspace and a pinned
- * staging area. All work is ordered on the context's stream. */
+ * staging area. All work is ordered on the context's stream. No counterpart
+ * in the reference (single-threaded host code, include/EigenTypes.h:133-135
+ * holds its only globals). */
 int bartels_ctx_create(int device, bartels_ctx *out);
 /* Destroy every plan created on ctx before destroying ctx. */
 int bartels_ctx_destroy(bartels_ctx ctx);
@@ -115,7 +117,9 @@ int bartels_tetmesh_volume(bartels_ctx ctx, int nV, const double *V, int nT, con
 /* ------------------------------------------------------------------ plan --- */
 /* A mesh plan is built once from (V, E): rest data, per-tet records, the
  * vertex->tet incidence lists in tet order, the block CSR pattern and the
- * element->CSR scatter positions. Plans are immutable after creation apart from
+ * element->CSR scatter positions. The reference has no counterpart: it
+ * rebuilds its triplets and pattern in every assemble call
+ * (src/assemble.cpp:57-94); the plan keeps that pattern, bit-exact. Plans are immutable after creation apart from
  * the element data set with bartels_plan_set_element_data. */
 int bartels_plan_create(bartels_ctx ctx, int nV, const double *V, int nT, const int *E, bartels_mesh_plan *out);
 int bartels_plan_destroy(bartels_mesh_plan plan);
@@ -150,7 +154,10 @@ int bartels_tetmesh_dq2(bartels_ctx ctx, bartels_mesh_plan plan, int model, cons
                         const double *vol, const double *params, int psd_mode, double psd_tol, int flags,
                         double *csr_values);
 
-/* Named drop-ins (same as the generic calls with the model fixed). */
+/* Named drop-ins, the reference's linear_tetmesh_<model>_{q,dq,dq2}
+ * (include/linear_tetmesh_neohookean_q.h:13-18, _dq.h:13-17, _dq2.h:14-21 and the
+ * StVK, corotational, ARAP and linear-elasticity siblings): the generic calls
+ * with the model fixed. */
 int bartels_tetmesh_neohookean_q(bartels_ctx, bartels_mesh_plan, const double *q, const double *dphidX,
                                  const double *vol, const double *params, double *energy);
 int bartels_tetmesh_neohookean_dq(bartels_ctx, bartels_mesh_plan, const double *q, const double *dphidX,
@@ -260,7 +267,7 @@ void bartels_pcg_default_params(bartels_pcg_params *p);
 /* search_direction_newton_sparse, src/search_direction_newton_sparse.cpp:5-26:
  * d = -H^{-1} g for an SPD H given as CSR (host arrays, nnz values double).
  * Replaces the reference's Eigen::SparseLU with block-Jacobi PCG (FP32 with
- * FP64 residual refinement). n must be a multiple of 3 for the 3x3 block
+ * float-float residual refinement). n must be a multiple of 3 for the 3x3 block
  * preconditioner (falls back to scalar Jacobi otherwise). Returns
  * BARTELS_E_NOT_CONVERGED where the reference's solver.info() != Success. */
 int bartels_search_direction_newton_sparse(bartels_ctx ctx, int n, const int *row_ptr, const int *col_idx,
@@ -333,7 +340,10 @@ void bartels_newton_default_params(bartels_newton_params *p);
  * q_base (3nV), x_hat (3nV), f_ext (3nV), pinned (nV bytes, 1 = vertex fixed). */
 int bartels_newton_set_problem(bartels_mesh_plan plan, const double *q_base, const double *x_hat,
                                const double *f_ext, const unsigned char *pinned);
-/* Solve from x (host, 3nV, in/out). Host buffers, copies counted in the time. */
+/* newtons_method_bisection (include/optimization_gradient_based.h:43-110) on the
+ * objective above: gradient test (relative, or the reference's absolute one),
+ * Hessian, search direction, line search, until converged or max_iterations.
+ * Solve from x (host, 3nV, in/out). Host buffers, copies counted in the time. */
 int bartels_newton_solve(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params *params,
                          double *x, bartels_newton_report *report);
 /* Device-resident variant: x_d is a device pointer (3nV doubles). */
@@ -429,8 +439,9 @@ int bartels_plan_spmv_d(bartels_ctx ctx, bartels_mesh_plan plan, const float *va
  * q_base += dt * v, x_hat = v (device v_d, 3nV). */
 int bartels_newton_advance_implicit_euler_d(bartels_ctx ctx, bartels_mesh_plan plan, double dt, const double *v_d);
 
-/* Device-pointer forms of bartels_tetmesh_q / bartels_tetmesh_dq with the
- * plan's element data (bartels_plan_set_element_data; for LINEAR_ELASTICITY
+/* Device-pointer forms of bartels_tetmesh_q / bartels_tetmesh_dq
+ * (linear_tetmesh_<model>_q / _dq, e.g. src/linear_tetmesh_neohookean_q.cpp:10-24,
+ * src/linear_tetmesh_neohookean_dq.cpp:5-22) with the plan's element data (bartels_plan_set_element_data; for LINEAR_ELASTICITY
  * the stored params are the Lame pair): q_d 3nV device doubles; the energy goes
  * to the device scalar energy_d, the gradient to device g_d (3nV). Enqueued on
  * the context's stream without a host synchronisation, so no finiteness check
