@@ -74,7 +74,7 @@ def lame_from_young(E, nu):
 
 def material_params(model: str, nT: int, young: float, nu: float):
     """Per-tet params in the reference's convention: Neo-Hookean (mu/2, lambda/2)
-    (README / matlab/examples/test_tet_materials.m:64), StVK and corotational (lambda, mu),
+    (the reference's README.md:50, matlab/examples/test_tet_materials.m:64), StVK and corotational (lambda, mu),
     ARAP (lambda/2, mu) with k = lambda/2 in column 0 (matlab/examples/test_tet_materials.m:80),
     linear elasticity (Young's modulus, Poisson ratio) (src/d2psi_linear_elasticity_de2.cpp:10-11)."""
     lam, mu = lame_from_young(young, nu)
