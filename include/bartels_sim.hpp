@@ -5,9 +5,8 @@
 // Matrix arguments are any column-major dense type exposing data(), rows(),
 // cols() (and resize(r, c) for outputs): Eigen::MatrixXd / MatrixXi /
 // VectorXd work as-is, as do the small sim::Dense<T> types below. Sparse
-// outputs are sim::SparseMatrix (compressed arrays; the pattern is symmetric,
-// so outer_ptr/inner_idx read as CSR or CSC) and can be wrapped with
-// Eigen::Map<Eigen::SparseMatrix<double>>.
+// outputs are sim::SparseMatrix (compressed columns, Eigen's default layout)
+// and can be wrapped with Eigen::Map<Eigen::SparseMatrix<double>>.
 //
 // Mesh plans are cached by content (E, and V for tets, compared exactly; the
 // four most recently used are kept), so repeated calls on one mesh reuse its
@@ -66,6 +65,10 @@ using MatrixXd = Dense<double>;
 using MatrixXi = Dense<int>;
 using VectorXd = Dense<double>;
 
+// Compressed-column storage, Eigen::SparseMatrix's default layout:
+// outer_ptr (n_cols + 1) indexes columns, inner_idx holds row indices. The
+// Hessians and mass matrices have a symmetric pattern, so the same arrays also
+// read as compressed rows; the constraint matrix P is rectangular.
 struct SparseMatrix {
   int n_rows = 0, n_cols = 0;
   std::vector<int> outer_ptr, inner_idx;
@@ -133,6 +136,23 @@ void copy_pattern(SparseMatrix &S, bartels_mesh_plan p, int n, int64_t nnz) {
   S.inner_idx.resize(nnz);
   check(bartels_plan_csr_pattern(p, S.outer_ptr.data(), S.inner_idx.data()), "bartels_plan_csr_pattern");
 }
+// The library returns values in row order (entry (i, j) of row i). For a
+// structurally symmetric pattern the same index arrays describe the columns;
+// this moves each value to its mirror position so that the stored entry at
+// (row inner_idx[k], column c) is H(inner_idx[k], c), as in the reference's
+// column-major Eigen matrix (the two differ by FP32 rounding only).
+inline void row_values_to_columns(SparseMatrix &S) {
+  std::vector<double> col_vals(S.values.size());
+  for (int r = 0; r < S.n_rows; ++r)
+    for (int k = S.outer_ptr[r]; k < S.outer_ptr[r + 1]; ++k) {
+      const int c = S.inner_idx[k];
+      const int *b = S.inner_idx.data() + S.outer_ptr[c], *e = S.inner_idx.data() + S.outer_ptr[c + 1];
+      const int *f = std::lower_bound(b, e, r);
+      if (f == e || *f != r) throw Error(BARTELS_E_INVALID_ARG, "pattern is not structurally symmetric");
+      col_vals[f - S.inner_idx.data()] = S.values[k];  // H(r, c) stored in column c at row r
+    }
+  S.values.swap(col_vals);
+}
 }  // namespace detail
 
 // element-matrix callback replacements (src/linear_tetmesh_neohookean_dq2.cpp:22)
@@ -186,6 +206,7 @@ void linear_tetmesh_dphi_dX(MR &dX, const MV &V, const ME &E) {
     check(bartels_tetmesh_dq2(context(), p, id, q.data(), dphidX.data(), volume.data(), params.data(), psd, tol, 0, \
                               H.values.data()),                                                                    \
           "linear_tetmesh_" #name "_dq2");                                                                         \
+    detail::row_values_to_columns(H);                                                                              \
   }
 
 BARTELS_SIM_MODEL(neohookean, BARTELS_NEOHOOKEAN)
@@ -304,6 +325,7 @@ void linear_tri2dmesh_dphi_dX(MR &dX, const MV &V, const ME &E) {
     check(bartels_tri2dmesh_dq2(context(), p, id, q.data(), dphidX.data(), area.data(), params.data(), psd, tol,   \
                                 H.values.data()),                                                                  \
           "linear_tri2dmesh_" #name "_dq2");                                                                       \
+    detail::row_values_to_columns(H);                                                                              \
   }
 
 BARTELS_SIM_TRI_MODEL(neohookean, BARTELS_NEOHOOKEAN)
@@ -324,6 +346,7 @@ void linear_tri2dmesh_linear_elasticity_dq2(SparseMatrix &H, const MV &V, const 
   check(bartels_tri2dmesh_dq2(context(), p, BARTELS_LINEAR_ELASTICITY, q.data(), dphidX.data(), area.data(),
                               params.data(), psd, tol, H.values.data()),
         "linear_tri2dmesh_linear_elasticity_dq2");
+  detail::row_values_to_columns(H);
 }
 
 // linear_tri2dmesh_mass_matrix, include/linear_tri2dmesh_mass_matrix.h
@@ -333,6 +356,7 @@ void linear_tri2dmesh_mass_matrix(SparseMatrix &M, const MV &V, const ME &E, con
   detail::tri_pattern(M, p);
   check(bartels_tri2dmesh_mass_matrix(context(), p, density.data(), area.data(), M.values.data()),
         "linear_tri2dmesh_mass_matrix");
+  detail::row_values_to_columns(M);
 }
 
 // linear_tri3dmesh_dphi_dX, include/linear_tri3dmesh_dphi_dX.h (dX: nT x 9)
@@ -356,6 +380,7 @@ void linear_tri3dmesh_stvk_dq2(SparseMatrix &H, const MV &V, const ME &E, const 
   check(bartels_tri3dmesh_stvk_dq2(context(), p, q.data(), dphidX.data(), N.data(), n.data(), dndq.data(),
                                    area.data(), params.data(), psd, tol, H.values.data()),
         "linear_tri3dmesh_stvk_dq2");
+  detail::row_values_to_columns(H);
 }
 
 // linear_tetmesh_mass_matrix, include/linear_tetmesh_mass_matrix.h
@@ -369,6 +394,7 @@ void linear_tetmesh_mass_matrix(SparseMatrix &M, const MV &V, const ME &E, const
   M.values.resize(nnz);
   check(bartels_tetmesh_mass_matrix(context(), p, density.data(), volume.data(), M.values.data()),
         "linear_tetmesh_mass_matrix");
+  detail::row_values_to_columns(M);
 }
 
 // linear_tetmesh_const_ext_force, include/linear_tetmesh_const_ext_force.h
@@ -379,7 +405,9 @@ void linear_tetmesh_const_ext_force(MF &f, const MV &V, const ME &E, const MVol 
         "linear_tetmesh_const_ext_force");
 }
 
-// fixed_point_constraint_matrix, include/fixed_point_constraint_matrix.h
+// fixed_point_constraint_matrix, include/fixed_point_constraint_matrix.h:
+// P (d (nV - k) x d nV, one 1 per row at a free DOF) in compressed columns:
+// column c holds row r when DOF c is the r-th free one.
 template <class MV, class MI>
 void fixed_point_constraint_matrix(SparseMatrix &P, const MV &V, const MI &fixed_indices) {
   int rows = 0;
@@ -387,14 +415,29 @@ void fixed_point_constraint_matrix(SparseMatrix &P, const MV &V, const MI &fixed
   check(bartels_fixed_point_constraint_matrix((int)V.rows(), (int)V.cols(), fixed_indices.data(), nfix, &rows,
                                               nullptr, nullptr, nullptr),
         "fixed_point_constraint_matrix");
+  std::vector<int> rp(rows + 1), col(rows);
+  check(bartels_fixed_point_constraint_matrix((int)V.rows(), (int)V.cols(), fixed_indices.data(), nfix, &rows,
+                                              rp.data(), col.data(), nullptr),
+        "fixed_point_constraint_matrix");
   P.n_rows = rows;
   P.n_cols = (int)(V.rows() * V.cols());
-  P.outer_ptr.resize(rows + 1);
+  P.outer_ptr.assign(P.n_cols + 1, 0);
   P.inner_idx.resize(rows);
-  P.values.resize(rows);
-  check(bartels_fixed_point_constraint_matrix((int)V.rows(), (int)V.cols(), fixed_indices.data(), nfix, &rows,
-                                              P.outer_ptr.data(), P.inner_idx.data(), P.values.data()),
-        "fixed_point_constraint_matrix");
+  P.values.assign(rows, 1.0);
+  for (int r = 0; r < rows; ++r) P.outer_ptr[col[r] + 1] = 1;
+  for (int c = 0; c < P.n_cols; ++c) P.outer_ptr[c + 1] += P.outer_ptr[c];
+  for (int r = 0; r < rows; ++r) P.inner_idx[P.outer_ptr[col[r]]] = r;
+}
+
+// find_min_vertices, include/find_min_vertices.h: appends (as the reference's
+// push_back) the vertices whose coordinate dim is within tol of its minimum.
+template <class MV>
+void find_min_vertices(std::vector<int> &indices, const MV &V, unsigned int dim, double tol = 1e-3) {
+  std::vector<int> found(V.rows() > 0 ? V.rows() : 1);
+  int count = 0;
+  check(bartels_find_min_vertices((int)V.rows(), V.data(), (int)dim, tol, found.data(), &count),
+        "find_min_vertices");
+  indices.insert(indices.end(), found.begin(), found.begin() + count);
 }
 
 // search_direction_newton_sparse, include/search_direction_newton_sparse.h:8-12.
@@ -405,12 +448,36 @@ struct PCGSolver {
   bartels_pcg_report report{};
   PCGSolver() { bartels_pcg_default_params(&params); }
 };
+namespace detail {
+// Compressed columns -> compressed rows (the C ABI's layout) of a square matrix.
+inline void columns_to_rows(const SparseMatrix &H, std::vector<int> &rp, std::vector<int> &ci,
+                            std::vector<double> &v) {
+  const int n = H.n_rows;
+  rp.assign(n + 1, 0);
+  ci.resize(H.inner_idx.size());
+  v.resize(H.values.size());
+  for (int i : H.inner_idx) rp[i + 1]++;
+  for (int r = 0; r < n; ++r) rp[r + 1] += rp[r];
+  std::vector<int> fill(rp.begin(), rp.end() - 1);
+  for (int c = 0; c < H.n_cols; ++c)  // columns in order: rows receive ascending column indices
+    for (int k = H.outer_ptr[c]; k < H.outer_ptr[c + 1]; ++k) {
+      const int r = H.inner_idx[k];
+      ci[fill[r]] = c;
+      v[fill[r]++] = H.values[k];
+    }
+}
+}  // namespace detail
+
 template <class MD, class MG>
 bool search_direction_newton_sparse(MD &d, const MG &g, const SparseMatrix &H, PCGSolver &solver) {
   d.resize((int)g.rows(), 1);
-  const int s = bartels_search_direction_newton_sparse(context(), H.rows(), H.outer_ptr.data(), H.inner_idx.data(),
-                                                       H.values.data(), g.data(), d.data(), &solver.params,
-                                                       &solver.report);
+  if (H.n_rows != H.n_cols || (int)H.outer_ptr.size() != H.n_cols + 1)
+    throw Error(BARTELS_E_INVALID_ARG, "search_direction_newton_sparse: H must be square, compressed columns");
+  std::vector<int> rp, ci;
+  std::vector<double> v;
+  detail::columns_to_rows(H, rp, ci, v);
+  const int s = bartels_search_direction_newton_sparse(context(), H.rows(), rp.data(), ci.data(), v.data(),
+                                                       g.data(), d.data(), &solver.params, &solver.report);
   if (s == BARTELS_E_NOT_CONVERGED) return false;
   check(s, "search_direction_newton_sparse");
   return true;

@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <vector>
 
 #include "bartels_sim.hpp"
 
@@ -119,11 +120,13 @@ int main() {
   sim::PCGSolver solver;
   sim::VectorXd d;
   REQUIRE(sim::search_direction_newton_sparse(d, g, A, solver));
+  // A d + g with A in compressed columns (column c, rows inner_idx)
+  std::vector<double> Ad(A.rows(), 0.0);
+  for (int c = 0; c < A.cols(); ++c)
+    for (int k = A.outer_ptr[c]; k < A.outer_ptr[c + 1]; ++k) Ad[A.inner_idx[k]] += A.values[k] * d(c);
   double rr = 0, gg = 0;
   for (int i = 0; i < A.rows(); ++i) {
-    double s = 0;
-    for (int k = A.outer_ptr[i]; k < A.outer_ptr[i + 1]; ++k) s += A.values[k] * d(A.inner_idx[k]);
-    rr += (s + g(i)) * (s + g(i));
+    rr += (Ad[i] + g(i)) * (Ad[i] + g(i));
     gg += g(i) * g(i);
   }
   REQUIRE(std::sqrt(rr) <= 2e-8 * std::sqrt(gg));

@@ -136,3 +136,19 @@ def test_sim_plan_cache_keys_on_content_and_evicts():
                            "-I", os.path.join(ROOT, "include"), "-o", exe])
     r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0 and "plan cache ok" in r.stdout, r.stderr
+
+
+def test_sim_host_parts_without_a_gpu():
+    """sim:: routines that run on the host (tests/sim_host_test.cpp): compressed
+    columns from row-ordered values, P in compressed columns, find_min_vertices,
+    the host line search."""
+    import subprocess
+    out_dir = os.path.join(ROOT, "tests", "_build")
+    os.makedirs(out_dir, exist_ok=True)
+    exe = os.path.join(out_dir, "sim_host_test")
+    libdir = os.path.join(ROOT, "bartels_gb300", "lib")
+    subprocess.check_call(["g++", "-std=c++17", "-O1", os.path.join(ROOT, "tests", "sim_host_test.cpp"), "-I",
+                           os.path.join(ROOT, "include"), "-L", libdir, "-lbartels_gpu", f"-Wl,-rpath,{libdir}",
+                           "-o", exe])
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and "sim host ok" in r.stdout, r.stderr
