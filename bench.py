@@ -17,8 +17,10 @@ on the same GPU ("jacobi_pcg" in the JSON line).
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--precond jacobi]
 
 Prints one JSON line. Under torchrun (N > 1) every rank runs an independent
-replica on its own GPU (the path does not shard: replicas only) and rank 0
-reports the max-over-ranks time.
+replica on its own GPU and rank 0 reports the max-over-ranks time. The path
+could shard (a vertex partition with a one-layer halo), but every run here has
+one GPU, so the multi-GPU mode is replicas only, with no collective on the
+data path.
 """
 from __future__ import annotations
 
