@@ -19,7 +19,8 @@ CSRC = os.path.join(PKG, "csrc")
 OBJ = os.path.join(PKG, "_build")
 LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libbartels_gpu.so")
-SOURCES = ["elements.cu", "plan.cu", "solver.cu", "capi.cu", "lpcg.cu", "gemm_tc.cu", "tri.cu", "laws.cu", "mex.cpp"]
+SOURCES = ["elements.cu", "plan.cu", "solver.cu", "amg.cu", "capi.cu", "lpcg.cu", "gemm_tc.cu", "tri.cu", "laws.cu",
+           "mex.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -29,6 +29,8 @@ int csr_search_direction(bartels_ctx ctx, int n, const int *rp, const int *ci, c
                          double *d, const bartels_pcg_params &prm, bartels_pcg_report *rep);
 int advance_implicit_euler(bartels_ctx ctx, bartels_mesh_plan plan, double dt, const double *v);
 int plan_spmv(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const float *x, float *y);
+int plan_precond_apply(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const float *r, float *z,
+                       int *levels);
 int noalloc_gradient(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q_d, double *g_d);
 int plan_pcg(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const double *b, double *x,
              const bartels_pcg_params &prm, bartels_pcg_report *rep);
@@ -530,6 +532,7 @@ int bartels_newton_set_problem(bartels_mesh_plan plan, const double *q_base, con
   BT_CHECK(put(&plan->q_base, q_base));
   BT_CHECK(put(&plan->x_hat, x_hat));
   BT_CHECK(put(&plan->f_ext, f_ext));
+  plan->pinned_gen++;
   if (pinned) {
     if (!plan->pinned) BT_CUDA(cudaMalloc(&plan->pinned, (size_t)plan->nV));
     BT_CUDA(cudaMemcpyAsync(plan->pinned, pinned, (size_t)plan->nV, cudaMemcpyHostToDevice, ctx->stream));
@@ -689,7 +692,13 @@ int bartels_plan_set_preconditioner(bartels_mesh_plan plan, int kind, bartels_lp
     plan->lpcg_net = nullptr;
     return BARTELS_OK;
   }
-  if (kind != BARTELS_PRECOND_LEARNED || !net) return fail(BARTELS_E_INVALID_ARG, "unknown preconditioner");
+  if (kind == BARTELS_PRECOND_MULTIGRID) {
+    plan->precond = kind;
+    plan->lpcg_net = nullptr;
+    return BARTELS_OK;
+  }
+  if ((kind != BARTELS_PRECOND_LEARNED && kind != BARTELS_PRECOND_LEARNED_MULTIGRID) || !net)
+    return fail(BARTELS_E_INVALID_ARG, "unknown preconditioner");
   if (lpcg_ctx(net) != plan->ctx) return fail(BARTELS_E_INVALID_ARG, "network belongs to another context");
   plan->precond = kind;
   plan->lpcg_net = net;
@@ -709,6 +718,13 @@ int bartels_plan_pcg_d(bartels_ctx ctx, bartels_mesh_plan plan, const float *val
   if (params) p = *params;
   else bartels_pcg_default_params(&p);
   return plan_pcg(ctx, plan, values_d, b_d, x_d, p, report);
+}
+
+int bartels_plan_precond_apply_d(bartels_ctx ctx, bartels_mesh_plan plan, const float *values_d, const float *r_d,
+                                 float *z_d, int *levels) {
+  BT_CHECK(check_plan(ctx, plan));
+  if (!values_d || !r_d || !z_d) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  return plan_precond_apply(ctx, plan, values_d, r_d, z_d, levels);
 }
 
 int bartels_newton_gradient_d(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params *params,

@@ -934,7 +934,11 @@ int values_to_double(bartels_ctx ctx, const float *v32, double *v64, int64_t n) 
 // nothing needs clearing. Calls that overlap on the GPU race on it.
 constexpr int kNoAllocMaxTets = 1 << 16;
 static __device__ __align__(256) double g_noalloc_scratch[12 * kNoAllocMaxTets];
-static double *g_noalloc_ptr[64];  // device address of the scratch, per device
+// Device address of the scratch, looked up once per device and kept for the
+// life of the process. A cudaDeviceReset (or any reset of the device's primary
+// context) invalidates it: a process that resets a device must not call the
+// allocation-free entry point on that device afterwards.
+static double *g_noalloc_ptr[64];
 static std::mutex g_noalloc_mutex;
 
 int noalloc_gradient(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q_d, double *g_d) {

@@ -72,6 +72,7 @@ static_assert(sizeof(TetRec64) == 128, "TetRec64 must be 128 bytes");
 
 struct FactorPattern;  // lower / upper block storage maps (learned preconditioner)
 struct LpcgPlanState;  // per-plan buffers of the learned preconditioner
+struct MgHierarchy;    // aggregation multigrid hierarchy of a plan
 
 // Device buffer with geometric growth.
 struct DevBuf {
@@ -137,6 +138,7 @@ struct bartels_mesh_plan_s {
   // Newton problem data
   double *q_base = nullptr, *x_hat = nullptr, *f_ext = nullptr;
   unsigned char *pinned = nullptr;
+  int pinned_gen = 0;  // incremented whenever the pinned set is replaced
   // true when dphidX is the rest shape's own (F = I + sum (u_a - u_0) phi_a^T)
   bool dphi_matches_rest = true;
   // triangular-factor pattern and learned-preconditioner buffers (built on first use)
@@ -146,8 +148,10 @@ struct bartels_mesh_plan_s {
   // lanes per vertex row chosen by the autotuner for this plan (0: the context's)
   int spmv_lanes = 0, tri_lanes = 0;
   bartels_lpcg lpcg_net = nullptr;
+  // aggregation multigrid hierarchy (built on first use for the current pinned set)
+  bartels::MgHierarchy *mg = nullptr;
   // solver workspace
-  bartels::DevBuf w_values, w_minv, w_vec, w_grad_e, w_energy, w_u, w_pcg, w_psd;
+  bartels::DevBuf w_values, w_minv, w_vec, w_grad_e, w_energy, w_u, w_pcg, w_psd, w_spmv;
 };
 
 namespace bartels {

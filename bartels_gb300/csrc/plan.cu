@@ -16,6 +16,7 @@
 #include <mutex>
 
 #include "devmath.cuh"
+#include "amg_internal.cuh"
 #include "internal.cuh"
 #include "lpcg_internal.cuh"
 
@@ -324,6 +325,8 @@ void plan_free(bartels_mesh_plan plan) {
     plan->factor = nullptr;
   }
   lpcg_plan_release(plan);
+  mg_destroy(plan->mg);
+  plan->mg = nullptr;
   void *ptrs[] = {plan->X,        plan->E,      plan->dphi64,  plan->vol,     plan->params,  plan->density,
                   plan->rec32,    plan->rec64,  plan->inc_ptr, plan->inc_tet, plan->inc_pos, plan->brp,
                   plan->bcol,     plan->diag_pos, plan->chunk_v, plan->csr_rp, plan->csr_col, plan->q_base,
@@ -338,6 +341,7 @@ void plan_free(bartels_mesh_plan plan) {
   plan->w_u.release();
   plan->w_pcg.release();
   plan->w_psd.release();
+  plan->w_spmv.release();
 }
 
 }  // namespace bartels

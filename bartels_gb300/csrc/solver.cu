@@ -18,7 +18,9 @@
 
 #include "devmath.cuh"
 #include "internal.cuh"
+#include "amg_internal.cuh"
 #include "lpcg_internal.cuh"
+#include "pcg_common.cuh"
 
 namespace bartels {
 
@@ -29,47 +31,6 @@ int launch_hess(bartels_ctx ctx, bartels_mesh_plan plan, int model, int psd_mode
 
 constexpr int kVecBlocksPerSM = 8;
 constexpr int kSpmvBlocksPerSM = 8;
-
-// Device-side PCG scalars. Reductions finish in the last block of the kernel
-// that produces them (fixed summation order), so consumers read scalars.
-struct PcgState {
-  double rz;            // r.z of the current iterate
-  double rr;            // r.r of the current iterate
-  double pap;           // p.Ap of the current direction
-  double rr0, tol2;
-  float alpha, beta;    // step and direction coefficients, computed once by the last block
-  int it;               // iterations completed in the current inner solve
-  int done;
-  int max_it;
-  unsigned int count;   // blocks finished (last-block reductions)
-};
-
-// ------------------------------------------------------------- reductions ---
-__device__ __forceinline__ double warp_sum(double v) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  return v;
-}
-__device__ __forceinline__ float warp_sumf(float v) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-// sum of blockDim-strided values of one double per thread; returns in thread 0
-__device__ __forceinline__ double cta_sum(double v) {
-  __shared__ double red[32];
-  v = warp_sum(v);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (lane == 0) red[w] = v;
-  __syncthreads();
-  double s = 0.0;
-  if (w == 0) {
-    const int nw = (blockDim.x + 31) >> 5;
-    s = lane < nw ? red[lane] : 0.0;
-    s = warp_sum(s);
-  }
-  __syncthreads();
-  return s;
-}
 
 // ------------------------------------------------------------------ SpMV ---
 // refinement residual r = b - A x of a generic scalar CSR (the drop-in search
@@ -165,54 +126,6 @@ __global__ void k_minv_csr(int nb, int n, const int *__restrict__ rp, const int 
   }
 }
 
-// ------------------------------------------------------------ PCG vectors ---
-__device__ __forceinline__ void apply_minv(const float *__restrict__ minv, int v, const float *r, float *z) {
-  const float *m = minv + 6ll * v;
-  const float m00 = m[0], m11 = m[1], m22 = m[2], m01 = m[3], m02 = m[4], m12 = m[5];
-  z[0] = m00 * r[0] + m01 * r[1] + m02 * r[2];
-  z[1] = m01 * r[0] + m11 * r[1] + m12 * r[2];
-  z[2] = m02 * r[0] + m12 * r[1] + m22 * r[2];
-}
-
-// Last-block completion: returns true in every thread of the block that
-// finished last (after all partials are visible).
-__device__ __forceinline__ bool last_block(unsigned int *count) {
-  __shared__ bool am_last;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const unsigned int prev = atomicAdd(count, 1u);
-    am_last = (prev == gridDim.x - 1);
-  }
-  __syncthreads();
-  return am_last;
-}
-
-// Block sum of per-thread FP32 partials: FP32 within a warp (fixed shuffle
-// tree), FP64 across warps. Valid in thread 0. Keeps the FP64 pipe (1/64 of
-// FP32 on GB300) off the per-element path.
-__device__ __forceinline__ double cta_sum_f(float v) {
-  __shared__ double redf[32];
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (lane == 0) redf[w] = (double)v;
-  __syncthreads();
-  double s = 0.0;
-  if (w == 0) {
-    const int nw = (blockDim.x + 31) >> 5;
-    s = lane < nw ? redf[lane] : 0.0;
-    s = warp_sum(s);
-  }
-  __syncthreads();
-  return s;
-}
-
-// deterministic sum of n partials (fixed order), valid in thread 0
-__device__ __forceinline__ double sum_partials(const double *a, int n) {
-  double acc = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) acc += __ldcg(a + i);
-  return cta_sum(acc);
-}
 
 // start of an inner solve: x = 0, r = rres (the refinement residual), z = M^-1 r. A fresh solve
 // (cont = 0) clears p and the iteration count; a continued one (cont = 1, the
@@ -267,48 +180,6 @@ __global__ void k_pcg_init(int nb, int n, const float *__restrict__ rres, const 
     }
   }
 }
-
-// One vertex row of the block-layout SpMV, split in two so that no shuffle
-// runs in a divergent region: spmv_row_acc (G lanes of a group walk the row's
-// (block, component) pairs and read the three scalar rows at that column with
-// streaming loads; xval(c) supplies the vector entry at scalar column c) runs
-// only for an active group, group_reduce runs in every lane of the warp.
-template <int G, class XV>
-__device__ __forceinline__ void spmv_row_acc(int v, int sl, const int *__restrict__ brp, const int *__restrict__ bcol,
-                                             const float *__restrict__ val, XV &&xval, float &s0, float &s1,
-                                             float &s2) {
-  const int rb = __ldg(brp + v);
-  const int rs = 3 * (__ldg(brp + v + 1) - rb);
-  const float *r0 = val + 9ll * rb;
-  for (int e = sl; e < rs; e += G) {
-    const int j = e / 3, l = e - 3 * j;
-    const float xv = xval(3 * __ldg(bcol + rb + j) + l);
-    s0 += __ldcs(r0 + e) * xv;
-    s1 += __ldcs(r0 + rs + e) * xv;
-    s2 += __ldcs(r0 + 2 * rs + e) * xv;
-  }
-}
-
-template <int G>
-__device__ __forceinline__ void group_reduce(float &s0, float &s1, float &s2) {
-#pragma unroll
-  for (int o = G / 2; o > 0; o >>= 1) {
-    s0 += __shfl_xor_sync(0xffffffffu, s0, o);
-    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
-    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
-  }
-}
-
-// Warp-uniform walk over vertex rows: each warp takes 32/G consecutive rows
-// per step, group g of the warp row vb + g (inactive past nV).
-#define BT_ROW_LOOP_BEGIN(G)                                                      \
-  const int lane_ = threadIdx.x & 31, sl = lane_ % (G), gw_ = lane_ / (G);       \
-  const int warp_ = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;                \
-  const int nwarps_ = (gridDim.x * blockDim.x) >> 5;                             \
-  for (int vb_ = warp_ * (32 / (G)); vb_ < nV; vb_ += nwarps_ * (32 / (G))) {    \
-    const int v = vb_ + gw_;                                                      \
-    const bool active = v < nV;
-#define BT_ROW_LOOP_END }
 
 // y = A x with the PCG's row mapping (rows of pinned vertices give 0)
 template <int G>
@@ -655,41 +526,9 @@ __global__ void k_f64_to_f32(int64_t n, const double *__restrict__ a, float *__r
 // ------------------------------------------- factor preconditioner (G^T G) ---
 // z = G^T (G r) with G block-lower-triangular on the plan's pattern (the
 // learned preconditioner). G is held twice: by rows of its lower part and by
-// rows of G^T (the transposed blocks), so both products are row gathers.
+// rows of G^T (the transposed blocks), so both products are row gathers
+// (tri_row_acc4).
 //
-// Row v of a triangular operand: blocks [b0, b0 + nblk) of the full pattern row
-// (columns cols[j] = bcol[brp[v] + b0 + j]), BF16 values in three scalar rows of
-// rs = 3 nblk entries padded to rsp (a multiple of 4). Each lane takes 4
-// consecutive columns per step: one 8-byte load per scalar row, and the 4
-// vector entries of the (at most two) blocks those columns fall in.
-// meta[v] = {brp, lower segment, upper segment, diag | nblocks << 16}.
-template <int G, class XV>
-__device__ __forceinline__ void tri_row_acc4(int sl, const int *__restrict__ cols, const __nv_bfloat16 *__restrict__ r0,
-                                             int rs, int rsp, XV &&xval, float &s0, float &s1, float &s2) {
-  for (int e0 = 4 * sl; e0 < rs; e0 += 4 * G) {
-    const uint2 w0 = __ldcs(reinterpret_cast<const uint2 *>(r0 + e0));
-    const uint2 w1 = __ldcs(reinterpret_cast<const uint2 *>(r0 + rsp + e0));
-    const uint2 w2 = __ldcs(reinterpret_cast<const uint2 *>(r0 + 2 * rsp + e0));
-    const int j0 = e0 / 3, l0 = e0 - 3 * j0;
-    const int c0 = __ldg(cols + j0);
-    const int c1 = 3 * (j0 + 1) < rs ? __ldg(cols + j0 + 1) : 0;
-    float xv[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int l = l0 + q;
-      const int c = l >= 3 ? c1 : c0;
-      xv[q] = e0 + q < rs ? xval(3 * c + (l >= 3 ? l - 3 : l)) : 0.f;
-    }
-    const uint32_t u0[2] = {w0.x, w0.y}, u1[2] = {w1.x, w1.y}, u2[2] = {w2.x, w2.y};
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      s0 += __uint_as_float(u0[h] << 16) * xv[2 * h] + __uint_as_float(u0[h] & 0xFFFF0000u) * xv[2 * h + 1];
-      s1 += __uint_as_float(u1[h] << 16) * xv[2 * h] + __uint_as_float(u1[h] & 0xFFFF0000u) * xv[2 * h + 1];
-      s2 += __uint_as_float(u2[h] << 16) * xv[2 * h] + __uint_as_float(u2[h] & 0xFFFF0000u) * xv[2 * h + 1];
-    }
-  }
-}
-
 // y = G r (lower rows; rows of pinned vertices give 0) and r.z = r^T G^T G r =
 // |y|^2; beta = r.z / r.z_old in the last block.
 template <int G>
@@ -854,6 +693,9 @@ struct PcgOperator {
   // factor preconditioner z = G^T G r (block layout only): lower and upper storage
   const __nv_bfloat16 *gl = nullptr, *gu = nullptr;
   const FactorPattern *fp = nullptr;
+  // multigrid V-cycle (block layout only) with its level-0 smoother
+  bool mg = false;
+  MgSmoother sm;
 };
 
 struct PcgWork {
@@ -869,6 +711,8 @@ static int lanes_spmv(bartels_ctx ctx, bartels_mesh_plan plan) {
 static int lanes_tri(bartels_ctx ctx, bartels_mesh_plan plan) {
   return (plan && plan->tri_lanes) ? plan->tri_lanes : ctx->tri_lanes;
 }
+int plan_lanes_spmv(bartels_ctx ctx, bartels_mesh_plan plan) { return lanes_spmv(ctx, plan); }
+int plan_lanes_tri(bartels_ctx ctx, bartels_mesh_plan plan) { return lanes_tri(ctx, plan); }
 
 static int grid_vec(bartels_ctx ctx, int64_t n) {
   int64_t g = (n + 255) / 256;
@@ -879,6 +723,11 @@ static int grid_spmv(bartels_ctx ctx, int64_t rows) {
   int64_t g = (rows + 7) / 8;  // 8 warps per 256-thread block
   int64_t cap = (int64_t)ctx->num_sms * kSpmvBlocksPerSM;
   return (int)std::max<int64_t>(1, std::min(g, cap));
+}
+int launch_minv_blk(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, float *minv) {
+  BT_LAUNCH(ctx, k_minv_blk, grid_vec(ctx, plan->nV), 256, 0, plan->nV, plan->brp, plan->diag_pos, values,
+            plan->pinned, minv);
+  return BARTELS_OK;
 }
 
 
@@ -902,6 +751,24 @@ static int pcg_enqueue_prec(bartels_ctx ctx, const PcgOperator &op, const PcgWor
   return BARTELS_OK;
 }
 
+// z = B r (V-cycle; its last kernel forms r.z and beta), then p = z + beta p
+static int pcg_enqueue_mg(bartels_ctx ctx, const PcgOperator &op, const PcgWork &w, int n) {
+  BT_CHECK(mg_enqueue_apply(ctx, op.plan, op.values, op.sm, w.r, w.z, w.ap, w.part_b, w.st));
+  BT_LAUNCH(ctx, k_pcg_dir, grid_vec(ctx, (n + 3) / 4), 256, 0, n, w.z, w.pa, w.pb, w.st);
+  return BARTELS_OK;
+}
+
+static int pcg_spmv_blk(bartels_ctx ctx, const PcgOperator &op, const PcgWork &w, int lanes, int gs) {
+#define BT_K0(G)                                                                                                 \
+  BT_LAUNCH(ctx, k_pcg_spmv_blk<G>, gs, 256, 0, op.plan->nV, op.plan->brp, op.plan->bcol, op.values, w.pa, w.pb, \
+            w.ap, op.pinned, w.part_a, w.st)
+  if (lanes == 4) BT_K0(4);
+  else if (lanes == 16) BT_K0(16);
+  else BT_K0(8);
+#undef BT_K0
+  return BARTELS_OK;
+}
+
 static int pcg_enqueue_iters(bartels_ctx ctx, const PcgOperator &op, const PcgWork &w, int n, int nb, int iters) {
   const bool blk = op.plan != nullptr;
   const bool fac = blk && op.gl != nullptr;
@@ -910,6 +777,13 @@ static int pcg_enqueue_iters(bartels_ctx ctx, const PcgOperator &op, const PcgWo
   const int gu = grid_vec(ctx, (nb + 3) / 4);
   const int gd = grid_vec(ctx, (n + 3) / 4);
   for (int i = 0; i < iters; ++i) {
+    if (op.mg) {
+      // p was formed at the end of the previous iteration (or at the start of the solve)
+      BT_CHECK(pcg_spmv_blk(ctx, op, w, lanes, gs));
+      BT_LAUNCH(ctx, k_pcg_update_f, gd, 256, 0, n, w.pa, w.pb, w.ap, w.x, w.r, w.part_b, w.st);
+      BT_CHECK(pcg_enqueue_mg(ctx, op, w, n));
+      continue;
+    }
     // with the factor preconditioner the direction is formed by k_pcg_prec_upper
     if (!fac) BT_LAUNCH(ctx, k_pcg_dir, gd, 256, 0, n, w.z, w.pa, w.pb, w.st);
     if (blk) {
@@ -997,14 +871,17 @@ static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double
   }
   const double target = prm.rel_tol * bnorm;
   // CUDA graph of a fixed number of PCG iterations (kernels no-op once done)
-  const int chunk = 16;
+  // (a V-cycle iteration is ~30 launches: shorter graphs waste fewer no-op launches after convergence)
+  const int chunk = op.mg ? 8 : 16;
   cudaGraphExec_t exec = nullptr;
+  int64_t graph_launches = 0;
   {
     cudaGraph_t graph;
     const int64_t launches_before = ctx->launches;
     BT_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     int s = pcg_enqueue_iters(ctx, op, w, n, nb, chunk);
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+    graph_launches = ctx->launches - launches_before;
     ctx->launches = launches_before;  // counted per graph launch below
     if (s != BARTELS_OK) return s;
     if (e != cudaSuccess) return fail(BARTELS_E_DEVICE, std::string("graph capture: ") + cudaGetErrorString(e));
@@ -1051,7 +928,11 @@ static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double
     const double abs2 = (0.5 * target) * (0.5 * target);
     const int cont = (pass > 0 && !prm.restart) ? 1 : 0;
     const int it0 = cont ? hs.it : 0;
-    if (op.gl) {
+    if (op.mg) {
+      BT_LAUNCH(ctx, k_pcg_init_f, gv, 256, 0, n, w.rres, w.x, w.r, w.pa, w.pb, w.part_a, w.st,
+                prm.inner_rel_tol * prm.inner_rel_tol, abs2, prm.max_iters - rep->iterations, cont);
+      BT_CHECK(pcg_enqueue_mg(ctx, op, w, n));
+    } else if (op.gl) {
       BT_LAUNCH(ctx, k_pcg_init_f, gv, 256, 0, n, w.rres, w.x, w.r, w.pa, w.pb, w.part_a, w.st,
                 prm.inner_rel_tol * prm.inner_rel_tol, abs2, prm.max_iters - rep->iterations, cont);
       BT_CHECK(pcg_enqueue_prec(ctx, op, w));
@@ -1061,7 +942,7 @@ static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double
     }
     for (;;) {
       BT_CUDA(cudaGraphLaunch(exec, ctx->stream));
-      ctx->launches += (op.gl ? 4 : 3) * chunk;
+      ctx->launches += graph_launches;
       BT_CUDA(cudaMemcpyAsync(&hs, w.st, sizeof(PcgState), cudaMemcpyDeviceToHost, ctx->stream));
       BT_CUDA(cudaStreamSynchronize(ctx->stream));
       if (hs.done) break;
@@ -1080,6 +961,34 @@ static double now_s() {
 // PCG on a plan's Hessian with the plan's preconditioner. The learned factor is
 // built from the current values; when its solve fails (not converged, not
 // finite) the system is solved again with block-Jacobi.
+// Multigrid hierarchy values for a Hessian: the level-0 smoother (block-Jacobi
+// inverse blocks, or the network's factor), Galerkin products, bounds.
+static int mg_values(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, bool learned, MgSmoother &sm) {
+  sm = MgSmoother();
+  if (learned) {
+    BT_CHECK(lpcg_factor(plan->lpcg_net, plan, values, &sm.gl, &sm.gu));
+    sm.fp = plan->factor;
+  } else {
+    BT_CHECK(plan->w_minv.ensure(24 * (size_t)plan->nV));
+    BT_CHECK(launch_minv_blk(ctx, plan, values, plan->w_minv.as<float>()));
+    sm.minv = plan->w_minv.as<float>();
+  }
+  return mg_setup_numeric(ctx, plan, values, sm);
+}
+
+int plan_precond_apply(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const float *r, float *z,
+                       int *levels) {
+  const bool learned = plan->precond == BARTELS_PRECOND_LEARNED_MULTIGRID && plan->lpcg_net;
+  if (plan->precond != BARTELS_PRECOND_MULTIGRID && !learned)
+    return fail(BARTELS_E_INVALID_ARG, "the plan's preconditioner is not a multigrid one");
+  BT_CHECK(mg_prepare(ctx, plan));
+  MgSmoother sm;
+  BT_CHECK(mg_values(ctx, plan, values, learned, sm));
+  BT_CHECK(mg_apply_once(ctx, plan, values, sm, r, z));
+  if (levels) *levels = (int)plan->mg->lv.size();
+  return BARTELS_OK;
+}
+
 static int plan_pcg_impl(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const double *b, double *x,
                          const bartels_pcg_params &prm, bartels_pcg_report *rep, int *fallback, double *t_factor) {
   const int n = 3 * plan->nV;
@@ -1088,6 +997,34 @@ static int plan_pcg_impl(bartels_ctx ctx, bartels_mesh_plan plan, const float *v
   op.values = values;
   op.pinned = plan->pinned;
   if (fallback) *fallback = 0;
+  const bool mg_learned = plan->precond == BARTELS_PRECOND_LEARNED_MULTIGRID && plan->lpcg_net;
+  if (plan->precond == BARTELS_PRECOND_MULTIGRID || mg_learned) {
+    const double t0 = now_s();
+    int s = mg_prepare(ctx, plan);
+    if (s != BARTELS_OK && s != BARTELS_E_UNSUPPORTED) return s;
+    if (s == BARTELS_OK) {
+      MgSmoother sm;
+      BT_CHECK(mg_values(ctx, plan, values, mg_learned, sm));
+      BT_CUDA(cudaStreamSynchronize(ctx->stream));
+      if (t_factor) *t_factor += now_s() - t0;
+      op.mg = true;
+      op.sm = sm;
+      s = pcg_solve(ctx, op, n, b, x, plan->w_pcg, prm, rep);
+      if (s == BARTELS_OK && rep->converged) return BARTELS_OK;
+      if (s != BARTELS_OK && s != BARTELS_E_NOT_CONVERGED && s != BARTELS_E_NONFINITE) return s;
+      // not converged or not finite: solve again with block-Jacobi
+      if (fallback) *fallback = 1;
+      const int used = rep->iterations;
+      op.mg = false;
+      op.sm = MgSmoother();
+      BT_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, ctx->stream));
+      s = pcg_solve(ctx, op, n, b, x, plan->w_pcg, prm, rep);
+      rep->iterations += used;
+      return s;
+    }
+    // a system too small for a coarse level: block-Jacobi
+    set_error("");
+  }
   if (plan->precond == BARTELS_PRECOND_LEARNED && plan->lpcg_net) {
     const double t0 = now_s();
     const __nv_bfloat16 *gl = nullptr, *gu = nullptr;
@@ -1312,15 +1249,28 @@ int advance_implicit_euler(bartels_ctx ctx, bartels_mesh_plan plan, double dt, c
   return BARTELS_OK;
 }
 
+// y = A x with the PCG loop's own SpMV kernel (k_pcg_spmv_blk, which also
+// forms the partial sums of x.Ax), on a scratch state of the plan, so that
+// timing this entry point times the SpMV the solves run. The state is zeroed
+// once when its buffer is made; the kernel's last block resets its counter.
 int plan_spmv(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const float *x, float *y) {
   const int lanes = lanes_spmv(ctx, plan);
   const int g = grid_spmv(ctx, (int64_t)plan->nV * lanes / 32 + 1);
-  if (lanes == 4)
-    BT_LAUNCH(ctx, k_spmv_blk_g<4>, g, 256, 0, plan->nV, plan->brp, plan->bcol, values, x, y, plan->pinned);
-  else if (lanes == 16)
-    BT_LAUNCH(ctx, k_spmv_blk_g<16>, g, 256, 0, plan->nV, plan->brp, plan->bcol, values, x, y, plan->pinned);
-  else
-    BT_LAUNCH(ctx, k_spmv_blk_g<8>, g, 256, 0, plan->nV, plan->brp, plan->bcol, values, x, y, plan->pinned);
+  const size_t o_st = (sizeof(double) * g + 255) & ~size_t(255);
+  const size_t need = o_st + sizeof(PcgState);
+  if (plan->w_spmv.bytes < need) {
+    BT_CHECK(plan->w_spmv.ensure(need));
+    BT_CUDA(cudaMemsetAsync(plan->w_spmv.p, 0, plan->w_spmv.bytes, ctx->stream));
+  }
+  double *part = plan->w_spmv.as<double>();
+  PcgState *st = reinterpret_cast<PcgState *>(plan->w_spmv.as<char>() + o_st);
+#define BT_SPMV(G)                                                                                              \
+  BT_LAUNCH(ctx, k_pcg_spmv_blk<G>, g, 256, 0, plan->nV, plan->brp, plan->bcol, values, x, x, y, plan->pinned, \
+            part, st)
+  if (lanes == 4) BT_SPMV(4);
+  else if (lanes == 16) BT_SPMV(16);
+  else BT_SPMV(8);
+#undef BT_SPMV
   return BARTELS_OK;
 }
 

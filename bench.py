@@ -284,15 +284,16 @@ def run_gpu(args, rank, world):
     spmv_bytes = 4 * nnz + 4 * nnzb + 4 * (nV + 1) + 12 * nV + 12 * nV
     qd = torch.from_numpy(V.ravel().copy()).to(f"cuda:{dev}")
     model_id = bg.api.MODELS[args.model]
-    hess_s = time_launch(lambda: _lib.check(L.bartels_plan_hessian_d(ctx.handle, plan.handle, model_id, psd, 1e-6, 0,
-                                                                     1.0, 0.0, C.c_void_p(qd.data_ptr()), None),
-                                            "hess"), 5)
-    # dq2 byte counts (n=96: 0.84 GB and 10.0 GB): compulsory = tet inputs (64 B) + vertex
-    # positions (12 B) + CSR values written (4 B); algorithmic = the traffic of the two-kernel
-    # formulation (element kernel 64 T + 12 V + 576 T written; reduction kernel 576 T read +
-    # 4 nnz written + 576 T of scatter map), which the fused kernel does not move
+
+    def hess_time(psd_mode):
+        return time_launch(lambda: _lib.check(L.bartels_plan_hessian_d(ctx.handle, plan.handle, model_id, psd_mode,
+                                                                       1e-6, 0, 1.0, 0.0, C.c_void_p(qd.data_ptr()),
+                                                                       None), "hess"), 5)
+    hess_off_s = hess_time(_lib.PSD_NONE)
+    hess_on_s = hess_time(_lib.PSD_SIMPLE_FIX)
+    # dq2 compulsory bytes (n=96: 0.84 GB): tet records (64 B) + vertex positions
+    # (12 B) + CSR values written (4 B each)
     hess_bytes = 64 * nT + 12 * nV + 4 * nnz
-    hess_alg_bytes = 64 * nT + 12 * nV + 576 * nT + 576 * nT + 4 * nnz + 4 * 144 * nT
     peak, peak_kind = peaks()
     spmv_gbs = spmv_bytes / spmv_s / 1e9
     traffic = None
@@ -383,15 +384,14 @@ def run_gpu(args, rank, world):
         "newton_iterations": newton_its, "pcg_iterations": pcg_its,
         "pcg_iters_per_newton": pcg_its / max(newton_its, 1),
         "roofline": {"bound": "hbm", "achieved": spmv_gbs, "peak": peak, "unit": "GB/s",
-                     "frac": spmv_gbs / peak, "traffic": traffic, "kernel": "k_spmv_blk (PCG SpMV, FP32 BCSR3)",
+                     "frac": spmv_gbs / peak, "traffic": traffic, "kernel": "k_pcg_spmv_blk (in-loop PCG SpMV, FP32 BCSR3)",
                      "bytes_per_launch": spmv_bytes, "us_per_launch": spmv_s * 1e6, "peak_source": peak_kind},
-        "kernels": {"dq2_fused_assembly": {"us_per_launch": hess_s * 1e6, "state": "rest (q = X), PSD on",
-                                           "compulsory_bytes": hess_bytes,
-                                           "achieved_gbs": hess_bytes / hess_s / 1e9,
-                                           "frac": hess_bytes / hess_s / 1e9 / peak,
-                                           "algorithmic_bytes": hess_alg_bytes,
-                                           "algorithmic_gbs": hess_alg_bytes / hess_s / 1e9,
-                                           "algorithmic_frac": hess_alg_bytes / hess_s / 1e9 / peak}},
+        "kernels": {"dq2_psd_off": {"us_per_launch": hess_off_s * 1e6, "state": "rest (q = X)",
+                                    "compulsory_bytes": hess_bytes, "achieved_gbs": hess_bytes / hess_off_s / 1e9,
+                                    "frac": hess_bytes / hess_off_s / 1e9 / peak, "bound": "hbm"},
+                    "dq2_psd_on": {"us_per_launch": hess_on_s * 1e6, "state": "rest (q = X)",
+                                   "compulsory_bytes": hess_bytes, "achieved_gbs": hess_bytes / hess_on_s / 1e9,
+                                   "frac": hess_bytes / hess_on_s / 1e9 / peak}},
         "jacobi_pcg": jacobi_pcg,
         "learned_precond": None if net is None else {
             "factor_build_ms_per_newton": 1e3 * main_arm["t_precond"] / max(newton_its, 1),

@@ -371,7 +371,12 @@ int bartels_newton_gradient_d(bartels_ctx ctx, bartels_mesh_plan plan, const bar
  * this library) to minimise log of Kaporin's condition number of G H G^T,
  * estimated with probe vectors, on Hessians the Newton solver produces. */
 typedef struct bartels_lpcg_s *bartels_lpcg;
-enum { BARTELS_PRECOND_BLOCK_JACOBI = 0, BARTELS_PRECOND_LEARNED = 1 };
+enum {
+  BARTELS_PRECOND_BLOCK_JACOBI = 0,
+  BARTELS_PRECOND_LEARNED = 1,            /* M^-1 = G^T G, the network's factor */
+  BARTELS_PRECOND_MULTIGRID = 2,          /* aggregation multigrid V-cycle, block-Jacobi smoothing */
+  BARTELS_PRECOND_LEARNED_MULTIGRID = 3   /* the same V-cycle with the network's G^T G as fine smoother */
+};
 
 int bartels_lpcg_create(bartels_ctx ctx, bartels_lpcg *out);
 int bartels_lpcg_destroy(bartels_lpcg net);
@@ -396,9 +401,26 @@ int bartels_lpcg_outputs(bartels_lpcg net, bartels_mesh_plan plan, const float *
 /* Number of lower (j <= v) and upper (j >= v) blocks of the plan's pattern. */
 int bartels_plan_factor_size(bartels_mesh_plan plan, int64_t *nnzl_blocks, int64_t *nnzu_blocks);
 /* Preconditioner of the plan's PCG solves (Newton and bartels_plan_pcg_d):
- * BARTELS_PRECOND_BLOCK_JACOBI, or BARTELS_PRECOND_LEARNED with net (block-
- * Jacobi is the fallback when the learned solve does not converge). */
+ * BARTELS_PRECOND_BLOCK_JACOBI; BARTELS_PRECOND_LEARNED with net;
+ * BARTELS_PRECOND_MULTIGRID (net ignored): one V-cycle of aggregation
+ * multigrid per PCG iteration (greedy aggregates of the free vertices, the
+ * six rigid-body modes per aggregate as the tentative prolongator, Galerkin
+ * coarse levels, Chebyshev smoothing, a dense coarsest solve; the hierarchy
+ * is built on the first solve and again whenever the pinned set changes);
+ * BARTELS_PRECOND_LEARNED_MULTIGRID with net: the same V-cycle with the
+ * network's M = G^T G as the smoother of the finest level. Block-Jacobi is
+ * the fallback when a learned or multigrid solve does not converge, and the
+ * preconditioner of systems too small for a coarse level. No counterpart in
+ * the reference (its solver is Eigen::SparseLU). */
 int bartels_plan_set_preconditioner(bartels_mesh_plan plan, int kind, bartels_lpcg net);
+/* z_d = B r_d: one application of the plan's multigrid preconditioner
+ * (BARTELS_PRECOND_MULTIGRID or _LEARNED_MULTIGRID) built for the Hessian
+ * values_d (FP32, the plan's CSR order, device); FP32 device vectors of 3nV,
+ * rows of pinned vertices zero. For tests of the preconditioner itself
+ * (symmetry, positivity). levels (host, may be NULL) receives the number of
+ * levels. No counterpart in the reference. */
+int bartels_plan_precond_apply_d(bartels_ctx ctx, bartels_mesh_plan plan, const float *values_d, const float *r_d,
+                                 float *z_d, int *levels);
 /* x_d = H^-1 b_d by PCG on the plan's Hessian (values_d, or NULL for the plan's
  * internal Hessian buffer) with the plan's preconditioner; device FP64 vectors,
  * rows of pinned vertices excluded. */
@@ -454,13 +476,16 @@ int bartels_tetmesh_dq_d(bartels_ctx ctx, bartels_mesh_plan plan, int model, con
 /* Gradient of the elastic energy (as bartels_tetmesh_dq, with the plan's
  * element data) at device positions q_d (3nV doubles) into device g_d (3nV),
  * without allocating any memory: for callers that cannot call cudaMalloc,
- * such as code running while a CUDA graph is being captured around it, memory
- * pools that forbid growth, or hosts that account every device allocation.
- * Its element-gradient scratch is a fixed array compiled into the library
- * (6 MiB, held by every GPU that loads it), so meshes of at most 65536 tets
- * are accepted; larger ones return BARTELS_E_UNSUPPORTED. The first call on a
- * device looks up the array's device address (make it before any stream
- * capture). All calls share the array: calls that overlap on the GPU race.
+ * such as a host application that reserves all device memory for its own
+ * pool at start-up, a time-stepping loop that must not take cudaMalloc's
+ * implicit device synchronisation, or a host that accounts every device
+ * allocation. Its element-gradient scratch is a fixed array compiled into the
+ * library (6 MiB, held by every GPU that loads it until the process exits),
+ * so meshes of at most 65536 tets are accepted; larger ones return
+ * BARTELS_E_UNSUPPORTED. The first call on a device looks up the array's
+ * device address and keeps it for the life of the process (make that first
+ * call before any stream capture; a device reset invalidates the address).
+ * All calls share the array: calls that overlap on the GPU race.
  * This entry point has no counterpart in the reference. */
 int bartels_tetmesh_dq_noalloc_d(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q_d,
                                  double *g_d);

@@ -1,7 +1,7 @@
 """Regenerate the golden fixtures in this folder from the reference's data files.
 
-Reads (read-only) the reference checkout given as argv[1] (default: the
-reference mount of the build machine) and writes compressed .npz fixtures:
+Reads (read-only) the Bartels source tree given as the one required argument
+and writes compressed .npz fixtures:
 
 * coarser_bunny.npz   V (500,3), E (1518,4) 0-based  <- data/meshes_mesh/coarser_bunny.mesh
 * tet.npz, two_tets.npz                               <- data/meshes_mesh/{tet,two_tets}.mesh
@@ -95,4 +95,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the Bartels source tree>")
+    main(sys.argv[1])

@@ -1,7 +1,8 @@
 """bartels_tetmesh_dq_noalloc_d: the gradient entry point for callers that
-cannot allocate device memory (code running inside a CUDA graph capture,
-fixed-size memory pools, hosts that account every allocation). It must give
-the same gradient as bartels_tetmesh_dq, call after call, without allocating.
+cannot allocate device memory (hosts that reserve all device memory for their
+own pool, loops that must not take cudaMalloc's implicit synchronisation,
+hosts that account every allocation). It must give the same gradient as
+bartels_tetmesh_dq, call after call, for every law, without allocating.
 
 Kept in its own file so that pytest collects it last."""
 import ctypes as C
@@ -21,11 +22,10 @@ def test_noalloc_gradient_matches_existing_entry_point():
     L = bg.lib()
     V, E = kuhn_cube(6)  # 1296 tets
     rng = np.random.default_rng(31)
-    for model in ("neohookean", "stvk", "corotational"):
+    for model in bg.api.MODELS:
         params = material_params(model, len(E), 2e6, 0.45)
         plan = bg.MeshPlan(V, E)
         plan.set_element_data(params=params)
-        free_after_first = None
         for call in range(2):
             q = (V + rng.uniform(-0.01, 0.01, V.shape)).ravel()
             g_ref = plan.dq(model, q)  # the existing entry point
@@ -43,8 +43,6 @@ def test_noalloc_gradient_matches_existing_entry_point():
             if call == 1:
                 # the second call cannot have taken device memory
                 assert torch.cuda.mem_get_info()[0] == free_before
-            free_after_first = free_before
-        assert free_after_first is not None
         plan.close()
 
 
