@@ -17,7 +17,7 @@ CONVERGED, MAX_ITERATIONS_REACHED = 0, 1
 NEOHOOKEAN, STVK, COROTATIONAL, NEOHOOKEAN_ISOCHORIC, ARAP, LINEAR_ELASTICITY = 0, 1, 2, 3, 4, 5
 PSD_NONE, PSD_SIMPLE_FIX = 0, 1
 DQ2_COROT_EXACT = 1
-PRECOND_BLOCK_JACOBI, PRECOND_LEARNED = 0, 1
+PRECOND_BLOCK_JACOBI, PRECOND_LEARNED, PRECOND_MULTIGRID, PRECOND_LEARNED_MULTIGRID = 0, 1, 2, 3
 
 
 class BartelsError(RuntimeError):
@@ -106,8 +106,12 @@ SIGNATURES = [
     ("bartels_lpcg_outputs", C.c_int, [_P, _P, _P, _P, _P]),
     ("bartels_plan_factor_size", C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     ("bartels_plan_set_preconditioner", C.c_int, [_P, C.c_int, _P]),
+    ("bartels_plan_precond_apply_d", C.c_int, [_P, _P, _P, _P, _P, _I]),
+    ("bartels_plan_mg_info", C.c_int, [_P, C.c_int, _I, _I, C.POINTER(C.c_int64), _I]),
     ("bartels_plan_pcg_d", C.c_int, [_P, _P, _P, _P, _P, C.POINTER(PcgParams), C.POINTER(PcgReport)]),
     ("bartels_newton_gradient_d", C.c_int, [_P, _P, C.POINTER(NewtonParams), _P, _P]),
+    ("bartels_newton_energy_d", C.c_int, [_P, _P, C.POINTER(NewtonParams), _P, _D]),
+    ("bartels_newton_get_problem", C.c_int, [_P, _D, _D]),
     ("bartels_plan_autotune", C.c_int, [_P, _P, _P, C.c_int, _I, _I]),
     ("bartels_segment_sumsq_d", C.c_int, [_P, C.c_int, _P, _P, _P]),
     ("bartels_gemm_bf16_d", C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, C.c_int, _P, _P, C.c_int, _P, C.c_int]),
@@ -129,6 +133,7 @@ SIGNATURES = [
     ("bartels_plan_assemble_matrix", C.c_int, [_P, _P, _D, _D]),
     ("bartels_plan_assemble_vector", C.c_int, [_P, _P, _D, _D]),
     ("bartels_tetmesh_dq_d", C.c_int, [_P, _P, C.c_int, _P, _P]),
+    ("bartels_tetmesh_q_elements_d", C.c_int, [_P, _P, C.c_int, _P, _P]),
     ("bartels_mex_routine_count", C.c_int, []),
     ("bartels_mex_routine_name", C.c_char_p, [C.c_int]),
     ("bartels_mex_release", None, []),

@@ -623,13 +623,34 @@ k_mg_dense_inv(int nodes, const int *__restrict__ rp, const int *__restrict__ ci
   }
 }
 
+__device__ __forceinline__ void apply_dinv6(const float *__restrict__ dinv, int I, const float r[6], float z[6]) {
+  const float4 *m4 = reinterpret_cast<const float4 *>(dinv + 36ll * I);
+  float m[36];
+#pragma unroll
+  for (int q = 0; q < 9; ++q) {
+    const float4 t = __ldg(m4 + q);
+    m[4 * q] = t.x; m[4 * q + 1] = t.y; m[4 * q + 2] = t.z; m[4 * q + 3] = t.w;
+  }
+#pragma unroll
+  for (int a = 0; a < 6; ++a) {
+    float s = 0.f;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) s += m[6 * a + c] * r[c];
+    z[a] = s;
+  }
+}
+
 // ============================================================= transfers ===
 // b_c[I] = sum over members v of Q_v^T r_v: 8 lanes per aggregate (members
 // strided over the lanes, fixed shuffle tree).
+// With cdinv set it also takes the coarse level's first smoothing step from
+// x = 0 (x = c Dinv b, r = b, d = x; c = ccoef[0], or 1 without ccoef).
 template <int BSF>
 __global__ void __launch_bounds__(256)
 k_mg_restrict(int nc, const int *__restrict__ mptr, const int *__restrict__ midx, const float *__restrict__ Q,
-              const float *__restrict__ r, float *__restrict__ bc, const PcgState *__restrict__ st) {
+              const float *__restrict__ r, float *__restrict__ bc, const float *__restrict__ cdinv,
+              float *__restrict__ cx, float *__restrict__ cr, float *__restrict__ cd, const float *__restrict__ ccoef,
+              const PcgState *__restrict__ st) {
   if (st && st->done) return;
   const int lane = threadIdx.x & 31, sl = lane & 7, g = lane >> 3;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -654,9 +675,22 @@ k_mg_restrict(int nc, const int *__restrict__ mptr, const int *__restrict__ midx
     for (int o = 4; o > 0; o >>= 1)
 #pragma unroll
       for (int c = 0; c < 6; ++c) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
-    if (I < nc && sl == 0)
+    if (I < nc && sl == 0) {
 #pragma unroll
       for (int c = 0; c < 6; ++c) bc[6 * I + c] = acc[c];
+      if (cdinv) {
+        const float cf = ccoef ? ccoef[0] : 1.f;
+        float z[6];
+        apply_dinv6(cdinv, I, acc, z);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+          const float xv = cf * z[c];
+          cx[6 * I + c] = xv;
+          if (cr) cr[6 * I + c] = acc[c];
+          if (cd) cd[6 * I + c] = xv;
+        }
+      }
+    }
   }
 }
 
@@ -697,6 +731,46 @@ k_mg0_bj(int nV, const float *__restrict__ minv, const float *__restrict__ r, fl
     apply_minv(minv, v, rv, zv);
 #pragma unroll
     for (int k = 0; k < 3; ++k) x[3 * v + k] = c * zv[k];
+  }
+}
+
+// The PCG update fused with the level-0 pre-smoothing of the block-Jacobi
+// V-cycle: x += alpha p; r -= alpha Ap; x0 = c Dinv r (c = coef[0]); partial
+// sums of r.r. The last block stores r.r, advances the iteration count and
+// applies the convergence test, as k_pcg_update_f does.
+__global__ void __launch_bounds__(256)
+k_mg0_update(int nV, const float *__restrict__ pa, const float *__restrict__ pb, const float *__restrict__ ap,
+             float *__restrict__ x, float *__restrict__ r, const float *__restrict__ minv, float *__restrict__ x0,
+             const float *__restrict__ coef, double *__restrict__ part, PcgState *__restrict__ st) {
+  if (st->done) return;
+  const int it = st->it;
+  const float *p = (it & 1) ? pb : pa;
+  const float alpha = st->alpha, c = coef[0];
+  float arr = 0.f;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nV; v += gridDim.x * blockDim.x) {
+    float rv[3], zv[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int i = 3 * v + k;
+      x[i] += alpha * __ldcg(p + i);
+      rv[k] = r[i] - alpha * __ldcg(ap + i);
+      r[i] = rv[k];
+      arr += rv[k] * rv[k];
+    }
+    apply_minv(minv, v, rv, zv);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) x0[3 * v + k] = c * zv[k];
+  }
+  double s = cta_sum_f(arr);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+  if (last_block(&st->count)) {
+    const double rr = sum_partials(part, gridDim.x);
+    if (threadIdx.x == 0) {
+      st->rr = rr;
+      st->it = it + 1;
+      if (rr <= st->tol2 || it + 1 >= st->max_it || !(rr == rr)) st->done = 1;
+      st->count = 0;
+    }
   }
 }
 
@@ -873,22 +947,6 @@ __device__ __forceinline__ void group_reduce6(float s[6]) {
     for (int r = 0; r < 6; ++r) s[r] += __shfl_xor_sync(0xffffffffu, s[r], o);
 }
 
-__device__ __forceinline__ void apply_dinv6(const float *__restrict__ dinv, int I, const float r[6], float z[6]) {
-  const float4 *m4 = reinterpret_cast<const float4 *>(dinv + 36ll * I);
-  float m[36];
-#pragma unroll
-  for (int q = 0; q < 9; ++q) {
-    const float4 t = __ldg(m4 + q);
-    m[4 * q] = t.x; m[4 * q + 1] = t.y; m[4 * q + 2] = t.z; m[4 * q + 3] = t.w;
-  }
-#pragma unroll
-  for (int a = 0; a < 6; ++a) {
-    float s = 0.f;
-#pragma unroll
-    for (int c = 0; c < 6; ++c) s += m[6 * a + c] * r[c];
-    z[a] = s;
-  }
-}
 
 #define BT_CROW_LOOP_BEGIN(G)                                                   \
   const int lane_ = threadIdx.x & 31, sl = lane_ % (G), gw_ = lane_ / (G);     \
@@ -1107,10 +1165,12 @@ float *level_result(const MgHierarchy *mg, int l) {
   return coarsest ? mg->lv[l].x : mg->lv[l].x2;
 }
 
-// Chebyshev smoothing of a coarse level from x = 0 (deg steps): x, r, d
-int cheb_from_zero(bartels_ctx ctx, const MgLevel &c, const float *coef, const PcgState *st) {
+// Chebyshev smoothing of a coarse level from x = 0 (deg steps): x, r, d. The
+// first step is skipped when the restriction into the level has taken it.
+int cheb_from_zero(bartels_ctx ctx, const MgLevel &c, const float *coef, bool first_done, const PcgState *st) {
   const int gr = grid_rows(ctx, c.n, kGc);
-  BT_LAUNCH(ctx, k_mgc_first, grid_n(ctx, c.n), 256, 0, c.n, c.dinv, c.b, c.x, c.r, c.d, coef, st);
+  if (!first_done)
+    BT_LAUNCH(ctx, k_mgc_first, grid_n(ctx, c.n), 256, 0, c.n, c.dinv, c.b, c.x, c.r, c.d, coef, st);
   float *dc = c.d, *dn = c.d2;
   for (int j = 1; j < c.deg; ++j) {
     BT_LAUNCH(ctx, k_mgc_cheb<kGc>, gr, 256, 0, c.n, c.rp, c.ci, c.val, c.dinv, dc, dn, c.r, c.x, coef, j, st);
@@ -1119,7 +1179,29 @@ int cheb_from_zero(bartels_ctx ctx, const MgLevel &c, const float *coef, const P
   return BARTELS_OK;
 }
 
-int enqueue_coarse(bartels_ctx ctx, MgHierarchy *mg, int l, const PcgState *st) {
+// Restriction into level l (from level l - 1's residual r with its transfer
+// blocks), taking level l's first smoothing step in the same kernel where that
+// step is local (every level but a dense coarsest). Returns whether it did.
+template <int BSF>
+int restrict_into(bartels_ctx ctx, MgHierarchy *mg, const MgLevel &f, const float *r, int l, const PcgState *st,
+                  bool *first_done) {
+  MgLevel &c = mg->lv[l];
+  const bool last = l + 1 == (int)mg->lv.size();
+  const bool fuse = !(last && mg->dense);
+  const bool exact = last && mg->coarse_blockdiag;  // x = Dinv b
+  const float *coef = exact ? nullptr : mg->coef + kMgCoef * l;
+  const int g = grid_rows(ctx, (c.n + 3) / 4, 32);
+  if (fuse)
+    BT_LAUNCH(ctx, k_mg_restrict<BSF>, g, 256, 0, c.n, f.mptr, f.midx, f.Q, r, c.b, (const float *)c.dinv, c.x,
+              exact ? (float *)nullptr : c.r, exact ? (float *)nullptr : c.d, coef, st);
+  else
+    BT_LAUNCH(ctx, k_mg_restrict<BSF>, g, 256, 0, c.n, f.mptr, f.midx, f.Q, r, c.b, (const float *)nullptr,
+              (float *)nullptr, (float *)nullptr, (float *)nullptr, (const float *)nullptr, st);
+  *first_done = fuse;
+  return BARTELS_OK;
+}
+
+int enqueue_coarse(bartels_ctx ctx, MgHierarchy *mg, int l, bool first_done, const PcgState *st) {
   MgLevel &c = mg->lv[l];
   const float *coef = mg->coef + kMgCoef * l;
   const int last = (int)mg->lv.size() - 1;
@@ -1127,20 +1209,20 @@ int enqueue_coarse(bartels_ctx ctx, MgHierarchy *mg, int l, const PcgState *st) 
     if (mg->dense) {
       BT_LAUNCH(ctx, k_mg_dense_apply, 1, 256, 0, mg->nd, mg->ainv, c.b, c.x, st);
     } else if (mg->coarse_blockdiag) {
-      BT_LAUNCH(ctx, k_mgc_first, grid_n(ctx, c.n), 256, 0, c.n, c.dinv, c.b, c.x, (float *)nullptr,
-                (float *)nullptr, (const float *)nullptr, st);
+      if (!first_done)
+        BT_LAUNCH(ctx, k_mgc_first, grid_n(ctx, c.n), 256, 0, c.n, c.dinv, c.b, c.x, (float *)nullptr,
+                  (float *)nullptr, (const float *)nullptr, st);
     } else {
-      BT_CHECK(cheb_from_zero(ctx, c, coef, st));
+      BT_CHECK(cheb_from_zero(ctx, c, coef, first_done, st));
     }
     return BARTELS_OK;
   }
-  MgLevel &nx = mg->lv[l + 1];
   const int gr = grid_rows(ctx, c.n, kGc);
-  BT_CHECK(cheb_from_zero(ctx, c, coef, st));
+  BT_CHECK(cheb_from_zero(ctx, c, coef, first_done, st));
   BT_LAUNCH(ctx, k_mgc_resid<kGc>, gr, 256, 0, c.n, c.rp, c.ci, c.val, c.b, c.x, c.r, st);
-  BT_LAUNCH(ctx, k_mg_restrict<6>, grid_rows(ctx, (nx.n + 3) / 4, 32), 256, 0, nx.n, c.mptr, c.midx, c.Q, c.r, nx.b,
-            st);
-  BT_CHECK(enqueue_coarse(ctx, mg, l + 1, st));
+  bool next_first = false;
+  BT_CHECK(restrict_into<6>(ctx, mg, c, c.r, l + 1, st, &next_first));
+  BT_CHECK(enqueue_coarse(ctx, mg, l + 1, next_first, st));
   BT_LAUNCH(ctx, k_mg_prolong<6>, grid_n(ctx, c.n), 256, 0, c.n, c.agg, c.Q, level_result(mg, l + 1), c.x, st);
   BT_LAUNCH(ctx, k_mgc_post_first<kGc>, gr, 256, 0, c.n, c.rp, c.ci, c.val, c.dinv, c.b, c.x, c.x2, c.r, c.d, coef,
             st);
@@ -1256,22 +1338,30 @@ int mg_setup_numeric(bartels_ctx ctx, bartels_mesh_plan plan, const float *value
   return BARTELS_OK;
 }
 
-int mg_enqueue_apply(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const MgSmoother &sm,
-                     const float *r, float *z, float *y, double *part, PcgState *st) {
+int mg_enqueue_update(bartels_ctx ctx, bartels_mesh_plan plan, const MgSmoother &sm, const float *pa,
+                      const float *pb, const float *ap, float *x, float *r, double *part, PcgState *st) {
   MgHierarchy *mg = plan->mg;
-  MgLevel &l0 = mg->lv[0], &l1 = mg->lv[1];
+  BT_LAUNCH(ctx, k_mg0_update, grid_n(ctx, plan->nV), 256, 0, plan->nV, pa, pb, ap, x, r, sm.minv, mg->lv[0].x,
+            (const float *)mg->coef, part, st);
+  return BARTELS_OK;
+}
+
+int mg_enqueue_apply(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const MgSmoother &sm,
+                     const float *r, float *z, float *y, double *part, PcgState *st, bool pre_done) {
+  MgHierarchy *mg = plan->mg;
+  MgLevel &l0 = mg->lv[0];
   const float *c0 = mg->coef;
   const int nV = plan->nV;
   if (sm.gl) {
     BT_CHECK(fac_lower(ctx, plan, sm, r, y, st));
     BT_CHECK(fac_upper(ctx, plan, sm, y, nullptr, l0.x, c0, nullptr, nullptr, st));
-  } else {
+  } else if (!pre_done) {
     BT_LAUNCH(ctx, k_mg0_bj, grid_n(ctx, nV), 256, 0, nV, sm.minv, r, l0.x, c0, st);
   }
   BT_CHECK(resid0(ctx, plan, values, r, l0.x, l0.r, st));
-  BT_LAUNCH(ctx, k_mg_restrict<3>, grid_rows(ctx, (l1.n + 3) / 4, 32), 256, 0, l1.n, l0.mptr, l0.midx, l0.Q, l0.r,
-            l1.b, st);
-  BT_CHECK(enqueue_coarse(ctx, mg, 1, st));
+  bool first_done = false;
+  BT_CHECK(restrict_into<3>(ctx, mg, l0, l0.r, 1, st, &first_done));
+  BT_CHECK(enqueue_coarse(ctx, mg, 1, first_done, st));
   BT_LAUNCH(ctx, k_mg_prolong<3>, grid_n(ctx, nV), 256, 0, nV, l0.agg, l0.Q, level_result(mg, 1), l0.x, st);
   if (sm.gl) {
     BT_CHECK(resid0(ctx, plan, values, r, l0.x, l0.r, st));
@@ -1293,7 +1383,7 @@ int mg_apply_once(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, 
     BT_CHECK(dalloc_n(mg, &mg->st_once, 1));
     BT_CUDA(cudaMemsetAsync(mg->st_once, 0, sizeof(PcgState), ctx->stream));
   }
-  BT_CHECK(mg_enqueue_apply(ctx, plan, values, sm, r, z, mg->lv[0].d, mg->part, mg->st_once));
+  BT_CHECK(mg_enqueue_apply(ctx, plan, values, sm, r, z, mg->lv[0].d, mg->part, mg->st_once, false));
   BT_CUDA(cudaStreamSynchronize(ctx->stream));
   return BARTELS_OK;
 }

@@ -71,8 +71,15 @@ void mg_destroy(MgHierarchy *mg);
 int mg_setup_numeric(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const MgSmoother &sm);
 // z = B r (one V-cycle) for the PCG loop: every kernel is a no-op once st->done;
 // the last one also forms r.z, beta = r.z / r.z_old and stores r.z in st.
+// pre_done: the level-0 pre-smoothing was taken by mg_enqueue_update (block-
+// Jacobi smoother only).
 int mg_enqueue_apply(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const MgSmoother &sm,
-                     const float *r, float *z, float *y, double *part, PcgState *st);
+                     const float *r, float *z, float *y, double *part, PcgState *st, bool pre_done);
+// The PCG update (x += alpha p, r -= alpha Ap, r.r, iteration count and
+// convergence test) fused with the level-0 block-Jacobi pre-smoothing of the
+// next V-cycle.
+int mg_enqueue_update(bartels_ctx ctx, bartels_mesh_plan plan, const MgSmoother &sm, const float *pa,
+                      const float *pb, const float *ap, float *x, float *r, double *part, PcgState *st);
 // z = B r once (no PCG state), for tests of the preconditioner itself.
 int mg_apply_once(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const MgSmoother &sm, const float *r,
                   float *z);

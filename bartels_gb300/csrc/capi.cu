@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "devmath.cuh"
+#include "amg_internal.cuh"
 #include "internal.cuh"
 #include "lpcg_internal.cuh"
 
@@ -36,6 +37,8 @@ int plan_pcg(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const
              const bartels_pcg_params &prm, bartels_pcg_report *rep);
 int newton_gradient(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params &p, const double *x,
                     double *g);
+int newton_energy(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params &p, const double *x,
+                  double *energy_host);
 int plan_autotune(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, int force, int *spmv_out,
                   int *tri_out);
 int segment_sumsq(bartels_ctx ctx, int nseg, const int *off, const double *v, double *out);
@@ -618,6 +621,13 @@ int bartels_tetmesh_q_d(bartels_ctx ctx, bartels_mesh_plan plan, int model, cons
   return energy(ctx, plan, model, obj, q_d, energy_d);
 }
 
+int bartels_tetmesh_q_elements_d(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q_d,
+                                 double *e_d) {
+  BT_CHECK(check_plan(ctx, plan));
+  if (!valid_model(model) || !q_d || !e_d) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  return energy_elements(ctx, plan, model, q_d, e_d);
+}
+
 int bartels_tetmesh_dq_d(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q_d, double *g_d) {
   BT_CHECK(check_plan(ctx, plan));
   if (!valid_model(model) || !q_d || !g_d) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
@@ -732,6 +742,45 @@ int bartels_newton_gradient_d(bartels_ctx ctx, bartels_mesh_plan plan, const bar
   BT_CHECK(check_plan(ctx, plan));
   if (!params || !x_d || !g_d || !valid_model(params->model)) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
   return newton_gradient(ctx, plan, *params, x_d, g_d);
+}
+
+int bartels_newton_get_problem(bartels_mesh_plan plan, double *q_base, double *x_hat) {
+  if (!plan) return fail(BARTELS_E_INVALID_ARG, "null plan");
+  BT_CHECK(check_ctx(plan->ctx));
+  const size_t n = 3 * (size_t)plan->nV;
+  BT_CUDA(cudaStreamSynchronize(plan->ctx->stream));
+  auto get = [&](double *dst, const double *src) -> int {
+    if (!dst) return BARTELS_OK;
+    if (!src) {
+      std::memset(dst, 0, sizeof(double) * n);
+      return BARTELS_OK;
+    }
+    BT_CUDA(cudaMemcpy(dst, src, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    return BARTELS_OK;
+  };
+  BT_CHECK(get(q_base, plan->q_base));
+  return get(x_hat, plan->x_hat);
+}
+
+int bartels_newton_energy_d(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params *params,
+                            const double *x_d, double *energy) {
+  BT_CHECK(check_plan(ctx, plan));
+  if (!params || !x_d || !energy || !valid_model(params->model)) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  return newton_energy(ctx, plan, *params, x_d, energy);
+}
+
+int bartels_plan_mg_info(bartels_mesh_plan plan, int max_levels, int *levels, int *nodes, int64_t *blocks,
+                         int *coarsest) {
+  if (!plan || !plan->mg) return fail(BARTELS_E_INVALID_ARG, "the plan has no multigrid hierarchy");
+  const MgHierarchy *mg = plan->mg;
+  const int L = (int)mg->lv.size();
+  if (levels) *levels = L;
+  for (int l = 0; l < L && l < max_levels; ++l) {
+    if (nodes) nodes[l] = mg->lv[l].n;
+    if (blocks) blocks[l] = mg->lv[l].nnzb;
+  }
+  if (coarsest) *coarsest = mg->dense ? 0 : (mg->coarse_blockdiag ? 1 : 2);
+  return BARTELS_OK;
 }
 
 int bartels_plan_autotune(bartels_ctx ctx, bartels_mesh_plan plan, const float *values_d, int force,

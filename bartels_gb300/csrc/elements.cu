@@ -224,6 +224,18 @@ __global__ void k_energy(int nT, const TetRec64 *__restrict__ rec, const double 
   if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
 
+// Energy of every tet, psi(F) vol at positions q (linear_tet_*_q,
+// src/linear_tet_neohookean_q.cpp:5-18): the per-element terms k_energy sums.
+template <int MODEL>
+__global__ void k_energy_elem(int nT, const TetRec64 *__restrict__ rec, const double *__restrict__ q,
+                              const double *__restrict__ X, double *__restrict__ e) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nT; t += gridDim.x * blockDim.x) {
+    double H[9];
+    disp_grad64(rec[t], q, nullptr, 1.0, X, nullptr, 0.0, H);
+    e[t] = psi_model_disp<double>(MODEL, H, rec[t].pv);
+  }
+}
+
 // f(x + alpha d) - f(x) of the objective, element by element, so that the
 // constant part of f (which dominates |f| near a minimum) cancels exactly:
 // per tet psi(H1) - psi(H0), alpha d^T M (x - x_hat) + alpha^2/2 d^T M d,
@@ -772,6 +784,24 @@ int dot(bartels_ctx ctx, const double *a, const double *b, int n, double *out) {
   const int g = grid_for(ctx, n, 256) < kRedBlocks ? grid_for(ctx, n, 256) : kRedBlocks;
   BT_LAUNCH(ctx, k_dot_partials, g, 256, 0, n, a, b, ctx->partials.as<double>());
   return reduce_sum(ctx, ctx->partials.as<double>(), g, out);
+}
+
+int energy_elements(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q, double *e) {
+  if (plan->nT == 0) return BARTELS_OK;
+  const int g = grid_for(ctx, plan->nT, 256);
+  const double *X = plan->dphi_matches_rest ? plan->X : nullptr;
+#define BT_EE(M) BT_LAUNCH(ctx, k_energy_elem<M>, g, 256, 0, plan->nT, plan->rec64, q, X, e)
+  switch (model) {
+    case MODEL_NH: BT_EE(MODEL_NH); break;
+    case MODEL_STVK: BT_EE(MODEL_STVK); break;
+    case MODEL_COROT: BT_EE(MODEL_COROT); break;
+    case MODEL_NH_ISO: BT_EE(MODEL_NH_ISO); break;
+    case MODEL_ARAP: BT_EE(MODEL_ARAP); break;
+    case MODEL_LE: BT_EE(MODEL_LE); break;
+    default: return fail(BARTELS_E_INVALID_ARG, "unknown model");
+  }
+#undef BT_EE
+  return BARTELS_OK;
 }
 
 int energy(bartels_ctx ctx, bartels_mesh_plan plan, int model, const ObjectiveDev &obj, const double *x,

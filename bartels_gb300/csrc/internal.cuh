@@ -182,6 +182,8 @@ struct ObjectiveDev {
 // returned through the pinned scalar if host_out != nullptr.
 int energy(bartels_ctx ctx, bartels_mesh_plan plan, int model, const ObjectiveDev &obj, const double *x,
            double *d_out);
+// energy of every tet (nT doubles) at positions q
+int energy_elements(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q, double *e);
 int gradient(bartels_ctx ctx, bartels_mesh_plan plan, int model, const ObjectiveDev &obj, const double *x,
              double *g);
 // f(x + alpha dx) - f(x), element by element (line search)

@@ -22,6 +22,7 @@ struct PcgState {
   int done;
   int max_it;
   unsigned int count;   // blocks finished (last-block reductions)
+  unsigned int loops;   // device-driven loop: body executions of the current inner solve
 };
 
 // 3x3 block-Jacobi apply: minv holds m00 m11 m22 m01 m02 m12 of each vertex's

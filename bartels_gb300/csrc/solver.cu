@@ -174,6 +174,7 @@ __global__ void k_pcg_init(int nb, int n, const float *__restrict__ rres, const 
       st->alpha = 0.f;
       st->tol2 = fmax(inner_rel2 * rr, abs_tol2);
       if (!cont) st->it = 0;
+      st->loops = 0;
       st->max_it = st->it + max_it;
       st->done = (rr <= st->tol2 || max_it <= 0 || !(rr == rr)) ? 1 : 0;
       st->count = 0;
@@ -673,6 +674,7 @@ __global__ void k_pcg_init_f(int n, const float *__restrict__ rres, float *__res
       st->beta = 0.f;
       st->tol2 = fmax(inner_rel2 * rr, abs_tol2);
       if (!cont) st->it = 0;
+      st->loops = 0;
       st->max_it = st->it + max_it;
       st->done = (rr <= st->tol2 || max_it <= 0 || !(rr == rr)) ? 1 : 0;
       st->count = 0;
@@ -752,8 +754,8 @@ static int pcg_enqueue_prec(bartels_ctx ctx, const PcgOperator &op, const PcgWor
 }
 
 // z = B r (V-cycle; its last kernel forms r.z and beta), then p = z + beta p
-static int pcg_enqueue_mg(bartels_ctx ctx, const PcgOperator &op, const PcgWork &w, int n) {
-  BT_CHECK(mg_enqueue_apply(ctx, op.plan, op.values, op.sm, w.r, w.z, w.ap, w.part_b, w.st));
+static int pcg_enqueue_mg(bartels_ctx ctx, const PcgOperator &op, const PcgWork &w, int n, bool pre_done) {
+  BT_CHECK(mg_enqueue_apply(ctx, op.plan, op.values, op.sm, w.r, w.z, w.ap, w.part_b, w.st, pre_done));
   BT_LAUNCH(ctx, k_pcg_dir, grid_vec(ctx, (n + 3) / 4), 256, 0, n, w.z, w.pa, w.pb, w.st);
   return BARTELS_OK;
 }
@@ -780,8 +782,12 @@ static int pcg_enqueue_iters(bartels_ctx ctx, const PcgOperator &op, const PcgWo
     if (op.mg) {
       // p was formed at the end of the previous iteration (or at the start of the solve)
       BT_CHECK(pcg_spmv_blk(ctx, op, w, lanes, gs));
-      BT_LAUNCH(ctx, k_pcg_update_f, gd, 256, 0, n, w.pa, w.pb, w.ap, w.x, w.r, w.part_b, w.st);
-      BT_CHECK(pcg_enqueue_mg(ctx, op, w, n));
+      if (op.sm.gl) {
+        BT_LAUNCH(ctx, k_pcg_update_f, gd, 256, 0, n, w.pa, w.pb, w.ap, w.x, w.r, w.part_b, w.st);
+      } else {
+        BT_CHECK(mg_enqueue_update(ctx, op.plan, op.sm, w.pa, w.pb, w.ap, w.x, w.r, w.part_b, w.st));
+      }
+      BT_CHECK(pcg_enqueue_mg(ctx, op, w, n, !op.sm.gl));
       continue;
     }
     // with the factor preconditioner the direction is formed by k_pcg_prec_upper
@@ -805,6 +811,82 @@ static int pcg_enqueue_iters(bartels_ctx ctx, const PcgOperator &op, const PcgWo
                 w.st);
     }
   }
+  return BARTELS_OK;
+}
+
+// Loop condition of the device-driven inner solve: a CUDA graph while-node
+// whose body is one PCG iteration runs until the solve is done. The body count
+// is bounded independently of the iteration count (the iteration cap of the
+// state bounds both).
+__global__ void k_pcg_cond(cudaGraphConditionalHandle h, PcgState *st) {
+  const unsigned int loops = ++st->loops;
+  const bool more = !st->done && st->it < st->max_it && loops <= (unsigned int)st->max_it + 4u;
+  cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+
+static int launch_cond(bartels_ctx ctx, cudaGraphConditionalHandle h, PcgState *st) {
+  BT_LAUNCH(ctx, k_pcg_cond, 1, 1, 0, h, st);
+  return BARTELS_OK;
+}
+
+// Executable graph of the inner PCG loop. Preferred: one while-node whose body
+// is one iteration (*device_loop = true: a launch runs the inner solve to its
+// end with no host round trip and no iteration after convergence). Fallback:
+// a fixed run of `chunk` iterations whose kernels turn into no-ops once the
+// state is done. *launches: kernel launches per body / chunk.
+static int pcg_build_graph(bartels_ctx ctx, const PcgOperator &op, const PcgWork &w, int n, int nb, int chunk,
+                           cudaGraphExec_t *exec, int64_t *launches, bool *device_loop) {
+  *exec = nullptr;
+  *device_loop = false;
+  cudaGraph_t graph = nullptr;
+  BT_CUDA(cudaGraphCreate(&graph, 0));
+  cudaGraphConditionalHandle h;
+  cudaGraphNodeParams cp = {};
+  cudaGraphNode_t node;
+  cudaError_t e = cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault);
+  if (e == cudaSuccess) {
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    e = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &cp);
+  }
+  if (e == cudaSuccess) {
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    const int64_t before = ctx->launches;
+    e = cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      int s = pcg_enqueue_iters(ctx, op, w, n, nb, 1);
+      if (s == BARTELS_OK) s = launch_cond(ctx, h, w.st);
+      cudaGraph_t captured = nullptr;
+      e = cudaStreamEndCapture(ctx->stream, &captured);
+      *launches = ctx->launches - before;
+      ctx->launches = before;  // counted per executed body below
+      if (s != BARTELS_OK) {
+        cudaGraphDestroy(graph);
+        return s;
+      }
+      if (e == cudaSuccess) e = cudaGraphInstantiate(exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (e != cudaSuccess) return fail(BARTELS_E_DEVICE, std::string("PCG loop graph: ") + cudaGetErrorString(e));
+      *device_loop = true;
+      return BARTELS_OK;
+    }
+  }
+  // conditional nodes unavailable: fixed-length graph
+  cudaGetLastError();
+  cudaGraphDestroy(graph);
+  const int64_t before = ctx->launches;
+  BT_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  int s = pcg_enqueue_iters(ctx, op, w, n, nb, chunk);
+  e = cudaStreamEndCapture(ctx->stream, &graph);
+  *launches = ctx->launches - before;
+  ctx->launches = before;  // counted per graph launch below
+  if (s != BARTELS_OK) return s;
+  if (e != cudaSuccess) return fail(BARTELS_E_DEVICE, std::string("graph capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return fail(BARTELS_E_DEVICE, std::string("graph instantiate: ") + cudaGetErrorString(e));
   return BARTELS_OK;
 }
 
@@ -871,24 +953,11 @@ static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double
   }
   const double target = prm.rel_tol * bnorm;
   // CUDA graph of a fixed number of PCG iterations (kernels no-op once done)
-  // (a V-cycle iteration is ~30 launches: shorter graphs waste fewer no-op launches after convergence)
-  const int chunk = op.mg ? 8 : 16;
+  const int chunk = op.mg ? 8 : 16;  // fixed-length fallback only
   cudaGraphExec_t exec = nullptr;
   int64_t graph_launches = 0;
-  {
-    cudaGraph_t graph;
-    const int64_t launches_before = ctx->launches;
-    BT_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    int s = pcg_enqueue_iters(ctx, op, w, n, nb, chunk);
-    cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
-    graph_launches = ctx->launches - launches_before;
-    ctx->launches = launches_before;  // counted per graph launch below
-    if (s != BARTELS_OK) return s;
-    if (e != cudaSuccess) return fail(BARTELS_E_DEVICE, std::string("graph capture: ") + cudaGetErrorString(e));
-    e = cudaGraphInstantiate(&exec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (e != cudaSuccess) return fail(BARTELS_E_DEVICE, std::string("graph instantiate: ") + cudaGetErrorString(e));
-  }
+  bool device_loop = false;
+  BT_CHECK(pcg_build_graph(ctx, op, w, n, nb, chunk, &exec, &graph_launches, &device_loop));
   int status = BARTELS_OK;
   double rel = 0.0;
   PcgState hs{};
@@ -931,7 +1000,7 @@ static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double
     if (op.mg) {
       BT_LAUNCH(ctx, k_pcg_init_f, gv, 256, 0, n, w.rres, w.x, w.r, w.pa, w.pb, w.part_a, w.st,
                 prm.inner_rel_tol * prm.inner_rel_tol, abs2, prm.max_iters - rep->iterations, cont);
-      BT_CHECK(pcg_enqueue_mg(ctx, op, w, n));
+      BT_CHECK(pcg_enqueue_mg(ctx, op, w, n, false));
     } else if (op.gl) {
       BT_LAUNCH(ctx, k_pcg_init_f, gv, 256, 0, n, w.rres, w.x, w.r, w.pa, w.pb, w.part_a, w.st,
                 prm.inner_rel_tol * prm.inner_rel_tol, abs2, prm.max_iters - rep->iterations, cont);
@@ -942,9 +1011,17 @@ static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double
     }
     for (;;) {
       BT_CUDA(cudaGraphLaunch(exec, ctx->stream));
-      ctx->launches += graph_launches;
       BT_CUDA(cudaMemcpyAsync(&hs, w.st, sizeof(PcgState), cudaMemcpyDeviceToHost, ctx->stream));
       BT_CUDA(cudaStreamSynchronize(ctx->stream));
+      if (device_loop) {
+        ctx->launches += graph_launches * (int64_t)std::max(1u, hs.loops);
+        if (!hs.done) {
+          cudaGraphExecDestroy(exec);
+          return fail(BARTELS_E_DEVICE, "PCG loop ended before the solve was done");
+        }
+        break;
+      }
+      ctx->launches += graph_launches;
       if (hs.done) break;
     }
     rep->iterations += hs.it - it0;
@@ -1196,6 +1273,14 @@ int newton_iterate(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton
 int newton_gradient(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params &p, const double *x,
                     double *g) {
   return gradient(ctx, plan, p.model, objective_of(plan, p), x, g);
+}
+
+int newton_energy(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params &p, const double *x,
+                  double *energy_host) {
+  NewtonWork w;
+  BT_CHECK(newton_work(plan, w));
+  BT_CHECK(energy(ctx, plan, p.model, objective_of(plan, p), x, w.scal));
+  return read_scalar(ctx, w.scal, energy_host);
 }
 
 int newton_solve(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params &p, double *x,

@@ -133,8 +133,11 @@ class LearnedPreconditioner:
                                          gl.ctypes.data_as(C.c_void_p)), "bartels_lpcg_outputs")
         return raw.reshape(nl, 9), gl
 
-    def attach(self, plan: MeshPlan):
-        check(lib().bartels_plan_set_preconditioner(plan.handle, _lib.PRECOND_LEARNED, self.handle),
+    def attach(self, plan: MeshPlan, multigrid: bool = False):
+        """Make the network the plan's preconditioner: M^-1 = G^T G, or (multigrid)
+        the smoother of the finest level of the multigrid V-cycle."""
+        kind = _lib.PRECOND_LEARNED_MULTIGRID if multigrid else _lib.PRECOND_LEARNED
+        check(lib().bartels_plan_set_preconditioner(plan.handle, kind, self.handle),
               "bartels_plan_set_preconditioner")
 
     def save(self, path: str, **meta):
@@ -161,6 +164,31 @@ def factor_size(plan: MeshPlan):
 def use_block_jacobi(plan: MeshPlan):
     check(lib().bartels_plan_set_preconditioner(plan.handle, _lib.PRECOND_BLOCK_JACOBI, None),
           "bartels_plan_set_preconditioner")
+
+
+def use_multigrid(plan: MeshPlan):
+    """Aggregation multigrid V-cycle with block-Jacobi smoothing as the plan's preconditioner."""
+    check(lib().bartels_plan_set_preconditioner(plan.handle, _lib.PRECOND_MULTIGRID, None),
+          "bartels_plan_set_preconditioner")
+
+
+def precond_apply(plan: MeshPlan, values, r, z):
+    """z = B r with the plan's multigrid preconditioner built for values (device tensors); returns the level count."""
+    levels = C.c_int()
+    check(lib().bartels_plan_precond_apply_d(plan.ctx.handle, plan.handle, _ptr(values), _ptr(r), _ptr(z),
+                                             C.byref(levels)), "bartels_plan_precond_apply_d")
+    return levels.value
+
+
+def mg_info(plan: MeshPlan):
+    """Levels of the plan's multigrid hierarchy: {"nodes": [...], "blocks": [...], "coarsest": ...}."""
+    n = C.c_int()
+    nodes = (C.c_int * 16)()
+    blocks = (C.c_int64 * 16)()
+    co = C.c_int()
+    check(lib().bartels_plan_mg_info(plan.handle, 16, C.byref(n), nodes, blocks, C.byref(co)), "bartels_plan_mg_info")
+    return {"nodes": list(nodes[:n.value]), "blocks": list(blocks[:n.value]),
+            "coarsest": ["dense", "block-diagonal", "chebyshev"][co.value]}
 
 
 def plan_pcg(plan: MeshPlan, values, b, x, rel_tol=1e-8, max_iters=20000, inner_rel_tol=0.1, max_refinements=40,

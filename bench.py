@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-faithful-baseline", action="store_true",
                     help="skip the 1-thread reference-structured CPU sample beside the OpenMP baseline")
-    ap.add_argument("--precond", default="learned", choices=["learned", "jacobi"])
+    ap.add_argument("--precond", default="learned", choices=["learned", "jacobi", "multigrid", "learned_multigrid"])
     ap.add_argument("--weights", default=os.path.join(ROOT, "bartels_gb300", "weights", "lpcg_neohookean.npz"))
     ap.add_argument("--no-jacobi-arm", action="store_true", help="skip the block-Jacobi comparison run")
     ap.add_argument("--no-autotune", action="store_true", help="default lane counts instead of the autotuner's")
@@ -198,16 +198,23 @@ def run_gpu(args, rank, world):
         lanes = {"spmv": a_l.value, "factor": b_l.value}
         del hv, q0
     net = None
-    if args.precond == "learned":
+    if args.precond in ("learned", "learned_multigrid"):
         from bartels_gb300 import lpcg
         net = lpcg.LearnedPreconditioner.load(args.weights, ctx)
 
-    def timed_newton(use_learned):
-        """W warm-up and K timed Newton iterations from rest (fresh state)."""
-        if use_learned:
+    def set_precond(kind):
+        if kind == "learned":
             net.attach(plan)
+        elif kind == "learned_multigrid":
+            net.attach(plan, multigrid=True)
+        elif kind == "multigrid":
+            _lib.check(L.bartels_plan_set_preconditioner(plan.handle, _lib.PRECOND_MULTIGRID, None), "precond")
         else:
-            L.bartels_plan_set_preconditioner(plan.handle, _lib.PRECOND_BLOCK_JACOBI, None)
+            _lib.check(L.bartels_plan_set_preconditioner(plan.handle, _lib.PRECOND_BLOCK_JACOBI, None), "precond")
+
+    def timed_newton(kind):
+        """W warm-up and K timed Newton iterations from rest (fresh state)."""
+        set_precond(kind)
         plan.set_problem(q_base=qt, x_hat=vt, f_ext=f_g, pinned=pb["pinned"])
         x.zero_()
         state = {"g0": -1.0, "steps": 0}
@@ -250,10 +257,53 @@ def run_gpu(args, rank, world):
         return dict(ms=ms, launches=ctx.kernel_launches - launches0, clocks=clk.summary(), rep=rep,
                     newton_its=rep.iterations - before[0], pcg_its=rep.pcg_iterations - before[1],
                     ls_its=rep.ls_iterations - before[2], fallbacks=rep.precond_fallbacks - before[3],
-                    t_precond=rep.t_precond - before[4], steps=state["steps"])
+                    t_precond=rep.t_precond - before[4], steps=state["steps"], g0=state["g0"])
 
-    main_arm = timed_newton(net is not None)
-    jac = main_arm if net is None else (None if args.no_jacobi_arm else timed_newton(False))
+    def oracle_check(cw, arm):
+        """The FP64 oracle (CPU restatement) against the GPU at the state after the
+        timed iterations: the Newton objective's energy and gradient there; then
+        the time step is finished on the GPU (untimed) and the oracle's gradient
+        at its solution, relative to the step's initial gradient, is the
+        solution's error against the 1e-8 criterion."""
+        Dp = C.POINTER(C.c_double)
+        qb, xh = np.zeros(3 * nV), np.zeros(3 * nV)
+        _lib.check(L.bartels_newton_get_problem(plan.handle, qb.ctypes.data_as(Dp), xh.ctypes.data_as(Dp)), "state")
+        cw.set_state(qb, xh)
+        xs = x.cpu().numpy()
+        e_gpu = C.c_double()
+        _lib.check(L.bartels_newton_energy_d(ctx.handle, plan.handle, C.byref(prm), xp, C.byref(e_gpu)), "energy")
+        g_gpu = torch.empty_like(x)
+        _lib.check(L.bartels_newton_gradient_d(ctx.handle, plan.handle, C.byref(prm), xp,
+                                               C.c_void_p(g_gpu.data_ptr())), "gradient")
+        gg = g_gpu.cpu().numpy()
+        e_cpu, g_cpu = cw.cb.energy(xs), cw.cb.gradient(xs)
+        out = {"state": f"after the timed iterations (time step {arm['steps'] + 1} of the run, mid-solve)",
+               "energy_rel_err": abs(e_gpu.value - e_cpu) / abs(e_cpu),
+               "gradient_rel_err": float(np.linalg.norm(gg - g_cpu) / np.linalg.norm(g_cpu))}
+        g0 = arm["g0"] if arm["g0"] > 0 else float(np.linalg.norm(gg))
+        its, rep2 = 0, _lib.NewtonReport()
+        while its < 100:
+            done = C.c_int()
+            _lib.check(L.bartels_newton_iterate_d(ctx.handle, plan.handle, C.byref(prm), xp, g0, C.byref(done),
+                                                  C.byref(rep2)), "newton_iterate")
+            if done.value:
+                break
+            its += 1
+        g_sol = cw.cb.gradient(x.cpu().numpy())
+        out["time_step_solution"] = {"newton_iterations_to_finish": its, "criterion": 1e-8,
+                                     "fp64_relative_gradient": float(np.linalg.norm(g_sol) / g0)}
+        return out
+
+    main_arm = timed_newton(args.precond)
+    mg_levels = None
+    if args.precond in ("multigrid", "learned_multigrid"):
+        from bartels_gb300 import lpcg
+        mg_levels = lpcg.mg_info(plan)
+    cpu_work, oracle_err = None, None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu_work = CpuWorkload(pb, args)
+        oracle_err = oracle_check(cpu_work, main_arm)
+    jac = main_arm if args.precond == "jacobi" else (None if args.no_jacobi_arm else timed_newton("jacobi"))
     L.bartels_plan_set_preconditioner(plan.handle, _lib.PRECOND_BLOCK_JACOBI, None)
     ms, launches, rep = main_arm["ms"], main_arm["launches"], main_arm["rep"]
     pcg_its, newton_its = main_arm["pcg_its"], main_arm["newton_its"]
@@ -310,8 +360,7 @@ def run_gpu(args, rank, world):
     e2e = None
     if rank == 0 and args.e2e_steps > 0:
         plan.set_problem(q_base=qt, x_hat=vt, f_ext=f_g, pinned=pb["pinned"])
-        if net is not None:
-            net.attach(plan)
+        set_precond(args.precond)
         v_host = np.zeros(3 * nV)
         its = 0
         t = 0.0
@@ -347,22 +396,36 @@ def run_gpu(args, rank, world):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        ref_arm = jac if jac is not None else main_arm
-        counts = {"pcg_per_newton": ref_arm["pcg_its"] / max(ref_arm["newton_its"], 1),
-                  "ls_per_newton": ref_arm["ls_its"] / max(ref_arm["newton_its"], 1)}
-        est, parts, threads, _ = cpu_newton_sample(pb, args, counts)
-        cpu = {"value": 1.0 / est[0], "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": cpu_sample_text(counts, args.n).replace("from the GPU run of the same workload", "from this run"),
-               "components": parts}
+        # one whole Newton iteration of this workload (the first from rest) on the host cores, measured
+        cw = cpu_work if cpu_work is not None else CpuWorkload(pb, args)
+        cw.set_state(V.ravel().copy(), np.zeros(3 * nV))
+        cw.x[:] = 0.0
+        cw.g0 = -1.0
+        t1 = time.perf_counter()
+        st = cw.newton_step()
+        t_one = time.perf_counter() - t1
+        cpu = {"value": 1.0 / t_one, "unit": UNIT, "cores": cw.cb.threads, "kind": "port", "estimated": False,
+               "sample": f"one whole Newton iteration of this workload (the first from rest), measured: FP64 OpenMP "
+                         f"CPU restatement, gradient, simple_psd_fix Hessian over all {nT} tets, block-Jacobi PCG to "
+                         f"1e-8 ({int(st['pcg_iterations'])} iterations), the reference's line search",
+               "components": {k: st[k] for k in ("t_gradient", "t_hessian", "t_pcg", "t_linesearch")},
+               "pcg_iterations": int(st["pcg_iterations"])}
         if not args.no_faithful_baseline:
-            f_est, f_parts = cpu_faithful_sample(pb, args, counts)
-            cpu["reference_faithful_1thread"] = {"value": 1.0 / f_est, "unit": UNIT, "cores": 1,
-                                                 "sample": cpu_faithful_text(counts, args.n), "components": f_parts}
+            f_est, f_parts, f_scale = cpu_faithful_sample(pb, args, st["pcg_iterations"])
+            cpu["reference_faithful_1thread"] = {
+                "value": 1.0 / f_est, "unit": UNIT, "cores": 1, "estimated": True, "scales": f_scale,
+                "sample": "ESTIMATE of one Newton iteration in the reference's structure on 1 thread (dense per-tet "
+                          "B^T d2psi B + simple_psd_fix, triplets + sort/compress, serial sums) from 1/64 of the "
+                          "tets x64 and 3 one-thread PCG iterations scaled to the measured CPU PCG count",
+                "components": f_parts}
+    if cpu_work is not None:
+        cpu_work.close()
 
-    precond_name = "learned factor G^T G" if net is not None else "block-Jacobi"
+    precond_name = {"learned": "learned factor G^T G", "jacobi": "block-Jacobi", "multigrid": "aggregation multigrid",
+                    "learned_multigrid": "aggregation multigrid with the learned smoother"}[args.precond]
     value = replica_value(newton_its, world, ms)
     jacobi_pcg = None
-    if jac is not None and net is not None:
+    if jac is not None and args.precond != "jacobi":
         jv = replica_value(jac["newton_its"], world, jac["ms"])
         jacobi_pcg = {"value": jv, "unit": UNIT, "ms_per_step": jac["ms"] / max(jac["newton_its"], 1),
                       "pcg_iters_per_newton": jac["pcg_its"] / max(jac["newton_its"], 1),
@@ -393,11 +456,12 @@ def run_gpu(args, rank, world):
                                    "compulsory_bytes": hess_bytes, "achieved_gbs": hess_bytes / hess_on_s / 1e9,
                                    "frac": hess_bytes / hess_on_s / 1e9 / peak}},
         "jacobi_pcg": jacobi_pcg,
-        "learned_precond": None if net is None else {
+        "learned_precond": None if args.precond == "jacobi" else {
             "factor_build_ms_per_newton": 1e3 * main_arm["t_precond"] / max(newton_its, 1),
             "fallbacks_to_block_jacobi": main_arm["fallbacks"],
             "pcg_us_per_iteration": 1e6 * rep.t_pcg / max(rep.pcg_iterations, 1)},
         "clocks": main_arm["clocks"], "gpu_launches": int(launches), "e2e": e2e, "cpu_baseline": cpu,
+        "oracle_error": oracle_err, "multigrid_hierarchy": mg_levels,
         "setup_s": {"plan": t_plan}, "time_steps_completed": state["steps"],
         "stage_seconds": {"gradient": rep.t_gradient, "hessian": rep.t_hessian, "pcg": rep.t_pcg,
                           "linesearch": rep.t_linesearch},
@@ -406,52 +470,61 @@ def run_gpu(args, rank, world):
 
 
 # --------------------------------------------------------- CPU baseline ----
-def cpu_newton_sample(pb, args, counts, reps=1):
-    """Time the FP64 OpenMP CPU restatement (oracle/oracle_baseline.cpp) of one
-    Newton iteration of this workload on the host cores, by components:
-    gradient and energy over all tets, the PSD-projected Hessian assembly over a
-    1/16 slice of the tets (scaled x16), and 20 block-Jacobi PCG iterations on
-    the full 3nV system (scaled to the PCG iteration count per Newton
-    iteration). Returns the estimated seconds per Newton iteration."""
-    from oracle import oracle as o
-    from oracle.baseline import CpuNewton
-    V, E = pb["V"], pb["E"]
-    nV, nT = len(V), len(E)
-    t0 = time.perf_counter()
-    cb = CpuNewton(V, E)
-    t_setup = time.perf_counter() - t0
-    vol = o.volume(V, E)
-    f_g = o.const_ext_force(nV, E, vol, pb["rho"] * pb["gravity"])
-    cb.set(args.model, pb["params"], np.full(nT, pb["rho"]), V.ravel(), np.zeros(3 * nV), f_g, pb["pinned"], 1.0,
-           pb["dt"], pb["dt"], None if args.no_psd else 1e-6)
-    x = np.zeros(3 * nV)
-    slice_t = max(1, nT // 16)
-    est = []
-    parts = {}
-    for _ in range(reps):
-        t = time.perf_counter(); g = cb.gradient(x); t_g = time.perf_counter() - t
-        t = time.perf_counter(); cb.energy(x); t_e = time.perf_counter() - t
-        t = time.perf_counter(); cb.hessian_range(x, 0, slice_t, True); t_h = (time.perf_counter() - t) * nT / slice_t
-        d = np.zeros(3 * nV)
-        t = time.perf_counter(); it, _ = cb.pcg(-g, d, 1e-30, 20); t_p = (time.perf_counter() - t) / max(it, 1)
-        n_pcg, n_ls = counts["pcg_per_newton"], counts["ls_per_newton"]
-        est.append(t_g + t_h + n_pcg * t_p + (1.0 + n_ls) * t_e)
-        parts = {"gradient_s": t_g, "hessian_s": t_h, "pcg_iter_s": t_p, "energy_s": t_e}
-    cb.close()
-    return est, parts, cb.threads, t_setup
+class CpuWorkload:
+    """The bench workload on the FP64 OpenMP CPU restatement of the path
+    (oracle/oracle_baseline.cpp): implicit-Euler Newton from rest with the same
+    state machine as the GPU arm (a converged time step advances q_base += dt v,
+    x_hat = v, and the next step starts from v). Each Newton iteration is the
+    reference's (include/optimization_gradient_based.h:77-106): gradient, the
+    simple_psd_fix-projected Hessian over all tets, the search direction (block-
+    Jacobi PCG to 1e-8 relative residual in place of Eigen::SparseLU, which
+    cannot factor 2.7M DOF here) and the backtracking line search
+    (src/linesearch_backtracking_bisection.cpp:17-30)."""
+
+    def __init__(self, pb, args):
+        from oracle import oracle as o
+        from oracle.baseline import CpuNewton
+        V, E = pb["V"], pb["E"]
+        self.pb, self.args = pb, args
+        self.cb = CpuNewton(V, E)
+        self.f_g = o.const_ext_force(len(V), E, o.volume(V, E), pb["rho"] * pb["gravity"])
+        self.q_base, self.x_hat = V.ravel().copy(), np.zeros(3 * len(V))
+        self.x = np.zeros(3 * len(V))
+        self.g0, self.steps = -1.0, 0
+        self.set_state(self.q_base, self.x_hat)
+
+    def set_state(self, q_base, x_hat):
+        pb, a = self.pb, self.args
+        self.q_base, self.x_hat = q_base, x_hat
+        self.cb.set(a.model, pb["params"], np.full(len(pb["E"]), pb["rho"]), q_base, x_hat, self.f_g, pb["pinned"],
+                    1.0, pb["dt"], pb["dt"], None if a.no_psd else 1e-6)
+
+    def newton_step(self):
+        """One whole Newton iteration (converged time steps are advanced first)."""
+        while True:
+            gn = float(np.linalg.norm(self.cb.gradient(self.x)))
+            if self.g0 < 0:
+                self.g0 = gn
+            if gn > 1e-8 * self.g0:
+                break
+            self.set_state(self.q_base + self.pb["dt"] * self.x, self.x.copy())
+            self.g0, self.steps = -1.0, self.steps + 1
+        return self.cb.newton_iteration(self.x, 1e-8, 60000, 100)
+
+    def close(self):
+        self.cb.close()
 
 
-def cpu_faithful_sample(pb, args, counts):
-    """The reference's own structure on one host thread, timed on bounded
-    samples of this workload: per-tet dense B^T d2psi B with simple_psd_fix, a
-    triplet list and a sort / compress into CSR (src/assemble.cpp:57-94), serial
-    gradient and energy sums (oracle/oracle_baseline.cpp, oracle/oracle_capi.cpp),
-    simple_psd_fix by tridiagonal QL as Eigen's solver does, over 1/64 of the tets
-    (scaled x64); the line search's two energy evaluations per trial
-    (src/linesearch_backtracking_bisection.cpp:21); block-Jacobi PCG
-    iterations on the full system with one OpenMP thread (scaled to the PCG
-    iteration count per Newton iteration; the reference's SparseLU cannot
-    factor 2.7M DOF here). Returns (seconds per Newton iteration, components)."""
+def cpu_faithful_sample(pb, args, pcg_per_newton):
+    """An ESTIMATE of one Newton iteration in the reference's own structure on one
+    host thread, from bounded samples: per-tet dense B^T d2psi B with
+    simple_psd_fix (tridiagonal QL, as Eigen's solver), a triplet list and a
+    sort / compress into CSR (src/assemble.cpp:57-94), over 1/64 of the tets
+    (x64); serial gradient and energy over the same slice (x64); the line
+    search's two energy evaluations per trial
+    (src/linesearch_backtracking_bisection.cpp:21); 3 block-Jacobi PCG
+    iterations on the full system with one thread, scaled to the measured CPU
+    PCG count per Newton iteration. Returns (seconds, components, scales)."""
     from oracle import oracle as o
     from oracle.baseline import CpuNewton, faithful_dq2
     V, E = pb["V"], pb["E"]
@@ -469,9 +542,9 @@ def cpu_faithful_sample(pb, args, counts):
     t = time.perf_counter(); o.tetmesh_q(args.model, sub, q, dphi, vol, params)
     t_e = (time.perf_counter() - t) * scale
     cb = CpuNewton(V, E)
-    full_vol = o.volume(V, E)
     cb.set(args.model, pb["params"], np.full(nT, pb["rho"]), q, np.zeros(3 * nV),
-           o.const_ext_force(nV, E, full_vol, pb["rho"] * pb["gravity"]), pb["pinned"], 1.0, pb["dt"], pb["dt"], psd)
+           o.const_ext_force(nV, E, o.volume(V, E), pb["rho"] * pb["gravity"]), pb["pinned"], 1.0, pb["dt"],
+           pb["dt"], psd)
     threads = cb.threads
     x = np.zeros(3 * nV)
     g = cb.gradient(x)
@@ -483,54 +556,57 @@ def cpu_faithful_sample(pb, args, counts):
     finally:
         cb.set_threads(threads)
         cb.close()
-    n_pcg, n_ls = counts["pcg_per_newton"], counts["ls_per_newton"]
-    est = t_g + t_h + n_pcg * t_p + 2.0 * (1.0 + n_ls) * t_e
-    return est, {"gradient_s": t_g, "hessian_s": t_h, "pcg_iter_s": t_p, "energy_s": t_e}
-
-
-def cpu_faithful_text(counts, n=96):
-    return (f"one Newton iteration of the n={n} workload in the reference's structure on 1 thread: dense per-tet "
-            "B^T d2psi B + simple_psd_fix, triplets + sort/compress, serial gradient and energy, over 1/64 of the "
-            f"tets x64; 3 block-Jacobi PCG iterations on the full system (1 thread) x {counts['pcg_per_newton']:.0f} "
-            "per Newton; 2 energy evaluations per line-search trial")
-
-
-def cpu_sample_text(counts, n=96):
-    return (f"one Newton iteration of the n={n} workload, FP64 OpenMP restatement: gradient + energy over all "
-            "tets, PSD Hessian assembly over 1/16 of the tets x16, 20 block-Jacobi PCG iterations on the full "
-            f"system x {counts['pcg_per_newton']:.0f} PCG iterations per Newton (count from the GPU run of the "
-            "same workload)")
-
-
-def load_counts(args):
-    try:
-        with open(os.path.join(ROOT, "profiles", "newton_counts.json")) as f:
-            c = json.load(f)
-        if c.get("n") == args.n and c.get("model") == args.model:
-            return c
-    except Exception:
-        pass
-    return {"pcg_per_newton": 1000.0, "ls_per_newton": 0.0, "source": "default"}
+    est = t_g + t_h + pcg_per_newton * t_p + 2.0 * t_e
+    return est, {"gradient_s": t_g, "hessian_s": t_h, "pcg_iter_s": t_p, "energy_s": t_e}, \
+        {"tets_sampled": len(sub), "tet_scale": scale, "pcg_iterations_sampled": 3,
+         "pcg_scale_to": pcg_per_newton}
 
 
 def run_reference(args):
-    """--impl reference: the reference's CPU path (its FP64 restatement; the
-    reference itself needs Eigen/libigl, absent here) on the host cores."""
+    """--impl reference: the reference's CPU path of this workload on the host
+    cores (its FP64 restatement: the reference itself needs Eigen and libigl,
+    absent here). Every timed step is one whole Newton iteration, measured:
+    nothing is sampled or scaled. The W warm-up steps are gradient and energy
+    evaluations (the first also assembles the Hessian), which touch every
+    array a Newton iteration uses."""
     pb = build_problem(args.n, args.model)
-    counts = load_counts(args)
-    cpu_newton_sample(pb, args, counts, reps=max(args.warmup, 0) and 1)
-    est, parts, threads, t_setup = cpu_newton_sample(pb, args, counts, reps=max(args.steps, 1))
-    total = sum(est)
-    value = len(est) / total
+    t0 = time.perf_counter()
+    cw = CpuWorkload(pb, args)
+    t_setup = time.perf_counter() - t0
+    for w in range(args.warmup):
+        cw.cb.gradient(cw.x)
+        cw.cb.energy(cw.x)
+        if w == 0:
+            cw.cb.hessian_range(cw.x, 0, len(pb["E"]), True)
+    secs, pcg, ls = [], [], []
+    comp = {"t_gradient": 0.0, "t_hessian": 0.0, "t_pcg": 0.0, "t_linesearch": 0.0}
+    for _ in range(max(args.steps, 1)):
+        t = time.perf_counter()
+        st = cw.newton_step()
+        secs.append(time.perf_counter() - t)
+        pcg.append(st["pcg_iterations"])
+        ls.append(st["ls_iterations"])
+        for k in comp:
+            comp[k] += st[k]
+    total = sum(secs)
+    value = len(secs) / total
+    threads = cw.cb.threads
+    steps_done = cw.steps
+    cw.close()
     return {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * total / len(est), "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": 1e3 * total / len(secs), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Kuhn cube, gravity)",
             "config": {"workload": f"implicit-Euler Newton, Neo-Hookean Kuhn cube n={args.n}, dt=0.01, z=0 pinned, "
-                                   "PSD simple_psd_fix 1e-6, block-Jacobi PCG 1e-8", "parallelism": "OpenMP host"},
+                                   f"PSD {'off' if args.no_psd else 'simple_psd_fix 1e-6'}, block-Jacobi PCG 1e-8, "
+                                   "Newton 1e-8 relative", "parallelism": f"OpenMP host, {threads} threads"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": cpu_sample_text(counts, args.n), "components": parts,
-                             "counts_source": counts.get("source", "profiles/newton_counts.json")},
+                             "sample": f"{len(secs)} whole Newton iterations of the workload from rest, each measured "
+                                       "(gradient, simple_psd_fix Hessian over all tets, block-Jacobi PCG to 1e-8, "
+                                       "line search), FP64 OpenMP CPU restatement",
+                             "estimated": False},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "pcg_iters_per_newton": float(np.mean(pcg)), "ls_backtracks_per_newton": float(np.mean(ls)),
+            "seconds_per_step": secs, "stage_seconds": comp, "time_steps_completed": steps_done,
             "setup_s": t_setup}
 
 

@@ -361,6 +361,20 @@ int bartels_newton_iterate_d(bartels_ctx ctx, bartels_mesh_plan plan, const bart
 int bartels_newton_gradient_d(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params *params,
                               const double *x_d, double *g_d);
 
+/* Copy the plan's current q_base and x_hat (host, 3nV doubles each; either may
+ * be NULL) back, e.g. after bartels_newton_advance_implicit_euler_d moved them
+ * on the device. A state accessor with no counterpart in the reference. */
+int bartels_newton_get_problem(bartels_mesh_plan plan, double *q_base, double *x_hat);
+
+/* Value of the Newton objective at device x_d (FP64, host *energy): the
+ * function f that newtons_method_bisection minimises and its line search
+ * evaluates (include/optimization_gradient_based.h:77-106; here the
+ * implicit-Euler objective of matlab/examples/implicit_integration.m:69-83,
+ * f = mass_coeff (x^T M x / 2 - x^T M x_hat) + Psi(q_base + scale x)
+ * - force_scale x^T f_ext over the free vertices). */
+int bartels_newton_energy_d(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params *params,
+                            const double *x_d, double *energy);
+
 /* --------------------------------------------------- learned preconditioner -- */
 /* No counterpart in the reference, whose linear solver is Eigen::SparseLU
  * (include/search_direction_newton_sparse.h:8). A message-passing network over
@@ -413,6 +427,15 @@ int bartels_plan_factor_size(bartels_mesh_plan plan, int64_t *nnzl_blocks, int64
  * preconditioner of systems too small for a coarse level. No counterpart in
  * the reference (its solver is Eigen::SparseLU). */
 int bartels_plan_set_preconditioner(bartels_mesh_plan plan, int kind, bartels_lpcg net);
+/* Shape of the plan's multigrid hierarchy (built by the last multigrid solve
+ * or bartels_plan_precond_apply_d): *levels, and for each of the first
+ * max_levels levels its nodes (vertices on level 0, aggregates below) and
+ * stored blocks (3x3 on level 0, 6x6 below); *coarsest is 0 for a dense
+ * coarsest solve, 1 for an exact block-diagonal one, 2 for Chebyshev
+ * smoothing. Arrays may be NULL. BARTELS_E_INVALID_ARG without a hierarchy.
+ * No counterpart in the reference. */
+int bartels_plan_mg_info(bartels_mesh_plan plan, int max_levels, int *levels, int *nodes, int64_t *blocks,
+                         int *coarsest);
 /* z_d = B r_d: one application of the plan's multigrid preconditioner
  * (BARTELS_PRECOND_MULTIGRID or _LEARNED_MULTIGRID) built for the Hessian
  * values_d (FP32, the plan's CSR order, device); FP32 device vectors of 3nV,
@@ -471,6 +494,12 @@ int bartels_newton_advance_implicit_euler_d(bartels_ctx ctx, bartels_mesh_plan p
  * order as the host forms: identical results. */
 int bartels_tetmesh_q_d(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q_d, double *energy_d);
 int bartels_tetmesh_dq_d(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q_d, double *g_d);
+/* Energy of every tet, psi(F) vol (linear_tet_{neohookean,stvk,corotational}_q
+ * per element, src/linear_tet_neohookean_q.cpp:5-18, with the plan's element
+ * data) at device positions q_d into device e_d (nT doubles): the terms
+ * bartels_tetmesh_q_d sums. FP64. */
+int bartels_tetmesh_q_elements_d(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q_d,
+                                 double *e_d);
 
 /* ------------------------------------------------- allocation-free variant -- */
 /* Gradient of the elastic energy (as bartels_tetmesh_dq, with the plan's

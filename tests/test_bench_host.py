@@ -6,6 +6,7 @@ by."""
 import argparse
 import json
 import os
+import time
 
 import bench
 
@@ -36,11 +37,19 @@ def test_clocks_without_nvidia_smi_record_nothing(monkeypatch):
     assert c.summary() == {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
 
 
-def test_newton_counts_file_matches_the_default_workload():
-    with open(os.path.join(bench.ROOT, "profiles", "newton_counts.json")) as f:
-        c = json.load(f)
-    args = argparse.Namespace(n=96, model="neohookean")
-    counts = bench.load_counts(args)
-    assert counts["pcg_per_newton"] == c["pcg_per_newton"] > 0
-    other = bench.load_counts(argparse.Namespace(n=12, model="stvk"))
-    assert other["source"] == "default"
+def test_reference_arm_times_whole_newton_iterations():
+    """--impl reference on a small cube: every timed step is a whole measured
+    Newton iteration (no sampled or scaled piece), time steps advance when
+    they converge, and the record's time per step adds up to the steps timed."""
+    args = argparse.Namespace(n=3, model="neohookean", no_psd=False, steps=12, warmup=2)
+    t0 = time.perf_counter()
+    out = bench.run_reference(args)
+    wall = time.perf_counter() - t0
+    assert out["impl"] == "reference" and out["unit"] == bench.UNIT
+    assert len(out["seconds_per_step"]) == 12
+    assert abs(out["ms_per_step"] * 12 - 1e3 * sum(out["seconds_per_step"])) < 1e-6
+    assert out["ms_per_step"] * 12 <= 1e3 * wall
+    assert out["cpu_baseline"]["estimated"] is False
+    assert out["pcg_iters_per_newton"] > 0
+    assert out["time_steps_completed"] >= 1  # 12 Newton iterations finish at least one time step
+    assert out["e2e"]["h2d_bytes_per_step"] == 0
