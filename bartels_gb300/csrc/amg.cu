@@ -651,6 +651,8 @@ k_mg_restrict(int nc, const int *__restrict__ mptr, const int *__restrict__ midx
               const float *__restrict__ r, float *__restrict__ bc, const float *__restrict__ cdinv,
               float *__restrict__ cx, float *__restrict__ cr, float *__restrict__ cd, const float *__restrict__ ccoef,
               const PcgState *__restrict__ st) {
+  pdl_wait();
+  pdl_trigger();
   if (st && st->done) return;
   const int lane = threadIdx.x & 31, sl = lane & 7, g = lane >> 3;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -699,6 +701,8 @@ template <int BSF>
 __global__ void __launch_bounds__(256)
 k_mg_prolong(int n, const int *__restrict__ agg, const float *__restrict__ Q, const float *__restrict__ xc,
              float *__restrict__ x, const PcgState *__restrict__ st) {
+  pdl_wait();
+  pdl_trigger();
   if (st && st->done) return;
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
     const int I = __ldg(agg + v);
@@ -722,6 +726,8 @@ k_mg_prolong(int n, const int *__restrict__ agg, const float *__restrict__ Q, co
 __global__ void __launch_bounds__(256)
 k_mg0_bj(int nV, const float *__restrict__ minv, const float *__restrict__ r, float *__restrict__ x,
          const float *__restrict__ coef, const PcgState *__restrict__ st) {
+  pdl_wait();
+  pdl_trigger();
   if (st && st->done) return;
   const float c = coef ? coef[0] : 1.f;
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nV; v += gridDim.x * blockDim.x) {
@@ -742,6 +748,8 @@ __global__ void __launch_bounds__(256)
 k_mg0_update(int nV, const float *__restrict__ pa, const float *__restrict__ pb, const float *__restrict__ ap,
              float *__restrict__ x, float *__restrict__ r, const float *__restrict__ minv, float *__restrict__ x0,
              const float *__restrict__ coef, double *__restrict__ part, PcgState *__restrict__ st) {
+  pdl_wait();
+  pdl_trigger();
   if (st->done) return;
   const int it = st->it;
   const float *p = (it & 1) ? pb : pa;
@@ -780,6 +788,8 @@ __global__ void __launch_bounds__(256)
 k_mg0_resid(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, const float *__restrict__ val,
             const float *__restrict__ b, const float *__restrict__ x, float *__restrict__ out,
             const unsigned char *__restrict__ pinned, const PcgState *__restrict__ st) {
+  pdl_wait();
+  pdl_trigger();
   if (st && st->done) return;
   BT_ROW_LOOP_BEGIN(G)
   float s0 = 0.f, s1 = 0.f, s2 = 0.f;
@@ -808,6 +818,8 @@ k_mg0_post_bj(int nV, const int *__restrict__ brp, const int *__restrict__ bcol,
               const float *__restrict__ minv, const float *__restrict__ b, const float *__restrict__ x,
               float *__restrict__ z, const unsigned char *__restrict__ pinned, const float *__restrict__ coef,
               double *__restrict__ part, PcgState *__restrict__ st) {
+  pdl_wait();
+  pdl_trigger();
   if (st->done) return;
   const float c = coef[0];
   float acc = 0.f;
@@ -850,6 +862,8 @@ __global__ void __launch_bounds__(256)
 k_mg0_fac_lower(int nV, const int4 *__restrict__ meta, const int *__restrict__ bcol,
                 const __nv_bfloat16 *__restrict__ gl, const float *__restrict__ r, float *__restrict__ y,
                 const unsigned char *__restrict__ pinned, const PcgState *__restrict__ st) {
+  pdl_wait();
+  pdl_trigger();
   if (st && st->done) return;
   BT_ROW_LOOP_BEGIN(G)
   float s0 = 0.f, s1 = 0.f, s2 = 0.f;
@@ -877,6 +891,8 @@ k_mg0_fac_upper(int nV, const int4 *__restrict__ meta, const int *__restrict__ b
                 const __nv_bfloat16 *__restrict__ gu, const float *__restrict__ y, const float *__restrict__ xin,
                 float *__restrict__ out, const unsigned char *__restrict__ pinned, const float *__restrict__ coef,
                 const float *__restrict__ b, double *__restrict__ part, PcgState *__restrict__ st) {
+  pdl_wait();
+  pdl_trigger();
   if (st && st->done) return;
   const float c = coef ? coef[0] : 1.f;
   float acc = 0.f;
@@ -962,6 +978,8 @@ __global__ void __launch_bounds__(256)
 k_mgc_first(int n, const float *__restrict__ dinv, const float *__restrict__ b, float *__restrict__ x,
             float *__restrict__ r, float *__restrict__ d, const float *__restrict__ coef,
             const PcgState *__restrict__ st) {
+  pdl_wait();
+  pdl_trigger();
   if (st && st->done) return;
   const float c = coef ? coef[0] : 1.f;
   for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < n; I += gridDim.x * blockDim.x) {
@@ -986,6 +1004,8 @@ k_mgc_cheb(int n, const int *__restrict__ rp, const int *__restrict__ ci, const 
            const float *__restrict__ dinv, const float *__restrict__ d_in, float *__restrict__ d_out,
            float *__restrict__ r, float *__restrict__ x, const float *__restrict__ coef, int j,
            const PcgState *__restrict__ st) {
+  pdl_wait();
+  pdl_trigger();
   if (st && st->done) return;
   const float c1 = coef[2 * j - 1], c2 = coef[2 * j];
   BT_CROW_LOOP_BEGIN(G)
@@ -1016,6 +1036,8 @@ __global__ void __launch_bounds__(256)
 k_mgc_resid(int n, const int *__restrict__ rp, const int *__restrict__ ci, const float *__restrict__ val,
             const float *__restrict__ b, const float *__restrict__ x, float *__restrict__ r,
             const PcgState *__restrict__ st) {
+  pdl_wait();
+  pdl_trigger();
   if (st && st->done) return;
   BT_CROW_LOOP_BEGIN(G)
   float s[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -1034,6 +1056,8 @@ k_mgc_post_first(int n, const int *__restrict__ rp, const int *__restrict__ ci, 
                  const float *__restrict__ dinv, const float *__restrict__ b, const float *__restrict__ x,
                  float *__restrict__ x_out, float *__restrict__ r, float *__restrict__ d,
                  const float *__restrict__ coef, const PcgState *__restrict__ st) {
+  pdl_wait();
+  pdl_trigger();
   if (st && st->done) return;
   const float c0 = coef[0];
   BT_CROW_LOOP_BEGIN(G)
@@ -1080,6 +1104,8 @@ k_mgc_MA(int n, const int *__restrict__ rp, const int *__restrict__ ci, const fl
 __global__ void __launch_bounds__(256)
 k_mg_dense_apply(int nd, const float *__restrict__ ainv, const float *__restrict__ b, float *__restrict__ x,
                  const PcgState *__restrict__ st) {
+  pdl_wait();
+  pdl_trigger();
   if (st && st->done) return;
   __shared__ float sb[6 * kDenseNodes];
   for (int i = threadIdx.x; i < nd; i += blockDim.x) sb[i] = __ldcg(b + i);
@@ -1170,10 +1196,10 @@ float *level_result(const MgHierarchy *mg, int l) {
 int cheb_from_zero(bartels_ctx ctx, const MgLevel &c, const float *coef, bool first_done, const PcgState *st) {
   const int gr = grid_rows(ctx, c.n, kGc);
   if (!first_done)
-    BT_LAUNCH(ctx, k_mgc_first, grid_n(ctx, c.n), 256, 0, c.n, c.dinv, c.b, c.x, c.r, c.d, coef, st);
+    BT_LAUNCH_PDL(ctx, k_mgc_first, grid_n(ctx, c.n), 256, 0, c.n, c.dinv, c.b, c.x, c.r, c.d, coef, st);
   float *dc = c.d, *dn = c.d2;
   for (int j = 1; j < c.deg; ++j) {
-    BT_LAUNCH(ctx, k_mgc_cheb<kGc>, gr, 256, 0, c.n, c.rp, c.ci, c.val, c.dinv, dc, dn, c.r, c.x, coef, j, st);
+    BT_LAUNCH_PDL(ctx, k_mgc_cheb<kGc>, gr, 256, 0, c.n, c.rp, c.ci, c.val, c.dinv, dc, dn, c.r, c.x, coef, j, st);
     std::swap(dc, dn);
   }
   return BARTELS_OK;
@@ -1192,10 +1218,10 @@ int restrict_into(bartels_ctx ctx, MgHierarchy *mg, const MgLevel &f, const floa
   const float *coef = exact ? nullptr : mg->coef + kMgCoef * l;
   const int g = grid_rows(ctx, (c.n + 3) / 4, 32);
   if (fuse)
-    BT_LAUNCH(ctx, k_mg_restrict<BSF>, g, 256, 0, c.n, f.mptr, f.midx, f.Q, r, c.b, (const float *)c.dinv, c.x,
+    BT_LAUNCH_PDL(ctx, k_mg_restrict<BSF>, g, 256, 0, c.n, f.mptr, f.midx, f.Q, r, c.b, (const float *)c.dinv, c.x,
               exact ? (float *)nullptr : c.r, exact ? (float *)nullptr : c.d, coef, st);
   else
-    BT_LAUNCH(ctx, k_mg_restrict<BSF>, g, 256, 0, c.n, f.mptr, f.midx, f.Q, r, c.b, (const float *)nullptr,
+    BT_LAUNCH_PDL(ctx, k_mg_restrict<BSF>, g, 256, 0, c.n, f.mptr, f.midx, f.Q, r, c.b, (const float *)nullptr,
               (float *)nullptr, (float *)nullptr, (float *)nullptr, (const float *)nullptr, st);
   *first_done = fuse;
   return BARTELS_OK;
@@ -1207,10 +1233,10 @@ int enqueue_coarse(bartels_ctx ctx, MgHierarchy *mg, int l, bool first_done, con
   const int last = (int)mg->lv.size() - 1;
   if (l == last) {
     if (mg->dense) {
-      BT_LAUNCH(ctx, k_mg_dense_apply, 1, 256, 0, mg->nd, mg->ainv, c.b, c.x, st);
+      BT_LAUNCH_PDL(ctx, k_mg_dense_apply, 1, 256, 0, mg->nd, mg->ainv, c.b, c.x, st);
     } else if (mg->coarse_blockdiag) {
       if (!first_done)
-        BT_LAUNCH(ctx, k_mgc_first, grid_n(ctx, c.n), 256, 0, c.n, c.dinv, c.b, c.x, (float *)nullptr,
+        BT_LAUNCH_PDL(ctx, k_mgc_first, grid_n(ctx, c.n), 256, 0, c.n, c.dinv, c.b, c.x, (float *)nullptr,
                   (float *)nullptr, (const float *)nullptr, st);
     } else {
       BT_CHECK(cheb_from_zero(ctx, c, coef, first_done, st));
@@ -1219,16 +1245,16 @@ int enqueue_coarse(bartels_ctx ctx, MgHierarchy *mg, int l, bool first_done, con
   }
   const int gr = grid_rows(ctx, c.n, kGc);
   BT_CHECK(cheb_from_zero(ctx, c, coef, first_done, st));
-  BT_LAUNCH(ctx, k_mgc_resid<kGc>, gr, 256, 0, c.n, c.rp, c.ci, c.val, c.b, c.x, c.r, st);
+  BT_LAUNCH_PDL(ctx, k_mgc_resid<kGc>, gr, 256, 0, c.n, c.rp, c.ci, c.val, c.b, c.x, c.r, st);
   bool next_first = false;
   BT_CHECK(restrict_into<6>(ctx, mg, c, c.r, l + 1, st, &next_first));
   BT_CHECK(enqueue_coarse(ctx, mg, l + 1, next_first, st));
-  BT_LAUNCH(ctx, k_mg_prolong<6>, grid_n(ctx, c.n), 256, 0, c.n, c.agg, c.Q, level_result(mg, l + 1), c.x, st);
-  BT_LAUNCH(ctx, k_mgc_post_first<kGc>, gr, 256, 0, c.n, c.rp, c.ci, c.val, c.dinv, c.b, c.x, c.x2, c.r, c.d, coef,
+  BT_LAUNCH_PDL(ctx, k_mg_prolong<6>, grid_n(ctx, c.n), 256, 0, c.n, c.agg, c.Q, level_result(mg, l + 1), c.x, st);
+  BT_LAUNCH_PDL(ctx, k_mgc_post_first<kGc>, gr, 256, 0, c.n, c.rp, c.ci, c.val, c.dinv, c.b, c.x, c.x2, c.r, c.d, coef,
             st);
   float *dc = c.d, *dn = c.d2;
   for (int j = 1; j < c.deg; ++j) {
-    BT_LAUNCH(ctx, k_mgc_cheb<kGc>, gr, 256, 0, c.n, c.rp, c.ci, c.val, c.dinv, dc, dn, c.r, c.x2, coef, j, st);
+    BT_LAUNCH_PDL(ctx, k_mgc_cheb<kGc>, gr, 256, 0, c.n, c.rp, c.ci, c.val, c.dinv, dc, dn, c.r, c.x2, coef, j, st);
     std::swap(dc, dn);
   }
   return BARTELS_OK;
@@ -1253,7 +1279,7 @@ int fac_lower(bartels_ctx ctx, bartels_mesh_plan plan, const MgSmoother &sm, con
               const PcgState *st) {
   const int GT = plan_lanes_tri(ctx, plan) == 8 ? 8 : 4;
   const int g = grid_rows(ctx, plan->nV, GT);
-  BT_MG_G(GT, BT_LAUNCH(ctx, k_mg0_fac_lower<GL>, g, 256, 0, plan->nV, sm.fp->meta, plan->bcol, sm.gl, in, out,
+  BT_MG_G(GT, BT_LAUNCH_PDL(ctx, k_mg0_fac_lower<GL>, g, 256, 0, plan->nV, sm.fp->meta, plan->bcol, sm.gl, in, out,
                         plan->pinned, st));
   return BARTELS_OK;
 }
@@ -1262,7 +1288,7 @@ int fac_upper(bartels_ctx ctx, bartels_mesh_plan plan, const MgSmoother &sm, con
               float *out, const float *coef, const float *b, double *part, PcgState *st) {
   const int GT = plan_lanes_tri(ctx, plan) == 8 ? 8 : 4;
   const int g = grid_rows(ctx, plan->nV, GT);
-  BT_MG_G(GT, BT_LAUNCH(ctx, k_mg0_fac_upper<GL>, g, 256, 0, plan->nV, sm.fp->meta, plan->bcol, sm.gu, y, xin, out,
+  BT_MG_G(GT, BT_LAUNCH_PDL(ctx, k_mg0_fac_upper<GL>, g, 256, 0, plan->nV, sm.fp->meta, plan->bcol, sm.gu, y, xin, out,
                         plan->pinned, coef, b, part, st));
   return BARTELS_OK;
 }
@@ -1271,7 +1297,7 @@ int resid0(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const f
            const PcgState *st) {
   const int G = plan_lanes_spmv(ctx, plan);
   const int g = grid_rows(ctx, plan->nV, G);
-  BT_MG_G(G, BT_LAUNCH(ctx, k_mg0_resid<GL>, g, 256, 0, plan->nV, plan->brp, plan->bcol, values, b, x, out,
+  BT_MG_G(G, BT_LAUNCH_PDL(ctx, k_mg0_resid<GL>, g, 256, 0, plan->nV, plan->brp, plan->bcol, values, b, x, out,
                        plan->pinned, st));
   return BARTELS_OK;
 }
@@ -1323,7 +1349,7 @@ int mg_setup_numeric(bartels_ctx ctx, bartels_mesh_plan plan, const float *value
           BT_CHECK(fac_lower(ctx, plan, sm, c.r, c.d, nullptr));
           BT_CHECK(fac_upper(ctx, plan, sm, c.d, nullptr, y, nullptr, nullptr, nullptr, nullptr));
         } else {
-          BT_LAUNCH(ctx, k_mg0_bj, grid_n(ctx, plan->nV), 256, 0, plan->nV, sm.minv, c.r, y, (const float *)nullptr,
+          BT_LAUNCH_PDL(ctx, k_mg0_bj, grid_n(ctx, plan->nV), 256, 0, plan->nV, sm.minv, c.r, y, (const float *)nullptr,
                     (const PcgState *)nullptr);
         }
       } else {
@@ -1341,7 +1367,7 @@ int mg_setup_numeric(bartels_ctx ctx, bartels_mesh_plan plan, const float *value
 int mg_enqueue_update(bartels_ctx ctx, bartels_mesh_plan plan, const MgSmoother &sm, const float *pa,
                       const float *pb, const float *ap, float *x, float *r, double *part, PcgState *st) {
   MgHierarchy *mg = plan->mg;
-  BT_LAUNCH(ctx, k_mg0_update, grid_n(ctx, plan->nV), 256, 0, plan->nV, pa, pb, ap, x, r, sm.minv, mg->lv[0].x,
+  BT_LAUNCH_PDL(ctx, k_mg0_update, grid_n(ctx, plan->nV), 256, 0, plan->nV, pa, pb, ap, x, r, sm.minv, mg->lv[0].x,
             (const float *)mg->coef, part, st);
   return BARTELS_OK;
 }
@@ -1356,13 +1382,13 @@ int mg_enqueue_apply(bartels_ctx ctx, bartels_mesh_plan plan, const float *value
     BT_CHECK(fac_lower(ctx, plan, sm, r, y, st));
     BT_CHECK(fac_upper(ctx, plan, sm, y, nullptr, l0.x, c0, nullptr, nullptr, st));
   } else if (!pre_done) {
-    BT_LAUNCH(ctx, k_mg0_bj, grid_n(ctx, nV), 256, 0, nV, sm.minv, r, l0.x, c0, st);
+    BT_LAUNCH_PDL(ctx, k_mg0_bj, grid_n(ctx, nV), 256, 0, nV, sm.minv, r, l0.x, c0, st);
   }
   BT_CHECK(resid0(ctx, plan, values, r, l0.x, l0.r, st));
   bool first_done = false;
   BT_CHECK(restrict_into<3>(ctx, mg, l0, l0.r, 1, st, &first_done));
   BT_CHECK(enqueue_coarse(ctx, mg, 1, first_done, st));
-  BT_LAUNCH(ctx, k_mg_prolong<3>, grid_n(ctx, nV), 256, 0, nV, l0.agg, l0.Q, level_result(mg, 1), l0.x, st);
+  BT_LAUNCH_PDL(ctx, k_mg_prolong<3>, grid_n(ctx, nV), 256, 0, nV, l0.agg, l0.Q, level_result(mg, 1), l0.x, st);
   if (sm.gl) {
     BT_CHECK(resid0(ctx, plan, values, r, l0.x, l0.r, st));
     BT_CHECK(fac_lower(ctx, plan, sm, l0.r, y, st));
@@ -1370,7 +1396,7 @@ int mg_enqueue_apply(bartels_ctx ctx, bartels_mesh_plan plan, const float *value
   } else {
     const int G = plan_lanes_spmv(ctx, plan);
     const int g = grid_rows(ctx, nV, G);
-    BT_MG_G(G, BT_LAUNCH(ctx, k_mg0_post_bj<GL>, g, 256, 0, nV, plan->brp, plan->bcol, values, sm.minv, r, l0.x, z,
+    BT_MG_G(G, BT_LAUNCH_PDL(ctx, k_mg0_post_bj<GL>, g, 256, 0, nV, plan->brp, plan->bcol, values, sm.minv, r, l0.x, z,
                          plan->pinned, c0, part, st));
   }
   return BARTELS_OK;

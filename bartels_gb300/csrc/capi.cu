@@ -317,7 +317,7 @@ int bartels_tetmesh_dq2(bartels_ctx ctx, bartels_mesh_plan plan, int model, cons
   const int64_t nnz = 9 * plan->nnzb;
   double *dq;
   BT_CHECK(stage_vec(ctx, ctx->stage_e, q, n, &dq));
-  BT_CHECK(plan->w_u.ensure(sizeof(float4) * (size_t)plan->nV));
+  BT_CHECK(plan->w_u.ensure(2 * sizeof(float4) * (size_t)plan->nV));
   BT_CHECK(plan->w_values.ensure(sizeof(float) * nnz));
   BT_CHECK(ctx->stage_d.ensure(sizeof(double) * nnz));
   float4 *u = plan->w_u.as<float4>();
@@ -589,7 +589,7 @@ int bartels_plan_hessian_d(bartels_ctx ctx, bartels_mesh_plan plan, int model, i
   BT_CHECK(check_plan(ctx, plan));
   if (!valid_model(model) || !q_d || (psd_mode != BARTELS_PSD_NONE && psd_mode != BARTELS_PSD_SIMPLE_FIX))
     return fail(BARTELS_E_INVALID_ARG, "bad arguments");
-  BT_CHECK(plan->w_u.ensure(sizeof(float4) * (size_t)plan->nV));
+  BT_CHECK(plan->w_u.ensure(2 * sizeof(float4) * (size_t)plan->nV));
   BT_CHECK(plan->w_values.ensure(sizeof(float) * 9 * (size_t)plan->nnzb));
   float4 *u = plan->w_u.as<float4>();
   BT_CHECK(launch_prep_u(ctx, plan, q_d, nullptr, 1.0, plan->dphi_matches_rest, u));

@@ -148,16 +148,24 @@ __global__ void k_build_records(int nT, const int4 *__restrict__ E, const double
 
 // FP32 per-vertex input of the Hessian kernel: displacement from the rest
 // shape (consistent element data, F = I + ...) or raw position.
+// u = q - X as an unevaluated float pair u = hi + lo (hi the nearest float,
+// lo the float nearest to the remainder): the edge differences that form F
+// then keep FP32 accuracy relative to themselves, instead of relative to |u|,
+// which under large deformation is many elements' length.
 __global__ void k_prep_u(int nV, const double *__restrict__ x, const double *__restrict__ q_base, double scale,
-                         const double *__restrict__ X, float4 *__restrict__ u) {
+                         const double *__restrict__ X, float4 *__restrict__ u, float4 *__restrict__ ul) {
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nV; v += gridDim.x * blockDim.x) {
     double q[3];
+    float hi[3], lo[3];
     for (int d = 0; d < 3; ++d) {
       q[d] = scale * x[3 * v + d];
       if (q_base) q[d] += q_base[3 * v + d];
       if (X) q[d] -= X[3 * v + d];
+      hi[d] = (float)q[d];
+      lo[d] = (float)(q[d] - (double)hi[d]);
     }
-    u[v] = make_float4((float)q[0], (float)q[1], (float)q[2], 0.f);
+    u[v] = make_float4(hi[0], hi[1], hi[2], 0.f);
+    ul[v] = make_float4(lo[0], lo[1], lo[2], 0.f);
   }
 }
 
@@ -369,17 +377,24 @@ __global__ void k_grad_gather(int nV, const int *__restrict__ inc_ptr, const int
 // precomputed in inc_pos. Every entry is therefore summed over its tets in tet
 // order, as the reference's setFromTriplets does. The chunk's values are then
 // written out with coalesced stores.
+// F of a tet from its vertices' displacement pairs (x = hi, l = lo): the edge
+// differences are (hi_a - hi_0) + (lo_a - lo_0).
 template <int MODEL>
 __device__ __forceinline__ void elem_F_from(const TetRec32 &r, const float4 &x0, const float4 &x1, const float4 &x2,
-                                            const float4 &x3, int add_identity, float *F) {
-  const float p0[3] = {x0.x, x0.y, x0.z}, p1[3] = {x1.x, x1.y, x1.z}, p2[3] = {x2.x, x2.y, x2.z},
-              p3[3] = {x3.x, x3.y, x3.z};
-  def_grad(F, p0, p1, p2, p3, r.dphi, add_identity != 0);
+                                            const float4 &x3, const float4 &l0, const float4 &l1, const float4 &l2,
+                                            const float4 &l3, int add_identity, float *F) {
+  const float d1[3] = {(x1.x - x0.x) + (l1.x - l0.x), (x1.y - x0.y) + (l1.y - l0.y), (x1.z - x0.z) + (l1.z - l0.z)};
+  const float d2[3] = {(x2.x - x0.x) + (l2.x - l0.x), (x2.y - x0.y) + (l2.y - l0.y), (x2.z - x0.z) + (l2.z - l0.z)};
+  const float d3[3] = {(x3.x - x0.x) + (l3.x - l0.x), (x3.y - x0.y) + (l3.y - l0.y), (x3.z - x0.z) + (l3.z - l0.z)};
+  const float z[3] = {0.f, 0.f, 0.f};
+  def_grad(F, z, d1, d2, d3, r.dphi, add_identity != 0);
 }
 
 template <int MODEL>
-__device__ __forceinline__ void elem_F(const TetRec32 &r, const float4 *__restrict__ u, int add_identity, float *F) {
-  elem_F_from<MODEL>(r, __ldg(u + r.idx.x), __ldg(u + r.idx.y), __ldg(u + r.idx.z), __ldg(u + r.idx.w), add_identity,
+__device__ __forceinline__ void elem_F(const TetRec32 &r, const float4 *__restrict__ u, const float4 *__restrict__ ul,
+                                       int add_identity, float *F) {
+  elem_F_from<MODEL>(r, __ldg(u + r.idx.x), __ldg(u + r.idx.y), __ldg(u + r.idx.z), __ldg(u + r.idx.w),
+                     __ldg(ul + r.idx.x), __ldg(ul + r.idx.y), __ldg(ul + r.idx.z), __ldg(ul + r.idx.w), add_identity,
                      F);
 }
 
@@ -403,7 +418,8 @@ __device__ __forceinline__ void with_law(const float *F, const float *pv, int co
 // F and the flag are stored per tet (12 floats) for the assembly kernel.
 template <int MODEL>
 __global__ void __launch_bounds__(128)
-k_psd_test(int nT, const TetRec32 *__restrict__ rec, const float4 *__restrict__ u, int add_identity, float tol,
+k_psd_test(int nT, const TetRec32 *__restrict__ rec, const float4 *__restrict__ u, const float4 *__restrict__ ul,
+           int add_identity, float tol,
            int corot_exact, float4 *__restrict__ fslot, int *__restrict__ list, int *__restrict__ count) {
   for (int t0 = blockIdx.x * blockDim.x; t0 < nT; t0 += gridDim.x * blockDim.x) {
     const int t = t0 + threadIdx.x;
@@ -414,7 +430,7 @@ k_psd_test(int nT, const TetRec32 *__restrict__ rec, const float4 *__restrict__ 
       float phi[4][3];
       phi4(r.dphi, phi);
       float F[9];
-      elem_F<MODEL>(r, u, add_identity, F);
+      elem_F<MODEL>(r, u, ul, add_identity, F);
       with_law<MODEL>(F, r.pv, corot_exact, [&](const auto &law) { flag = !psd_fast_ok(law, phi, tol); });
       // the assembly reads F and the flag from here instead of gathering the vertices again
       float4 *o = fslot + 3ll * t;
@@ -439,7 +455,8 @@ k_psd_test(int nT, const TetRec32 *__restrict__ rec, const float4 *__restrict__ 
 template <int MODEL>
 __global__ void __launch_bounds__(128)
 k_psd_eig(const int *__restrict__ list, const int *__restrict__ count, const TetRec32 *__restrict__ rec,
-          const float4 *__restrict__ u, int add_identity, float tol, int corot_exact, float *__restrict__ Nbuf) {
+          const float4 *__restrict__ u, const float4 *__restrict__ ul, int add_identity, float tol, int corot_exact,
+          float *__restrict__ Nbuf) {
   const int n = *count;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int t = __ldg(list + i);
@@ -448,7 +465,7 @@ k_psd_eig(const int *__restrict__ list, const int *__restrict__ count, const Tet
     float phi[4][3];
     phi4(r.dphi, phi);
     float F[9];
-    elem_F<MODEL>(r, u, add_identity, F);
+    elem_F<MODEL>(r, u, ul, add_identity, F);
     with_law<MODEL>(F, r.pv, corot_exact, [&](const auto &law) {
       float N[45];
       psd_eig_N(law, phi, tol, N);
@@ -464,6 +481,7 @@ k_psd_eig(const int *__restrict__ list, const int *__restrict__ count, const Tet
 struct HessInc {
   TetRec32 r;
   float4 x[4];
+  float4 xl[4];  // lo parts of the vertices' displacement pairs (without the pre-pass)
   uint32_t pos;
   int t, a;
   bool slow;
@@ -492,12 +510,16 @@ __device__ __forceinline__ void load_inc_head(const int *__restrict__ inc_tet, c
 }
 
 template <bool PRE>
-__device__ __forceinline__ void load_inc_x(const float4 *__restrict__ u, HessInc &h) {
+__device__ __forceinline__ void load_inc_x(const float4 *__restrict__ u, const float4 *__restrict__ ul, HessInc &h) {
   if constexpr (!PRE) {
     h.x[0] = __ldg(u + h.r.idx.x);
     h.x[1] = __ldg(u + h.r.idx.y);
     h.x[2] = __ldg(u + h.r.idx.z);
     h.x[3] = __ldg(u + h.r.idx.w);
+    h.xl[0] = __ldg(ul + h.r.idx.x);
+    h.xl[1] = __ldg(ul + h.r.idx.y);
+    h.xl[2] = __ldg(ul + h.r.idx.z);
+    h.xl[3] = __ldg(ul + h.r.idx.w);
   }
 }
 
@@ -533,7 +555,7 @@ __device__ __forceinline__ void hess_inc(const HessInc &h, float *row, int rs, f
         F[4] = h.x[1].x; F[5] = h.x[1].y; F[6] = h.x[1].z; F[7] = h.x[1].w;
         F[8] = h.x[2].x;
       } else {
-        elem_F_from<MODEL>(h.r, h.x[0], h.x[1], h.x[2], h.x[3], add_identity, F);
+        elem_F_from<MODEL>(h.r, h.x[0], h.x[1], h.x[2], h.x[3], h.xl[0], h.xl[1], h.xl[2], h.xl[3], add_identity, F);
       }
       const float pv[2] = {cK * h.r.pv[0], cK * h.r.pv[1]};
       float pa[3];
@@ -597,8 +619,8 @@ template <int MODEL, bool PSD>
 __global__ void __launch_bounds__(kChunkMaxVerts)
 k_hess(const int *__restrict__ chunk_v, const int *__restrict__ brp, const int *__restrict__ inc_ptr,
        const int *__restrict__ inc_tet, const uint32_t *__restrict__ inc_pos, const TetRec32 *__restrict__ rec,
-       const float4 *__restrict__ u, int add_identity, float cK, float cM, float tol, int corot_exact,
-       const float4 *__restrict__ fslot, const float *__restrict__ Nbuf, float *__restrict__ values) {
+       const float4 *__restrict__ u, const float4 *__restrict__ ul, int add_identity, float cK, float cM, float tol,
+       int corot_exact, const float4 *__restrict__ fslot, const float *__restrict__ Nbuf, float *__restrict__ values) {
   constexpr bool PRE = PSD && MODEL >= 0;
   extern __shared__ float sbuf[];
   const int v0 = chunk_v[blockIdx.x], v1 = chunk_v[blockIdx.x + 1];
@@ -621,8 +643,8 @@ k_hess(const int *__restrict__ chunk_v, const int *__restrict__ brp, const int *
       HessInc h0, h1;
       load_inc_head<PRE>(inc_tet, inc_pos, rec, fslot, k, h0);
       load_inc_head<PRE>(inc_tet, inc_pos, rec, fslot, two ? k + 1 : k, h1);
-      load_inc_x<PRE>(u, h0);
-      load_inc_x<PRE>(u, h1);
+      load_inc_x<PRE>(u, ul, h0);
+      load_inc_x<PRE>(u, ul, h1);
       jd = (h0.pos >> (8 * h0.a)) & 255;
       hess_inc<MODEL, PSD>(h0, row, rs, D, add_identity, cK, cM, tol, corot_exact, Nbuf);
       if (two) hess_inc<MODEL, PSD>(h1, row, rs, D, add_identity, cK, cM, tol, corot_exact, Nbuf);
@@ -768,7 +790,7 @@ int plan_refresh_records(bartels_mesh_plan plan) {
 int launch_prep_u(bartels_ctx ctx, bartels_mesh_plan plan, const double *x, const double *q_base, double scale,
                   bool displacement, float4 *u) {
   BT_LAUNCH(ctx, k_prep_u, grid_for(ctx, plan->nV, 256), 256, 0, plan->nV, x, q_base, scale,
-            displacement ? plan->X : (const double *)nullptr, u);
+            displacement ? plan->X : (const double *)nullptr, u, u + plan->nV);
   return BARTELS_OK;
 }
 
@@ -885,6 +907,7 @@ static int launch_hess_t(bartels_ctx ctx, bartels_mesh_plan plan, const float4 *
   }
   float4 *fslot = nullptr;
   float *nbuf = nullptr;
+  const float4 *ul = u + plan->nV;  // lo parts of the displacement pairs follow the hi parts
   if constexpr (PSD && MODEL >= 0) {
     const size_t nT = (size_t)plan->nT;
     // F + flag slots (12 floats per tet), N (45 floats per tet), the slow-tet list and its count
@@ -894,13 +917,14 @@ static int launch_hess_t(bartels_ctx ctx, bartels_mesh_plan plan, const float4 *
     int *list = reinterpret_cast<int *>(nbuf + 45 * nT);
     int *count = list + nT;
     BT_CUDA(cudaMemsetAsync(count, 0, sizeof(int), ctx->stream));
-    BT_LAUNCH(ctx, k_psd_test<MODEL>, grid_for(ctx, plan->nT, 128), 128, 0, plan->nT, plan->rec32, u, add_identity,
-              tol, corot_exact, fslot, list, count);
-    BT_LAUNCH(ctx, k_psd_eig<MODEL>, grid_for(ctx, plan->nT, 128), 128, 0, list, count, plan->rec32, u,
+    BT_LAUNCH(ctx, k_psd_test<MODEL>, grid_for(ctx, plan->nT, 128), 128, 0, plan->nT, plan->rec32, u, ul,
+              add_identity, tol, corot_exact, fslot, list, count);
+    BT_LAUNCH(ctx, k_psd_eig<MODEL>, grid_for(ctx, plan->nT, 128), 128, 0, list, count, plan->rec32, u, ul,
               add_identity, tol, corot_exact, nbuf);
   }
   BT_LAUNCH(ctx, (k_hess<MODEL, PSD>), plan->nchunks, kChunkMaxVerts, smem, plan->chunk_v, plan->brp, plan->inc_ptr,
-            plan->inc_tet, plan->inc_pos, plan->rec32, u, add_identity, cK, cM, tol, corot_exact, fslot, nbuf, values);
+            plan->inc_tet, plan->inc_pos, plan->rec32, u, ul, add_identity, cK, cM, tol, corot_exact, fslot, nbuf,
+            values);
   return BARTELS_OK;
 }
 

@@ -43,6 +43,26 @@ const char *last_error_cstr();
       return ::bartels::fail(BARTELS_E_DEVICE, std::string("launch ") + #kernel + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
+// The same with programmatic dependent launch (the kernel must call pdl_wait()
+// before it reads anything its predecessor writes).
+#define BT_LAUNCH_PDL(ctx, kernel, grid, block, smem, ...)                                 \
+  do {                                                                                      \
+    cudaLaunchConfig_t cfg_ = {};                                                           \
+    cfg_.gridDim = dim3(grid);                                                              \
+    cfg_.blockDim = dim3(block);                                                            \
+    cfg_.dynamicSmemBytes = (smem);                                                         \
+    cfg_.stream = (ctx)->stream;                                                            \
+    cudaLaunchAttribute at_[1];                                                             \
+    at_[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;                         \
+    at_[0].val.programmaticStreamSerializationAllowed = 1;                                  \
+    cfg_.attrs = at_;                                                                       \
+    cfg_.numAttrs = 1;                                                                      \
+    cudaError_t e_ = cudaLaunchKernelEx(&cfg_, kernel, __VA_ARGS__);                         \
+    (ctx)->launches++;                                                                      \
+    if (e_ != cudaSuccess)                                                                  \
+      return ::bartels::fail(BARTELS_E_DEVICE, std::string("launch ") + #kernel + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
 // ------------------------------------------------------------------ records ---
 // FP32 record of one tet for the Hessian kernels: 64 bytes, one aligned line
 // pair, loaded with four 16-byte loads.

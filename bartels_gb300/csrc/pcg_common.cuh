@@ -35,6 +35,16 @@ __device__ __forceinline__ void apply_minv(const float *__restrict__ minv, int v
   z[2] = m02 * r[0] + m12 * r[1] + m22 * r[2];
 }
 
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialisation (BT_LAUNCH_PDL) may be scheduled while its predecessor is
+// finishing; pdl_wait() returns once the predecessor has completed and its
+// memory is visible, so every such kernel calls it before touching any data
+// (it returns at once for a kernel launched without the attribute).
+// pdl_trigger() lets the successor be scheduled once every block of this
+// kernel runs.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // ------------------------------------------------------------- reductions ---
 __device__ __forceinline__ double warp_sum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);

@@ -137,6 +137,8 @@ __global__ void k_pcg_init(int nb, int n, const float *__restrict__ rres, const 
                            float *__restrict__ p0, float *__restrict__ p1, double *__restrict__ part_a,
                            double *__restrict__ part_b, PcgState *__restrict__ st, double inner_rel2, double abs_tol2,
                            int max_it, int cont) {
+  pdl_wait();
+  pdl_trigger();
   float arz = 0.f, arr = 0.f;
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nb; v += gridDim.x * blockDim.x) {
     float rv[3], zv[3];
@@ -205,6 +207,8 @@ k_spmv_blk_g(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, 
 __global__ void __launch_bounds__(256)
 k_pcg_dir(int n, const float *__restrict__ z, float *__restrict__ pa, float *__restrict__ pb,
           const PcgState *__restrict__ st) {
+  pdl_wait();
+  pdl_trigger();
   if (st->done) return;
   const int it = st->it;
   const float beta = st->beta;
@@ -228,6 +232,8 @@ __global__ void __launch_bounds__(256)
 k_pcg_spmv_blk(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, const float *__restrict__ val,
                const float *__restrict__ pa, const float *__restrict__ pb, float *__restrict__ ap,
                const unsigned char *__restrict__ pinned, double *__restrict__ part, PcgState *__restrict__ st) {
+  pdl_wait();
+  pdl_trigger();
   if (st->done) return;
   const float *p = (st->it & 1) ? pb : pa;
   float acc = 0.f;
@@ -260,6 +266,8 @@ __global__ void __launch_bounds__(256)
 k_pcg_spmv_csr(int n, const int *__restrict__ rp, const int *__restrict__ ci, const float *__restrict__ val,
                const float *__restrict__ pa, const float *__restrict__ pb, float *__restrict__ ap,
                double *__restrict__ part, PcgState *__restrict__ st) {
+  pdl_wait();
+  pdl_trigger();
   if (st->done) return;
   const float *p = (st->it & 1) ? pb : pa;
   const int lane = threadIdx.x & 31;
@@ -317,6 +325,8 @@ k_pcg_update(int nb, int n, const float *__restrict__ minv, const float *__restr
              const float *__restrict__ pb, const float *__restrict__ ap, float *__restrict__ x,
              float *__restrict__ r, float *__restrict__ z, double *__restrict__ part_a, double *__restrict__ part_b,
              PcgState *__restrict__ st) {
+  pdl_wait();
+  pdl_trigger();
   if (st->done) return;
   const int it = st->it;
   const float *p = (it & 1) ? pb : pa;
@@ -537,6 +547,8 @@ __global__ void __launch_bounds__(256)
 k_pcg_prec_lower(int nV, const int4 *__restrict__ meta, const int *__restrict__ bcol,
                  const __nv_bfloat16 *__restrict__ gl, const float *__restrict__ r, float *__restrict__ y,
                  const unsigned char *__restrict__ pinned, double *__restrict__ part, PcgState *__restrict__ st) {
+  pdl_wait();
+  pdl_trigger();
   if (st->done) return;
   float acc = 0.f;
   BT_ROW_LOOP_BEGIN(G)
@@ -575,6 +587,8 @@ __global__ void __launch_bounds__(256)
 k_pcg_prec_upper(int nV, const int4 *__restrict__ meta, const int *__restrict__ bcol,
                  const __nv_bfloat16 *__restrict__ gu, const float *__restrict__ y, float *__restrict__ pa,
                  float *__restrict__ pb, const unsigned char *__restrict__ pinned, const PcgState *__restrict__ st) {
+  pdl_wait();
+  pdl_trigger();
   if (st->done) return;
   const int it = st->it;
   const float beta = st->beta;
@@ -603,6 +617,8 @@ k_pcg_prec_upper(int nV, const int4 *__restrict__ meta, const int *__restrict__ 
 __global__ void __launch_bounds__(256)
 k_pcg_update_f(int n, const float *__restrict__ pa, const float *__restrict__ pb, const float *__restrict__ ap,
                float *__restrict__ x, float *__restrict__ r, double *__restrict__ part, PcgState *__restrict__ st) {
+  pdl_wait();
+  pdl_trigger();
   if (st->done) return;
   const int it = st->it;
   const float *p = (it & 1) ? pb : pa;
@@ -649,6 +665,8 @@ k_pcg_update_f(int n, const float *__restrict__ pa, const float *__restrict__ pb
 __global__ void k_pcg_init_f(int n, const float *__restrict__ rres, float *__restrict__ x, float *__restrict__ r,
                              float *__restrict__ p0, float *__restrict__ p1, double *__restrict__ part,
                              PcgState *__restrict__ st, double inner_rel2, double abs_tol2, int max_it, int cont) {
+  pdl_wait();
+  pdl_trigger();
   float arr = 0.f;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float rv = rres[i];
@@ -740,9 +758,9 @@ static int pcg_enqueue_prec(bartels_ctx ctx, const PcgOperator &op, const PcgWor
   const int G = lanes_tri(ctx, plan);
   const int gt = grid_spmv(ctx, (int64_t)plan->nV * G / 32 + 1);
 #define BT_T(G_)                                                                                                 \
-  BT_LAUNCH(ctx, k_pcg_prec_lower<G_>, gt, 256, 0, plan->nV, op.fp->meta, plan->bcol, op.gl, w.r, w.ap, op.pinned, \
+  BT_LAUNCH_PDL(ctx, k_pcg_prec_lower<G_>, gt, 256, 0, plan->nV, op.fp->meta, plan->bcol, op.gl, w.r, w.ap, op.pinned, \
             w.part_b, w.st);                                                                                     \
-  BT_LAUNCH(ctx, k_pcg_prec_upper<G_>, gt, 256, 0, plan->nV, op.fp->meta, plan->bcol, op.gu, w.ap, w.pa, w.pb,     \
+  BT_LAUNCH_PDL(ctx, k_pcg_prec_upper<G_>, gt, 256, 0, plan->nV, op.fp->meta, plan->bcol, op.gu, w.ap, w.pa, w.pb,     \
             op.pinned, w.st)
   if (G == 4) {
     BT_T(4);
@@ -756,13 +774,13 @@ static int pcg_enqueue_prec(bartels_ctx ctx, const PcgOperator &op, const PcgWor
 // z = B r (V-cycle; its last kernel forms r.z and beta), then p = z + beta p
 static int pcg_enqueue_mg(bartels_ctx ctx, const PcgOperator &op, const PcgWork &w, int n, bool pre_done) {
   BT_CHECK(mg_enqueue_apply(ctx, op.plan, op.values, op.sm, w.r, w.z, w.ap, w.part_b, w.st, pre_done));
-  BT_LAUNCH(ctx, k_pcg_dir, grid_vec(ctx, (n + 3) / 4), 256, 0, n, w.z, w.pa, w.pb, w.st);
+  BT_LAUNCH_PDL(ctx, k_pcg_dir, grid_vec(ctx, (n + 3) / 4), 256, 0, n, w.z, w.pa, w.pb, w.st);
   return BARTELS_OK;
 }
 
 static int pcg_spmv_blk(bartels_ctx ctx, const PcgOperator &op, const PcgWork &w, int lanes, int gs) {
 #define BT_K0(G)                                                                                                 \
-  BT_LAUNCH(ctx, k_pcg_spmv_blk<G>, gs, 256, 0, op.plan->nV, op.plan->brp, op.plan->bcol, op.values, w.pa, w.pb, \
+  BT_LAUNCH_PDL(ctx, k_pcg_spmv_blk<G>, gs, 256, 0, op.plan->nV, op.plan->brp, op.plan->bcol, op.values, w.pa, w.pb, \
             w.ap, op.pinned, w.part_a, w.st)
   if (lanes == 4) BT_K0(4);
   else if (lanes == 16) BT_K0(16);
@@ -783,7 +801,7 @@ static int pcg_enqueue_iters(bartels_ctx ctx, const PcgOperator &op, const PcgWo
       // p was formed at the end of the previous iteration (or at the start of the solve)
       BT_CHECK(pcg_spmv_blk(ctx, op, w, lanes, gs));
       if (op.sm.gl) {
-        BT_LAUNCH(ctx, k_pcg_update_f, gd, 256, 0, n, w.pa, w.pb, w.ap, w.x, w.r, w.part_b, w.st);
+        BT_LAUNCH_PDL(ctx, k_pcg_update_f, gd, 256, 0, n, w.pa, w.pb, w.ap, w.x, w.r, w.part_b, w.st);
       } else {
         BT_CHECK(mg_enqueue_update(ctx, op.plan, op.sm, w.pa, w.pb, w.ap, w.x, w.r, w.part_b, w.st));
       }
@@ -791,23 +809,23 @@ static int pcg_enqueue_iters(bartels_ctx ctx, const PcgOperator &op, const PcgWo
       continue;
     }
     // with the factor preconditioner the direction is formed by k_pcg_prec_upper
-    if (!fac) BT_LAUNCH(ctx, k_pcg_dir, gd, 256, 0, n, w.z, w.pa, w.pb, w.st);
+    if (!fac) BT_LAUNCH_PDL(ctx, k_pcg_dir, gd, 256, 0, n, w.z, w.pa, w.pb, w.st);
     if (blk) {
 #define BT_K1(G)                                                                                                 \
-  BT_LAUNCH(ctx, k_pcg_spmv_blk<G>, gs, 256, 0, op.plan->nV, op.plan->brp, op.plan->bcol, op.values, w.pa, w.pb, \
+  BT_LAUNCH_PDL(ctx, k_pcg_spmv_blk<G>, gs, 256, 0, op.plan->nV, op.plan->brp, op.plan->bcol, op.values, w.pa, w.pb, \
             w.ap, op.pinned, w.part_a, w.st)
       if (lanes == 4) BT_K1(4);
       else if (lanes == 16) BT_K1(16);
       else BT_K1(8);
 #undef BT_K1
     } else {
-      BT_LAUNCH(ctx, k_pcg_spmv_csr, gs, 256, 0, n, op.rp, op.ci, op.values, w.pa, w.pb, w.ap, w.part_a, w.st);
+      BT_LAUNCH_PDL(ctx, k_pcg_spmv_csr, gs, 256, 0, n, op.rp, op.ci, op.values, w.pa, w.pb, w.ap, w.part_a, w.st);
     }
     if (fac) {
-      BT_LAUNCH(ctx, k_pcg_update_f, gd, 256, 0, n, w.pa, w.pb, w.ap, w.x, w.r, w.part_b, w.st);
+      BT_LAUNCH_PDL(ctx, k_pcg_update_f, gd, 256, 0, n, w.pa, w.pb, w.ap, w.x, w.r, w.part_b, w.st);
       BT_CHECK(pcg_enqueue_prec(ctx, op, w));
     } else {
-      BT_LAUNCH(ctx, k_pcg_update, gu, 256, 0, nb, n, w.minv, w.pa, w.pb, w.ap, w.x, w.r, w.z, w.part_a, w.part_b,
+      BT_LAUNCH_PDL(ctx, k_pcg_update, gu, 256, 0, nb, n, w.minv, w.pa, w.pb, w.ap, w.x, w.r, w.z, w.part_a, w.part_b,
                 w.st);
     }
   }
@@ -819,13 +837,15 @@ static int pcg_enqueue_iters(bartels_ctx ctx, const PcgOperator &op, const PcgWo
 // is bounded independently of the iteration count (the iteration cap of the
 // state bounds both).
 __global__ void k_pcg_cond(cudaGraphConditionalHandle h, PcgState *st) {
+  pdl_wait();
+  pdl_trigger();
   const unsigned int loops = ++st->loops;
   const bool more = !st->done && st->it < st->max_it && loops <= (unsigned int)st->max_it + 4u;
   cudaGraphSetConditional(h, more ? 1u : 0u);
 }
 
 static int launch_cond(bartels_ctx ctx, cudaGraphConditionalHandle h, PcgState *st) {
-  BT_LAUNCH(ctx, k_pcg_cond, 1, 1, 0, h, st);
+  BT_LAUNCH_PDL(ctx, k_pcg_cond, 1, 1, 0, h, st);
   return BARTELS_OK;
 }
 
@@ -998,15 +1018,15 @@ static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double
     const int cont = (pass > 0 && !prm.restart) ? 1 : 0;
     const int it0 = cont ? hs.it : 0;
     if (op.mg) {
-      BT_LAUNCH(ctx, k_pcg_init_f, gv, 256, 0, n, w.rres, w.x, w.r, w.pa, w.pb, w.part_a, w.st,
+      BT_LAUNCH_PDL(ctx, k_pcg_init_f, gv, 256, 0, n, w.rres, w.x, w.r, w.pa, w.pb, w.part_a, w.st,
                 prm.inner_rel_tol * prm.inner_rel_tol, abs2, prm.max_iters - rep->iterations, cont);
       BT_CHECK(pcg_enqueue_mg(ctx, op, w, n, false));
     } else if (op.gl) {
-      BT_LAUNCH(ctx, k_pcg_init_f, gv, 256, 0, n, w.rres, w.x, w.r, w.pa, w.pb, w.part_a, w.st,
+      BT_LAUNCH_PDL(ctx, k_pcg_init_f, gv, 256, 0, n, w.rres, w.x, w.r, w.pa, w.pb, w.part_a, w.st,
                 prm.inner_rel_tol * prm.inner_rel_tol, abs2, prm.max_iters - rep->iterations, cont);
       BT_CHECK(pcg_enqueue_prec(ctx, op, w));
     } else {
-      BT_LAUNCH(ctx, k_pcg_init, gv, 256, 0, nb, n, w.rres, w.minv, w.x, w.r, w.z, w.pa, w.pb, w.part_a, w.part_b,
+      BT_LAUNCH_PDL(ctx, k_pcg_init, gv, 256, 0, nb, n, w.rres, w.minv, w.x, w.r, w.z, w.pa, w.pb, w.part_a, w.part_b,
                 w.st, prm.inner_rel_tol * prm.inner_rel_tol, abs2, prm.max_iters - rep->iterations, cont);
     }
     for (;;) {
@@ -1142,7 +1162,7 @@ struct NewtonWork {
 static int newton_work(bartels_mesh_plan plan, NewtonWork &w) {
   const size_t n = 3 * (size_t)plan->nV;
   BT_CHECK(plan->w_vec.ensure(sizeof(double) * (3 * n + 16)));
-  BT_CHECK(plan->w_u.ensure(sizeof(float4) * (size_t)plan->nV));
+  BT_CHECK(plan->w_u.ensure(2 * sizeof(float4) * (size_t)plan->nV));
   BT_CHECK(plan->w_values.ensure(sizeof(float) * 9 * (size_t)plan->nnzb));
   double *b = plan->w_vec.as<double>();
   w.g = b;
@@ -1350,7 +1370,7 @@ int plan_spmv(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, cons
   double *part = plan->w_spmv.as<double>();
   PcgState *st = reinterpret_cast<PcgState *>(plan->w_spmv.as<char>() + o_st);
 #define BT_SPMV(G)                                                                                              \
-  BT_LAUNCH(ctx, k_pcg_spmv_blk<G>, g, 256, 0, plan->nV, plan->brp, plan->bcol, values, x, x, y, plan->pinned, \
+  BT_LAUNCH_PDL(ctx, k_pcg_spmv_blk<G>, g, 256, 0, plan->nV, plan->brp, plan->bcol, values, x, x, y, plan->pinned, \
             part, st)
   if (lanes == 4) BT_SPMV(4);
   else if (lanes == 16) BT_SPMV(16);

@@ -496,8 +496,9 @@ int bartels_tetmesh_q_d(bartels_ctx ctx, bartels_mesh_plan plan, int model, cons
 int bartels_tetmesh_dq_d(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q_d, double *g_d);
 /* Energy of every tet, psi(F) vol (linear_tet_{neohookean,stvk,corotational}_q
  * per element, src/linear_tet_neohookean_q.cpp:5-18, with the plan's element
- * data) at device positions q_d into device e_d (nT doubles): the terms
- * bartels_tetmesh_q_d sums. FP64. */
+ * data; for LINEAR_ELASTICITY the stored params are the Lame pair) at device
+ * positions q_d into device e_d (nT doubles): the terms bartels_tetmesh_q_d
+ * sums. FP64. */
 int bartels_tetmesh_q_elements_d(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q_d,
                                  double *e_d);
 

@@ -62,7 +62,13 @@ def _check_elements(oracle, model, V, E, q, psd_tols):
     params = material_params(model, len(E), 2e6, 0.45)
     Vx, Ex, qx = _explode(V, E, q)
     plan = bg.MeshPlan(Vx, Ex)
-    plan.set_element_data(params=params)
+    # the plan stores linear elasticity's parameters as the Lame pair (the
+    # entry points that take params convert the reference's (E, nu) to it)
+    stored = params
+    if model == "linear_elasticity":
+        young, nu = params[:, 0], params[:, 1]
+        stored = np.stack([young * nu / ((1 + nu) * (1 - 2 * nu)), young / (2 * (1 + nu))], axis=1)
+    plan.set_element_data(params=stored)
     dphi, vol = oracle.dphi_dX(Vx, Ex), oracle.volume(Vx, Ex)
     # energies
     q_d = torch.from_numpy(qx.ravel().copy()).cuda()
