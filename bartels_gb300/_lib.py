@@ -114,7 +114,11 @@ SIGNATURES = [
     ("bartels_newton_get_problem", C.c_int, [_P, _D, _D]),
     ("bartels_plan_autotune", C.c_int, [_P, _P, _P, C.c_int, _I, _I]),
     ("bartels_segment_sumsq_d", C.c_int, [_P, C.c_int, _P, _P, _P]),
+    ("bartels_plan_set_segments", C.c_int, [_P, C.c_int, _I, C.POINTER(C.c_int64)]),
+    ("bartels_plan_set_segment_active", C.c_int, [_P, _P]),
+    ("bartels_plan_segment_pcg_iterations", C.c_int, [_P, _I]),
     ("bartels_gemm_bf16_d", C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, C.c_int, _P, _P, C.c_int, _P, C.c_int]),
+    ("bartels_gemm_bf16_wait_probe_d", C.c_int, [_P, C.c_int, C.c_int, C.c_int, _P, C.c_int, _P, _P, C.c_int, C.c_int]),
     ("bartels_newton_iterate_d", C.c_int,
      [_P, _P, C.POINTER(NewtonParams), _P, C.c_double, _I, C.POINTER(NewtonReport)]),
     ("bartels_tri_plan_create", C.c_int, [_P, C.c_int, C.c_int, _I, C.c_int, C.POINTER(_P)]),

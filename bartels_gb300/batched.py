@@ -1,14 +1,19 @@
 """Batched Newton over many meshes of uneven size packed into one plan.
 
-    python -m bartels_gb300.batched [--count 256] [--nmin 8] [--nmax 40] [--precond jacobi|learned]
+    python -m bartels_gb300.batched [--count 256] [--nmin 8] [--nmax 40]
+                                    [--precond jacobi|multigrid|learned_multigrid|learned]
 
 All instances become one block-diagonal system on a single plan, so every
 Newton stage (gradient, fused Hessian, each PCG kernel, line search) is one
-grid-stride launch over all instances, and the PCG inner loop runs as CUDA
-graphs. Each instance is checked against its own relative gradient criterion
-(bartels_segment_sumsq_d over its vertex range); the Newton loop runs until
-every instance satisfies it. The SpMV / factor-pass lane counts come from the
-autotuner (bartels_plan_autotune), cached per size bucket.
+launch over all instances, and the PCG inner loop runs as one CUDA graph. The
+plan is told where the instances lie (bartels_plan_set_segments), so each
+instance keeps its own PCG scalars and its own line-search step: every
+instance follows the Newton iterates it would follow alone. Each instance is
+checked against its own relative gradient criterion (bartels_segment_sumsq_d
+over its vertex range) and stops taking steps once it meets it
+(bartels_plan_set_segment_active); the loop ends when every instance has. The
+SpMV / factor-pass lane counts come from the autotuner (bartels_plan_autotune),
+cached per size bucket.
 
 Instances (seeded): Neo-Hookean Kuhn cubes, n uniform in [nmin, nmax], Young's
 modulus log-uniform in [1e5, 1e7] Pa, Poisson ratio uniform in [0.30, 0.48],
@@ -77,6 +82,10 @@ def solve(packed, dt=0.01, tol=1e-8, max_newton=60, precond="jacobi", net=None, 
     from .api import volume as _volume
     f_g = plan.const_ext_force(_volume(V, E), np.array([0.0, 0.0, -9.81 * rho]))
     plan.set_problem(q_base=packed["q_base"].ravel(), x_hat=np.zeros(3 * nV), f_ext=f_g, pinned=packed["pinned"])
+    voff_h = np.ascontiguousarray(packed["voff"], np.int32)
+    toff_h = np.ascontiguousarray(packed["toff"], np.int64)
+    _lib.check(L.bartels_plan_set_segments(plan.handle, ns, voff_h.ctypes.data_as(C.POINTER(C.c_int)),
+                                           toff_h.ctypes.data_as(C.POINTER(C.c_int64))), "set_segments")
     t_setup = time.perf_counter() - t0
     prm = bg.newton_params(model="neohookean", psd_mode=_lib.PSD_SIMPLE_FIX, psd_tol=1e-6, mass_coeff=1.0, scale=dt,
                            force_scale=dt, gradient_tol=0.0, relative=0, max_iterations=1 << 30)
@@ -105,6 +114,12 @@ def solve(packed, dt=0.01, tol=1e-8, max_newton=60, precond="jacobi", net=None, 
         tuned = dict(spmv_lanes=a.value, factor_lanes=b.value, seconds=round(time.perf_counter() - t1, 3))
     if precond == "learned":
         net.attach(plan)
+    elif precond == "learned_multigrid":
+        net.attach(plan, multigrid=True)
+    elif precond == "multigrid":
+        _lib.check(L.bartels_plan_set_preconditioner(plan.handle, _lib.PRECOND_MULTIGRID, None), "precond")
+    if precond in ("multigrid", "learned_multigrid"):
+        prm.pcg.inner_rel_tol = 1e-2
     g0 = inst_norms()
     rep = _lib.NewtonReport()
     its = 0
@@ -117,10 +132,12 @@ def solve(packed, dt=0.01, tol=1e-8, max_newton=60, precond="jacobi", net=None, 
                                               C.byref(done), C.byref(rep)), "newton_iterate")
         its += 1
         rel = inst_norms() / np.maximum(g0, 1e-300)
+        active = (rel > tol).astype(np.uint8)
+        _lib.check(L.bartels_plan_set_segment_active(plan.handle, active.ctypes.data_as(C.c_void_p)), "active")
         if log:
             log(json.dumps(dict(newton=its, max_rel=float(rel.max()), median_rel=float(np.median(rel)),
-                                pcg=rep.last_pcg_iterations, alpha=rep.last_alpha)))
-        if rel.max() <= tol:
+                                active=int(active.sum()), pcg=rep.last_pcg_iterations, alpha=rep.last_alpha)))
+        if not active.any():
             break
     torch.cuda.synchronize()
     t_solve = time.perf_counter() - t1
@@ -139,7 +156,7 @@ def main(argv=None):
     ap.add_argument("--nmin", type=int, default=8)
     ap.add_argument("--nmax", type=int, default=40)
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--precond", default="jacobi", choices=["jacobi", "learned"])
+    ap.add_argument("--precond", default="jacobi", choices=["jacobi", "multigrid", "learned_multigrid", "learned"])
     ap.add_argument("--tol", type=float, default=1e-8)
     args = ap.parse_args(argv)
     t = time.time()
@@ -148,7 +165,7 @@ def main(argv=None):
     print(json.dumps(dict(instances=args.count, vertices=len(packed["V"]), tets=len(packed["E"]),
                           pack_s=round(time.time() - t, 1))), flush=True)
     net = None
-    if args.precond == "learned":
+    if args.precond in ("learned", "learned_multigrid"):
         import bartels_gb300 as bg
         from bartels_gb300 import lpcg
         net = lpcg.LearnedPreconditioner.load(lpcg.WEIGHTS, bg.Context.default())

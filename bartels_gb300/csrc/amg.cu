@@ -401,6 +401,7 @@ int mg_prepare(bartels_ctx ctx, bartels_mesh_plan plan) {
     BT_CHECK(dalloc_n(mg, &d.d, nv));
     if (l > 0) BT_CHECK(dalloc_n(mg, &d.d2, nv));
   }
+  if (env_int("BARTELS_MG_FINE_BF16", 1, 0, 1)) BT_CHECK(dalloc_n(mg, &mg->a16, 9 * (size_t)plan->nnzb));
   if (mg->dense) {
     mg->nd = 6 * mg->lv.back().n;
     BT_CHECK(dalloc_n(mg, &mg->ainv, (size_t)mg->nd * mg->nd));
@@ -782,10 +783,38 @@ k_mg0_update(int nV, const float *__restrict__ pa, const float *__restrict__ pb,
   }
 }
 
-// out = b - A x, or A x without b (rows of pinned vertices give 0)
-template <int G>
+// BF16 copy of the finest level's values for the V-cycle's SpMVs, exactly
+// symmetric: entry (3v+k, 3w+l) of block p = (v, w) and entry (3w+l, 3v+k) of
+// its transpose q = rev[p] both take bf16((A_p(k,l) + A_q(l,k)) / 2). One warp
+// per vertex row, one lane per block.
 __global__ void __launch_bounds__(256)
-k_mg0_resid(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, const float *__restrict__ val,
+k_mg0_to_bf16(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, const int *__restrict__ rev,
+              const float *__restrict__ val, __nv_bfloat16 *__restrict__ a16) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int v = warp; v < nV; v += nwarps) {
+    const int rb = brp[v], nb = brp[v + 1] - rb, rs = 3 * nb;
+    for (int j = lane; j < nb; j += 32) {
+      const int w = __ldg(bcol + rb + j);
+      const int q = __ldg(rev + rb + j);
+      const int rbw = __ldg(brp + w), rsw = 3 * (__ldg(brp + w + 1) - rbw), jq = q - rbw;
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int l = 0; l < 3; ++l) {
+          const float a = __ldg(val + 9ll * rb + k * rs + 3 * j + l);
+          const float t = __ldg(val + 9ll * rbw + l * rsw + 3 * jq + k);
+          a16[9ll * rb + k * rs + 3 * j + l] = __float2bfloat16_rn(0.5f * (a + t));
+        }
+    }
+  }
+}
+
+// out = b - A x, or A x without b (rows of pinned vertices give 0)
+template <int G, class VT>
+__global__ void __launch_bounds__(256)
+k_mg0_resid(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, const VT *__restrict__ val,
             const float *__restrict__ b, const float *__restrict__ x, float *__restrict__ out,
             const unsigned char *__restrict__ pinned, const PcgState *__restrict__ st) {
   pdl_wait();
@@ -812,9 +841,9 @@ k_mg0_resid(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, c
 // Final step of the V-cycle with the block-Jacobi smoother:
 // z = x + c Dinv (b - A x), partial sums of b.z; the last block stores r.z
 // and beta = r.z / r.z_old in the PCG state.
-template <int G>
+template <int G, class VT>
 __global__ void __launch_bounds__(256)
-k_mg0_post_bj(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, const float *__restrict__ val,
+k_mg0_post_bj(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, const VT *__restrict__ val,
               const float *__restrict__ minv, const float *__restrict__ b, const float *__restrict__ x,
               float *__restrict__ z, const unsigned char *__restrict__ pinned, const float *__restrict__ coef,
               double *__restrict__ part, PcgState *__restrict__ st) {
@@ -1293,12 +1322,19 @@ int fac_upper(bartels_ctx ctx, bartels_mesh_plan plan, const MgSmoother &sm, con
   return BARTELS_OK;
 }
 
+// out = b - A x on the finest level, with the V-cycle's BF16 copy of A when it has one
 int resid0(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const float *b, const float *x, float *out,
            const PcgState *st) {
   const int G = plan_lanes_spmv(ctx, plan);
   const int g = grid_rows(ctx, plan->nV, G);
-  BT_MG_G(G, BT_LAUNCH_PDL(ctx, k_mg0_resid<GL>, g, 256, 0, plan->nV, plan->brp, plan->bcol, values, b, x, out,
-                       plan->pinned, st));
+  using B16 = __nv_bfloat16;
+  const B16 *a16 = plan->mg ? plan->mg->a16 : nullptr;
+  if (a16)
+    BT_MG_G(G, BT_LAUNCH_PDL(ctx, (k_mg0_resid<GL, B16>), g, 256, 0, plan->nV, plan->brp, plan->bcol, a16, b, x, out,
+                             plan->pinned, st));
+  else
+    BT_MG_G(G, BT_LAUNCH_PDL(ctx, (k_mg0_resid<GL, float>), g, 256, 0, plan->nV, plan->brp, plan->bcol, values, b, x,
+                             out, plan->pinned, st));
   return BARTELS_OK;
 }
 
@@ -1316,6 +1352,12 @@ int mg_setup_numeric(bartels_ctx ctx, bartels_mesh_plan plan, const float *value
   MgHierarchy *mg = plan->mg;
   if (!mg) return fail(BARTELS_E_INVALID_ARG, "multigrid: no hierarchy");
   const int L = (int)mg->lv.size();
+  if (mg->a16) {
+    FactorPattern *fp = nullptr;
+    BT_CHECK(plan_factor_pattern(plan, &fp));
+    BT_LAUNCH(ctx, k_mg0_to_bf16, grid_rows(ctx, plan->nV, 32), 256, 0, plan->nV, plan->brp, plan->bcol, fp->rev,
+              values, mg->a16);
+  }
   for (int l = 0; l + 1 < L; ++l) {
     MgLevel &f = mg->lv[l], &c = mg->lv[l + 1];
     const int g = grid_n(ctx, c.nnzb, 128);
@@ -1396,8 +1438,13 @@ int mg_enqueue_apply(bartels_ctx ctx, bartels_mesh_plan plan, const float *value
   } else {
     const int G = plan_lanes_spmv(ctx, plan);
     const int g = grid_rows(ctx, nV, G);
-    BT_MG_G(G, BT_LAUNCH_PDL(ctx, k_mg0_post_bj<GL>, g, 256, 0, nV, plan->brp, plan->bcol, values, sm.minv, r, l0.x, z,
-                         plan->pinned, c0, part, st));
+    using B16 = __nv_bfloat16;
+    if (mg->a16)
+      BT_MG_G(G, BT_LAUNCH_PDL(ctx, (k_mg0_post_bj<GL, B16>), g, 256, 0, nV, plan->brp, plan->bcol,
+                               (const B16 *)mg->a16, sm.minv, r, l0.x, z, plan->pinned, c0, part, st));
+    else
+      BT_MG_G(G, BT_LAUNCH_PDL(ctx, (k_mg0_post_bj<GL, float>), g, 256, 0, nV, plan->brp, plan->bcol, values, sm.minv,
+                               r, l0.x, z, plan->pinned, c0, part, st));
   }
   return BARTELS_OK;
 }

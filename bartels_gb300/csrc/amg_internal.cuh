@@ -51,6 +51,9 @@ struct MgHierarchy {
   int pinned_gen = -1;    // plan->pinned_gen the hierarchy was built for
   int64_t coarse_nnz = 0; // stored entries of all coarse levels (operator complexity)
   PcgState *st_once = nullptr;  // state for a single application outside PCG
+  // BF16 copy of the finest level's values (the plan's layout), made exactly
+  // symmetric, for the V-cycle's own SpMVs (nullptr: the FP32 values are used)
+  __nv_bfloat16 *a16 = nullptr;
   std::vector<void *> allocs;
   ~MgHierarchy();
 };

@@ -35,6 +35,7 @@ int plan_precond_apply(bartels_ctx ctx, bartels_mesh_plan plan, const float *val
 int noalloc_gradient(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q_d, double *g_d);
 int plan_pcg(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const double *b, double *x,
              const bartels_pcg_params &prm, bartels_pcg_report *rep);
+int plan_set_segments(bartels_mesh_plan plan, int nseg, const int *voff, const int64_t *toff);
 int newton_gradient(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params &p, const double *x,
                     double *g);
 int newton_energy(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params &p, const double *x,
@@ -535,7 +536,18 @@ int bartels_newton_set_problem(bartels_mesh_plan plan, const double *q_base, con
   BT_CHECK(put(&plan->q_base, q_base));
   BT_CHECK(put(&plan->x_hat, x_hat));
   BT_CHECK(put(&plan->f_ext, f_ext));
-  plan->pinned_gen++;
+  // the pinned set's generation moves only when the set itself changes (the
+  // multigrid hierarchy of a plan is built for one set)
+  if (pinned) {
+    if (plan->h_pinned.size() != (size_t)plan->nV ||
+        std::memcmp(plan->h_pinned.data(), pinned, (size_t)plan->nV) != 0) {
+      plan->h_pinned.assign(pinned, pinned + plan->nV);
+      plan->pinned_gen++;
+    }
+  } else if (!plan->h_pinned.empty()) {
+    plan->h_pinned.clear();
+    plan->pinned_gen++;
+  }
   if (pinned) {
     if (!plan->pinned) BT_CUDA(cudaMalloc(&plan->pinned, (size_t)plan->nV));
     BT_CUDA(cudaMemcpyAsync(plan->pinned, pinned, (size_t)plan->nV, cudaMemcpyHostToDevice, ctx->stream));
@@ -794,6 +806,28 @@ int bartels_plan_autotune(bartels_ctx ctx, bartels_mesh_plan plan, const float *
   return plan_autotune(ctx, plan, values_d, force, spmv_lanes, factor_lanes);
 }
 
+int bartels_plan_set_segments(bartels_mesh_plan plan, int nseg, const int *vertex_offsets,
+                              const int64_t *tet_offsets) {
+  if (!plan) return fail(BARTELS_E_INVALID_ARG, "null plan");
+  BT_CHECK(check_ctx(plan->ctx));
+  return plan_set_segments(plan, nseg, vertex_offsets, tet_offsets);
+}
+
+int bartels_plan_set_segment_active(bartels_mesh_plan plan, const unsigned char *active) {
+  if (!plan || !active) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  if (!plan->seg) return fail(BARTELS_E_INVALID_ARG, "the plan has no segments");
+  plan->seg->active.assign(active, active + plan->seg->nseg);
+  return BARTELS_OK;
+}
+
+int bartels_plan_segment_pcg_iterations(bartels_mesh_plan plan, int *iterations) {
+  if (!plan || !iterations) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  if (!plan->seg) return fail(BARTELS_E_INVALID_ARG, "the plan has no segments");
+  for (int q = 0; q < plan->seg->nseg; ++q)
+    iterations[q] = q < (int)plan->seg->last_iters.size() ? plan->seg->last_iters[q] : 0;
+  return BARTELS_OK;
+}
+
 int bartels_segment_sumsq_d(bartels_ctx ctx, int nseg, const int *vertex_offsets_d, const double *v_d, double *out_d) {
   BT_CHECK(check_ctx(ctx));
   if (nseg < 0 || (nseg > 0 && (!vertex_offsets_d || !v_d || !out_d)))
@@ -801,8 +835,21 @@ int bartels_segment_sumsq_d(bartels_ctx ctx, int nseg, const int *vertex_offsets
   return segment_sumsq(ctx, nseg, vertex_offsets_d, v_d, out_d);
 }
 
+static int gemm_entry(bartels_ctx ctx, int M, int N, int K, const void *x_d, int ldx, const void *w_d,
+                      const float *bias_d, int relu, float *y_d, int ldy, int probe_polls);
+
 int bartels_gemm_bf16_d(bartels_ctx ctx, int M, int N, int K, const void *x_d, int ldx, const void *w_d,
                         const float *bias_d, int relu, float *y_d, int ldy) {
+  return gemm_entry(ctx, M, N, K, x_d, ldx, w_d, bias_d, relu, y_d, ldy, 0);
+}
+
+int bartels_gemm_bf16_wait_probe_d(bartels_ctx ctx, int M, int N, int K, const void *x_d, int ldx,
+                                   const void *w_d, float *y_d, int ldy, int polls) {
+  return gemm_entry(ctx, M, N, K, x_d, ldx, w_d, nullptr, 0, y_d, ldy, polls > 0 ? polls : 1);
+}
+
+static int gemm_entry(bartels_ctx ctx, int M, int N, int K, const void *x_d, int ldx, const void *w_d,
+                      const float *bias_d, int relu, float *y_d, int ldy, int probe_polls) {
   BT_CHECK(check_ctx(ctx));
   if (M < 0 || !x_d || !w_d || !y_d) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
   BT_CHECK(ctx->stage_e.ensure(sizeof(int)));
@@ -820,6 +867,7 @@ int bartels_gemm_bf16_d(bartels_ctx ctx, int M, int N, int K, const void *x_d, i
   g.y = y_d;
   g.ldy = ldy;
   g.err = err;
+  g.probe_polls = probe_polls;
   BT_CHECK(gemm_bf16(ctx, g));
   int h = 0;
   BT_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));

@@ -2,6 +2,7 @@
 // per-tet records, FP64 energy and gradient, and the fused FP32 Hessian
 // assembly (element math + PSD projection + deterministic per-row sums in tet
 // order, written straight into the CSR value array).
+#include <algorithm>
 #include <mutex>
 #include <string>
 
@@ -283,6 +284,54 @@ __global__ void k_energy_diff(int nT, const TetRec64 *__restrict__ rec, const do
       acc -= force_scale * alpha * f_ext[i] * dx[i];
   double s = block_sum(acc);
   if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+// Packed meshes: the terms of f(x + alpha_s d) - f(x) with every tet and
+// vertex taking its own segment's step (tseg / vseg): per tet the elastic and
+// mass difference (as k_energy_diff), per vertex the force term. A term whose
+// step is 0 is 0. The per-segment sums follow in fixed order.
+template <int MODEL>
+__global__ void k_energy_diff_seg(int nT, int nV, const TetRec64 *__restrict__ rec, const double *__restrict__ x,
+                                  const double *__restrict__ dx, const double *__restrict__ alpha_seg,
+                                  const int *__restrict__ tseg, const int *__restrict__ vseg,
+                                  const double *__restrict__ q_base, double scale, const double *__restrict__ X,
+                                  double mass_coeff, const double *__restrict__ x_hat, const double *__restrict__ f_ext,
+                                  double force_scale, double *__restrict__ et, double *__restrict__ ev) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nT; t += gridDim.x * blockDim.x) {
+    const double alpha = alpha_seg[tseg[t]];
+    if (alpha == 0.0) {
+      et[t] = 0.0;
+      continue;
+    }
+    const TetRec64 &r = rec[t];
+    double H0[9], H1[9];
+    disp_grad64(r, x, q_base, scale, X, nullptr, 0.0, H0);
+    disp_grad64(r, x, q_base, scale, X, dx, alpha, H1);
+    double acc = psi_model_disp<double>(MODEL, H1, r.pv) - psi_model_disp<double>(MODEL, H0, r.pv);
+    if (mass_coeff != 0.0) {
+      const int id[4] = {r.idx.x, r.idx.y, r.idx.z, r.idx.w};
+      double sd[3] = {0, 0, 0}, se[3] = {0, 0, 0}, de = 0.0, dd = 0.0;
+      for (int a = 0; a < 4; ++a)
+        for (int d = 0; d < 3; ++d) {
+          const int i = 3 * id[a] + d;
+          const double dv = dx[i], evv = x[i] - (x_hat ? x_hat[i] : 0.0);
+          sd[d] += dv;
+          se[d] += evv;
+          de += dv * evv;
+          dd += dv * dv;
+        }
+      const double m20 = r.mass / 20.0;
+      acc += mass_coeff * m20 * (alpha * (dot3(sd, se) + de) + 0.5 * alpha * alpha * (dot3(sd, sd) + dd));
+    }
+    et[t] = acc;
+  }
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nV; v += gridDim.x * blockDim.x) {
+    const double alpha = alpha_seg[vseg[v]];
+    double acc = 0.0;
+    if (f_ext && force_scale != 0.0 && alpha != 0.0)
+      for (int d = 0; d < 3; ++d) acc -= force_scale * alpha * f_ext[3 * v + d] * dx[3 * v + d];
+    ev[v] = acc;
+  }
 }
 
 // deterministic final sum of n partials (one block)
@@ -872,6 +921,27 @@ int energy_diff(bartels_ctx ctx, bartels_mesh_plan plan, int model, const Object
   }
 #undef BT_ED
   return reduce_sum(ctx, part, g, d_out);
+}
+
+int energy_diff_seg(bartels_ctx ctx, bartels_mesh_plan plan, int model, const ObjectiveDev &obj, const double *x,
+                    const double *dx, const double *alpha_seg, const int *tseg, const int *vseg, double *et,
+                    double *ev) {
+  const int g = grid_for(ctx, std::max(plan->nT, plan->nV), 256);
+  const double *X = plan->dphi_matches_rest ? plan->X : nullptr;
+#define BT_EDS(M)                                                                                                 \
+  BT_LAUNCH(ctx, k_energy_diff_seg<M>, g, 256, 0, plan->nT, plan->nV, plan->rec64, x, dx, alpha_seg, tseg, vseg, \
+            obj.q_base, obj.scale, X, obj.mass_coeff, obj.x_hat, obj.f_ext, obj.force_scale, et, ev)
+  switch (model) {
+    case MODEL_NH: BT_EDS(MODEL_NH); break;
+    case MODEL_STVK: BT_EDS(MODEL_STVK); break;
+    case MODEL_COROT: BT_EDS(MODEL_COROT); break;
+    case MODEL_NH_ISO: BT_EDS(MODEL_NH_ISO); break;
+    case MODEL_ARAP: BT_EDS(MODEL_ARAP); break;
+    case MODEL_LE: BT_EDS(MODEL_LE); break;
+    default: return fail(BARTELS_E_INVALID_ARG, "unknown model");
+  }
+#undef BT_EDS
+  return BARTELS_OK;
 }
 
 int gradient(bartels_ctx ctx, bartels_mesh_plan plan, int model, const ObjectiveDev &obj, const double *x,

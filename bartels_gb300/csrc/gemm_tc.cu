@@ -39,7 +39,7 @@ template <int N, int K>
 __global__ void __launch_bounds__(kGemmThreads)
 k_gemm_tc(const __grid_constant__ CUtensorMap tmap_x, const __grid_constant__ CUtensorMap tmap_w, int M,
           const float *__restrict__ bias, const float *resid, int ldr, int relu, float *__restrict__ ypre, int ldp,
-          float *y, int ldy, __nv_bfloat16 *__restrict__ y2, int ldy2, int *__restrict__ err) {
+          float *y, int ldy, __nv_bfloat16 *__restrict__ y2, int ldy2, int *__restrict__ err, int probe_polls) {
   using S = GemmSmem<N, K>;
   static_assert(N == 64 || N == 128, "N must be 64 or 128");
   static_assert(K % 64 == 0 && K <= 256, "K must be a multiple of 64");
@@ -66,7 +66,13 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmap_x, const __grid_constant__ CU
   tc::fence_after_sync();
   const uint32_t tmem = *tslot;
 
-  if (threadIdx.x == 0) {
+  if (threadIdx.x == 0 && probe_polls > 0) {
+    // failure-path probe: no copy and no MMA is issued, so nothing is in
+    // flight; the bounded wait on a barrier nothing arrives on runs out and
+    // the CTA takes the error path below (flag, no epilogue, TMEM freed)
+    tc::mbar_wait(&bars[0], 0, probe_polls);
+    s_fail = 1;
+  } else if (threadIdx.x == 0) {
     tc::mbar_expect_tx(&bars[0], S::kAtoms * (S::kABytes + S::kBBytes));
 #pragma unroll
     for (int a = 0; a < S::kAtoms; ++a) {
@@ -192,7 +198,7 @@ static int launch_gemm_t(bartels_ctx ctx, const GemmArgs &g) {
   BT_CHECK(make_map(&mw, g.w, N, K, K, N));
   const int grid = (g.M + 127) / 128;
   BT_LAUNCH(ctx, (k_gemm_tc<N, K>), grid, kGemmThreads, S::kDyn, mx, mw, g.M, g.bias, g.resid, g.ldr, g.relu, g.ypre,
-            g.ldp, g.y, g.ldy, g.y2, g.ldy2, g.err);
+            g.ldp, g.y, g.ldy, g.y2, g.ldy2, g.err, g.probe_polls);
   return BARTELS_OK;
 }
 

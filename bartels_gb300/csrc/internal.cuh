@@ -94,6 +94,28 @@ struct FactorPattern;  // lower / upper block storage maps (learned precondition
 struct LpcgPlanState;  // per-plan buffers of the learned preconditioner
 struct MgHierarchy;    // aggregation multigrid hierarchy of a plan
 
+// Packed meshes: the plan's vertices and tets as independent segments
+// (instances), each with its own PCG scalars and line-search step.
+struct SegInfo {
+  int nseg = 0;
+  int *voff = nullptr;           // nseg + 1 vertex offsets (device)
+  int64_t *toff = nullptr;       // nseg + 1 tet offsets (device)
+  int *vseg = nullptr;           // segment of each vertex (device)
+  int *tseg = nullptr;           // segment of each tet (device)
+  std::vector<int> h_voff;
+  std::vector<int64_t> h_toff;
+  std::vector<unsigned char> active;  // segments still solved (host)
+  // per-segment PCG scalars and line-search buffers (device)
+  double *rz = nullptr, *rr = nullptr, *tol2 = nullptr, *abs2 = nullptr, *red = nullptr, *red2 = nullptr;
+  float *alpha = nullptr, *beta = nullptr;
+  int *done = nullptr, *iters = nullptr;
+  double *alpha64 = nullptr;     // line-search steps
+  double *et = nullptr, *ev = nullptr;  // per-tet and per-vertex energy-difference terms
+  std::vector<int> last_iters;   // PCG iterations per segment of the last solve (host)
+  std::vector<void *> allocs;
+  ~SegInfo();
+};
+
 // Device buffer with geometric growth.
 struct DevBuf {
   void *p = nullptr;
@@ -158,7 +180,8 @@ struct bartels_mesh_plan_s {
   // Newton problem data
   double *q_base = nullptr, *x_hat = nullptr, *f_ext = nullptr;
   unsigned char *pinned = nullptr;
-  int pinned_gen = 0;  // incremented whenever the pinned set is replaced
+  int pinned_gen = 0;  // incremented whenever the pinned set changes
+  std::vector<unsigned char> h_pinned;  // host copy of the pinned set (empty: none)
   // true when dphidX is the rest shape's own (F = I + sum (u_a - u_0) phi_a^T)
   bool dphi_matches_rest = true;
   // triangular-factor pattern and learned-preconditioner buffers (built on first use)
@@ -170,6 +193,8 @@ struct bartels_mesh_plan_s {
   bartels_lpcg lpcg_net = nullptr;
   // aggregation multigrid hierarchy (built on first use for the current pinned set)
   bartels::MgHierarchy *mg = nullptr;
+  // packed-mesh segments (nullptr: one system)
+  bartels::SegInfo *seg = nullptr;
   // solver workspace
   bartels::DevBuf w_values, w_minv, w_vec, w_grad_e, w_energy, w_u, w_pcg, w_psd, w_spmv;
 };
@@ -202,6 +227,11 @@ struct ObjectiveDev {
 // returned through the pinned scalar if host_out != nullptr.
 int energy(bartels_ctx ctx, bartels_mesh_plan plan, int model, const ObjectiveDev &obj, const double *x,
            double *d_out);
+// per-tet (et, nT) and per-vertex force (ev, nV) terms of f(x + alpha_s d) - f(x)
+// with each tet / vertex taking its segment's step alpha_seg[s] (0: term 0)
+int energy_diff_seg(bartels_ctx ctx, bartels_mesh_plan plan, int model, const ObjectiveDev &obj, const double *x,
+                    const double *dx, const double *alpha_seg, const int *tseg, const int *vseg, double *et,
+                    double *ev);
 // energy of every tet (nT doubles) at positions q
 int energy_elements(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q, double *e);
 int gradient(bartels_ctx ctx, bartels_mesh_plan plan, int model, const ObjectiveDev &obj, const double *x,

@@ -28,6 +28,7 @@ struct GemmArgs {
   __nv_bfloat16 *y2 = nullptr;
   int ldy2 = 0;
   int *err = nullptr;  // device int, set non-zero when a bounded wait gave up
+  int probe_polls = 0;  // > 0: failure-path probe (no copy, no MMA; the first wait runs out)
 };
 int gemm_bf16(bartels_ctx ctx, const GemmArgs &g);
 

@@ -117,19 +117,24 @@ __device__ __forceinline__ double sum_partials(const double *a, int n) {
 // (block, component) pairs and read the three scalar rows at that column with
 // streaming loads; xval(c) supplies the vector entry at scalar column c) runs
 // only for an active group, group_reduce runs in every lane of the warp.
-template <int G, class XV>
+// ld_val: streaming load of one matrix value (FP32, or the BF16 copy the
+// multigrid V-cycle uses on its finest level).
+__device__ __forceinline__ float ld_val(const float *p) { return __ldcs(p); }
+__device__ __forceinline__ float ld_val(const __nv_bfloat16 *p) { return __bfloat162float(__ldcs(p)); }
+
+template <int G, class VT, class XV>
 __device__ __forceinline__ void spmv_row_acc(int v, int sl, const int *__restrict__ brp, const int *__restrict__ bcol,
-                                             const float *__restrict__ val, XV &&xval, float &s0, float &s1,
+                                             const VT *__restrict__ val, XV &&xval, float &s0, float &s1,
                                              float &s2) {
   const int rb = __ldg(brp + v);
   const int rs = 3 * (__ldg(brp + v + 1) - rb);
-  const float *r0 = val + 9ll * rb;
+  const VT *r0 = val + 9ll * rb;
   for (int e = sl; e < rs; e += G) {
     const int j = e / 3, l = e - 3 * j;
     const float xv = xval(3 * __ldg(bcol + rb + j) + l);
-    s0 += __ldcs(r0 + e) * xv;
-    s1 += __ldcs(r0 + rs + e) * xv;
-    s2 += __ldcs(r0 + 2 * rs + e) * xv;
+    s0 += ld_val(r0 + e) * xv;
+    s1 += ld_val(r0 + rs + e) * xv;
+    s2 += ld_val(r0 + 2 * rs + e) * xv;
   }
 }
 

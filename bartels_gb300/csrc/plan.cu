@@ -327,6 +327,8 @@ void plan_free(bartels_mesh_plan plan) {
   lpcg_plan_release(plan);
   mg_destroy(plan->mg);
   plan->mg = nullptr;
+  delete plan->seg;
+  plan->seg = nullptr;
   void *ptrs[] = {plan->X,        plan->E,      plan->dphi64,  plan->vol,     plan->params,  plan->density,
                   plan->rec32,    plan->rec64,  plan->inc_ptr, plan->inc_tet, plan->inc_pos, plan->brp,
                   plan->bcol,     plan->diag_pos, plan->chunk_v, plan->csr_rp, plan->csr_col, plan->q_base,

@@ -15,6 +15,8 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <functional>
+#include <vector>
 
 #include "devmath.cuh"
 #include "internal.cuh"
@@ -854,8 +856,8 @@ static int launch_cond(bartels_ctx ctx, cudaGraphConditionalHandle h, PcgState *
 // end with no host round trip and no iteration after convergence). Fallback:
 // a fixed run of `chunk` iterations whose kernels turn into no-ops once the
 // state is done. *launches: kernel launches per body / chunk.
-static int pcg_build_graph(bartels_ctx ctx, const PcgOperator &op, const PcgWork &w, int n, int nb, int chunk,
-                           cudaGraphExec_t *exec, int64_t *launches, bool *device_loop) {
+static int build_loop_graph(bartels_ctx ctx, PcgState *st, const std::function<int(int)> &enqueue, int chunk,
+                            cudaGraphExec_t *exec, int64_t *launches, bool *device_loop) {
   *exec = nullptr;
   *device_loop = false;
   cudaGraph_t graph = nullptr;
@@ -876,8 +878,8 @@ static int pcg_build_graph(bartels_ctx ctx, const PcgOperator &op, const PcgWork
     const int64_t before = ctx->launches;
     e = cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-      int s = pcg_enqueue_iters(ctx, op, w, n, nb, 1);
-      if (s == BARTELS_OK) s = launch_cond(ctx, h, w.st);
+      int s = enqueue(1);
+      if (s == BARTELS_OK) s = launch_cond(ctx, h, st);
       cudaGraph_t captured = nullptr;
       e = cudaStreamEndCapture(ctx->stream, &captured);
       *launches = ctx->launches - before;
@@ -898,7 +900,7 @@ static int pcg_build_graph(bartels_ctx ctx, const PcgOperator &op, const PcgWork
   cudaGraphDestroy(graph);
   const int64_t before = ctx->launches;
   BT_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-  int s = pcg_enqueue_iters(ctx, op, w, n, nb, chunk);
+  int s = enqueue(chunk);
   e = cudaStreamEndCapture(ctx->stream, &graph);
   *launches = ctx->launches - before;
   ctx->launches = before;  // counted per graph launch below
@@ -977,7 +979,9 @@ static int pcg_solve(bartels_ctx ctx, const PcgOperator &op, int n, const double
   cudaGraphExec_t exec = nullptr;
   int64_t graph_launches = 0;
   bool device_loop = false;
-  BT_CHECK(pcg_build_graph(ctx, op, w, n, nb, chunk, &exec, &graph_launches, &device_loop));
+  BT_CHECK(build_loop_graph(
+      ctx, w.st, [&](int k) { return pcg_enqueue_iters(ctx, op, w, n, nb, k); }, chunk, &exec, &graph_launches,
+      &device_loop));
   int status = BARTELS_OK;
   double rel = 0.0;
   PcgState hs{};
@@ -1058,6 +1062,365 @@ static double now_s() {
 // PCG on a plan's Hessian with the plan's preconditioner. The learned factor is
 // built from the current values; when its solve fails (not converged, not
 // finite) the system is solved again with block-Jacobi.
+// ===================================================== packed meshes ======
+// PCG with one set of scalars per segment (an instance of a packed batch):
+// alpha_s, beta_s, r.z_s, r.r_s and the convergence test per segment, from
+// deterministic per-segment sums (one CTA per segment, fixed order). The
+// preconditioners are block diagonal over the segments, so a segment's
+// iterates are those it would have alone.
+struct SegPtrs {
+  int nseg;
+  const int *voff, *vseg;
+  double *rz, *rr, *tol2, *abs2, *red;
+  float *alpha, *beta;
+  int *done, *iters;
+};
+
+enum { kSegNorm = 0, kSegInit = 1, kSegPap = 2, kSegRzRr = 3 };
+
+// Per-segment sums a.b (and c.d) and the scalars of MODE:
+//   kSegNorm: red_s = a.b;
+//   kSegInit: r.z_s = a.b, r.r_s = c.d, tol2_s, done_s (also set by the host
+//             for segments that need no iterations), beta_s = 0;
+//   kSegPap:  alpha_s = r.z_s / (p.Ap)_s with p taken by iteration parity;
+//   kSegRzRr: beta_s = r.z'_s / r.z_s, r.z_s, r.r_s, done_s, iteration count.
+// kSegInit and kSegRzRr end with the last CTA setting the global state (all
+// segments done, or the iteration cap) that the shared kernels and the loop
+// condition read.
+template <int MODE>
+__global__ void __launch_bounds__(256)
+k_seg_scalars(SegPtrs sp, const float *__restrict__ a, const float *__restrict__ b, const float *__restrict__ c,
+              const float *__restrict__ d, const float *__restrict__ pa, const float *__restrict__ pb, double inner2,
+              int max_it, PcgState *__restrict__ st) {
+  pdl_wait();
+  pdl_trigger();
+  if ((MODE == kSegPap || MODE == kSegRzRr) && st->done) return;
+  if (MODE == kSegPap) a = (st->it & 1) ? pb : pa;
+  const int s = blockIdx.x;
+  const int i0 = 3 * sp.voff[s], i1 = 3 * sp.voff[s + 1];
+  float acc1 = 0.f, acc2 = 0.f;
+  for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+    acc1 += __ldcg(a + i) * __ldcg(b + i);
+    if (c) acc2 += __ldcg(c + i) * __ldcg(d + i);
+  }
+  const double s1 = cta_sum_f(acc1);
+  const double s2 = c ? cta_sum_f(acc2) : 0.0;
+  if (threadIdx.x == 0) {
+    if (MODE == kSegNorm) {
+      sp.red[s] = s1;
+    } else if (MODE == kSegInit) {
+      const bool skip = sp.done[s] != 0;
+      sp.rz[s] = s1;
+      sp.rr[s] = s2;
+      sp.tol2[s] = fmax(inner2 * s2, sp.abs2[s]);
+      sp.alpha[s] = 0.f;
+      sp.beta[s] = 0.f;
+      sp.done[s] = (skip || s2 <= sp.tol2[s] || !(s2 == s2)) ? 1 : 0;
+    } else if (MODE == kSegPap) {
+      sp.alpha[s] = sp.done[s] ? 0.f : (float)(sp.rz[s] / s1);
+    } else {
+      if (!sp.done[s]) {
+        sp.beta[s] = (float)(s1 / sp.rz[s]);
+        sp.rz[s] = s1;
+        sp.rr[s] = s2;
+        sp.iters[s] += 1;
+        if (s2 <= sp.tol2[s] || !(s2 == s2)) sp.done[s] = 1;
+      } else {
+        sp.beta[s] = 0.f;
+      }
+    }
+  }
+  if (MODE == kSegInit || MODE == kSegRzRr) {
+    if (last_block(&st->count)) {
+      int all = 1;
+      for (int q = threadIdx.x; q < sp.nseg; q += blockDim.x)
+        if (!__ldcg(sp.done + q)) all = 0;
+      all = __syncthreads_and(all);
+      if (threadIdx.x == 0) {
+        if (MODE == kSegInit) {
+          st->it = 0;
+          st->max_it = max_it;
+          st->loops = 0;
+          st->done = (all || max_it <= 0) ? 1 : 0;
+        } else {
+          st->it += 1;
+          st->done = (all || st->it >= st->max_it) ? 1 : 0;
+        }
+        st->count = 0;
+      }
+    }
+  }
+}
+
+// start of a pass: x = 0, r = rres (0 in segments that take no iterations),
+// z = M^-1 r with block-Jacobi (multigrid computes z afterwards), p = 0; the
+// global state reopened for the kernels that follow
+__global__ void __launch_bounds__(256)
+k_seg_init(int nV, const int *__restrict__ vseg, const int *__restrict__ done, const float *__restrict__ rres,
+           const float *__restrict__ minv, float *__restrict__ x, float *__restrict__ r, float *__restrict__ z,
+           float *__restrict__ p0, float *__restrict__ p1, PcgState *__restrict__ st) {
+  pdl_wait();
+  pdl_trigger();
+  if (blockIdx.x == 0 && threadIdx.x == 0) st->done = 0;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nV; v += gridDim.x * blockDim.x) {
+    const bool skip = done[vseg[v]] != 0;
+    float rv[3], zv[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      rv[k] = skip ? 0.f : rres[3 * v + k];
+      x[3 * v + k] = 0.f;
+      r[3 * v + k] = rv[k];
+      p0[3 * v + k] = 0.f;
+      p1[3 * v + k] = 0.f;
+    }
+    if (minv) {
+      apply_minv(minv, v, rv, zv);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) z[3 * v + k] = zv[k];
+    }
+  }
+}
+
+// x += alpha_s p; r -= alpha_s Ap; z = M^-1 r with block-Jacobi (minv), per vertex with its segment's step
+__global__ void __launch_bounds__(256)
+k_seg_update(int nV, const int *__restrict__ vseg, const float *__restrict__ alpha, const float *__restrict__ pa,
+             const float *__restrict__ pb, const float *__restrict__ ap, float *__restrict__ x, float *__restrict__ r,
+             float *__restrict__ z, const float *__restrict__ minv, const PcgState *__restrict__ st) {
+  pdl_wait();
+  pdl_trigger();
+  if (st->done) return;
+  const float *p = (st->it & 1) ? pb : pa;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nV; v += gridDim.x * blockDim.x) {
+    const float al = alpha[vseg[v]];
+    float rv[3], zv[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int i = 3 * v + k;
+      x[i] += al * __ldcg(p + i);
+      rv[k] = r[i] - al * __ldcg(ap + i);
+      r[i] = rv[k];
+    }
+    if (minv) {
+      apply_minv(minv, v, rv, zv);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) z[3 * v + k] = zv[k];
+    }
+  }
+}
+
+// p = z + beta_s p_old (double-buffered by iteration parity, as k_pcg_dir)
+__global__ void __launch_bounds__(256)
+k_seg_dir(int nV, const int *__restrict__ vseg, const float *__restrict__ beta, const float *__restrict__ z,
+          float *__restrict__ pa, float *__restrict__ pb, const PcgState *__restrict__ st) {
+  pdl_wait();
+  pdl_trigger();
+  if (st->done) return;
+  const int it = st->it;
+  const float *p_old = (it & 1) ? pa : pb;
+  float *p_new = (it & 1) ? pb : pa;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nV; v += gridDim.x * blockDim.x) {
+    const float bt = beta[vseg[v]];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) p_new[3 * v + k] = __ldcg(z + 3 * v + k) + bt * __ldcg(p_old + 3 * v + k);
+  }
+}
+
+// per-segment FP64 sums a.b (or of a alone when b is NULL) over the entries
+// [mult voff[s], mult voff[s + 1]) (vertex offsets: mult = 3 for DOF vectors,
+// 1 for per-vertex values) or [eoff[s], eoff[s + 1]) (tet offsets)
+__global__ void __launch_bounds__(256)
+k_seg_dot64(const int *__restrict__ voff, int mult, const int64_t *__restrict__ eoff, const double *__restrict__ a,
+            const double *__restrict__ b, double *__restrict__ out) {
+  const int s = blockIdx.x;
+  const int64_t i0 = eoff ? eoff[s] : (int64_t)mult * voff[s], i1 = eoff ? eoff[s + 1] : (int64_t)mult * voff[s + 1];
+  double acc = 0.0;
+  for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) acc += b ? a[i] * b[i] : a[i];
+  const double t = cta_sum(acc);
+  if (threadIdx.x == 0) out[s] = t;
+}
+
+// x += alpha_s d per vertex (FP64)
+__global__ void k_seg_axpy(int nV, const int *__restrict__ vseg, const double *__restrict__ alpha,
+                           const double *__restrict__ d, double *__restrict__ x) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < nV; v += gridDim.x * blockDim.x) {
+    const double al = alpha[vseg[v]];
+    for (int k = 0; k < 3; ++k) x[3 * v + k] += al * d[3 * v + k];
+  }
+}
+
+static SegPtrs seg_ptrs(const SegInfo *sg) {
+  SegPtrs sp;
+  sp.nseg = sg->nseg;
+  sp.voff = sg->voff;
+  sp.vseg = sg->vseg;
+  sp.rz = sg->rz;
+  sp.rr = sg->rr;
+  sp.tol2 = sg->tol2;
+  sp.abs2 = sg->abs2;
+  sp.red = sg->red;
+  sp.alpha = sg->alpha;
+  sp.beta = sg->beta;
+  sp.done = sg->done;
+  sp.iters = sg->iters;
+  return sp;
+}
+
+// One PCG iteration of the segmented solve (or `iters` of them).
+static int seg_enqueue_iters(bartels_ctx ctx, const PcgOperator &op, const PcgWork &w, const SegPtrs &sp, int iters) {
+  const bartels_mesh_plan plan = op.plan;
+  const int nV = plan->nV;
+  const int lanes = lanes_spmv(ctx, plan);
+  const int gs = grid_spmv(ctx, (int64_t)nV * lanes / 32 + 1);
+  const int gv = grid_vec(ctx, nV);
+  for (int i = 0; i < iters; ++i) {
+    BT_CHECK(pcg_spmv_blk(ctx, op, w, lanes, gs));
+    BT_LAUNCH_PDL(ctx, k_seg_scalars<kSegPap>, sp.nseg, 256, 0, sp, (const float *)nullptr, w.ap,
+                  (const float *)nullptr, (const float *)nullptr, w.pa, w.pb, 0.0, 0, w.st);
+    BT_LAUNCH_PDL(ctx, k_seg_update, gv, 256, 0, nV, sp.vseg, sp.alpha, w.pa, w.pb, w.ap, w.x, w.r, w.z,
+                  op.mg ? (const float *)nullptr : w.minv, w.st);
+    if (op.mg) BT_CHECK(mg_enqueue_apply(ctx, plan, op.values, op.sm, w.r, w.z, w.ap, w.part_b, w.st, false));
+    BT_LAUNCH_PDL(ctx, k_seg_scalars<kSegRzRr>, sp.nseg, 256, 0, sp, w.r, w.z, w.r, w.r, (const float *)nullptr,
+                  (const float *)nullptr, 0.0, 0, w.st);
+    BT_LAUNCH_PDL(ctx, k_seg_dir, gv, 256, 0, nV, sp.vseg, sp.beta, w.z, w.pa, w.pb, w.st);
+  }
+  return BARTELS_OK;
+}
+
+// A full solve of A x = b over the plan's segments (FP64 in / out, device),
+// FP64 residual refinement per segment: each pass computes b - A x (float-
+// float), and the segments whose residual is still above rel_tol of their own
+// |b_s| (and that are active) take a restarted inner FP32 PCG to inner_rel_tol.
+static int seg_pcg_solve(bartels_ctx ctx, const PcgOperator &op, const double *b, double *x, DevBuf &wbuf,
+                         const bartels_pcg_params &prm, bartels_pcg_report *rep) {
+  const bartels_mesh_plan plan = op.plan;
+  SegInfo *sg = plan->seg;
+  const int nseg = sg->nseg, nV = plan->nV, n = 3 * nV;
+  const int gs = grid_spmv(ctx, nV);
+  const int gv = grid_vec(ctx, nV);
+  const int nparts = std::max(std::max(gs, gv), 1024);
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    size_t o = off;
+    off += (bytes + 255) & ~size_t(255);
+    return o;
+  };
+  const size_t o_x = take(4ull * n), o_r = take(4ull * n), o_z = take(4ull * n), o_pa = take(4ull * n),
+               o_pb = take(4ull * n), o_ap = take(4ull * n), o_minv = take(24ull * nV), o_rres = take(4ull * n),
+               o_xh = take(4ull * n), o_xl = take(4ull * n), o_bh = take(4ull * n), o_bl = take(4ull * n),
+               o_pa8 = take(8ull * nparts), o_pb8 = take(8ull * nparts), o_st = take(sizeof(PcgState));
+  BT_CHECK(wbuf.ensure(off));
+  char *base = wbuf.as<char>();
+  PcgWork w;
+  w.x = (float *)(base + o_x);
+  w.r = (float *)(base + o_r);
+  w.z = (float *)(base + o_z);
+  w.pa = (float *)(base + o_pa);
+  w.pb = (float *)(base + o_pb);
+  w.ap = (float *)(base + o_ap);
+  w.minv = (float *)(base + o_minv);
+  w.rres = (float *)(base + o_rres);
+  w.bh = (float *)(base + o_bh);
+  w.bl = (float *)(base + o_bl);
+  w.xh = (float *)(base + o_xh);
+  w.xl = (float *)(base + o_xl);
+  w.part_a = (double *)(base + o_pa8);
+  w.part_b = (double *)(base + o_pb8);
+  w.st = (PcgState *)(base + o_st);
+  BT_CUDA(cudaMemsetAsync(w.st, 0, sizeof(PcgState), ctx->stream));
+  BT_CUDA(cudaMemsetAsync(sg->iters, 0, sizeof(int) * nseg, ctx->stream));
+  if (!op.mg) BT_LAUNCH(ctx, k_minv_blk, grid_vec(ctx, nV), 256, 0, nV, plan->brp, plan->diag_pos, op.values,
+                        op.pinned, w.minv);
+  const SegPtrs sp = seg_ptrs(sg);
+  // |b_s|
+  BT_LAUNCH(ctx, k_seg_dot64, nseg, 256, 0, sg->voff, 3, (const int64_t *)nullptr, b, b, sg->red2);
+  std::vector<double> bn(nseg), rr(nseg), abs2(nseg);
+  std::vector<int> skip(nseg);
+  BT_CUDA(cudaMemcpyAsync(bn.data(), sg->red2, sizeof(double) * nseg, cudaMemcpyDeviceToHost, ctx->stream));
+  BT_CUDA(cudaStreamSynchronize(ctx->stream));
+  for (int q = 0; q < nseg; ++q) {
+    bn[q] = std::sqrt(bn[q]);
+    abs2[q] = (0.5 * prm.rel_tol * bn[q]) * (0.5 * prm.rel_tol * bn[q]);
+  }
+  BT_CUDA(cudaMemcpyAsync(sg->abs2, abs2.data(), sizeof(double) * nseg, cudaMemcpyHostToDevice, ctx->stream));
+  cudaGraphExec_t exec = nullptr;
+  int64_t graph_launches = 0;
+  bool device_loop = false;
+  BT_CHECK(build_loop_graph(
+      ctx, w.st, [&](int k) { return seg_enqueue_iters(ctx, op, w, sp, k); }, 8, &exec, &graph_launches,
+      &device_loop));
+  rep->iterations = 0;
+  rep->refinements = 0;
+  rep->converged = 0;
+  rep->rel_residual = 0.0;
+  int status = BARTELS_OK;
+  PcgState hs{};
+  const int lanes_r = 16;
+  for (int pass = 0; pass <= prm.max_refinements; ++pass) {
+    if (pass == 0) {
+      BT_LAUNCH(ctx, k_axpy64, grid_vec(ctx, n), 256, 0, n, nullptr, x, w.xh, w.xl);
+      BT_LAUNCH(ctx, k_split64, grid_vec(ctx, n), 256, 0, n, b, w.bh, w.bl);
+    }
+    BT_LAUNCH(ctx, k_resid_blk_ff<lanes_r>, gs, 256, 0, nV, plan->brp, plan->bcol, op.values, w.xh, w.xl, w.bh,
+              w.bl, w.rres, op.pinned, w.part_a);
+    BT_LAUNCH(ctx, k_seg_scalars<kSegNorm>, nseg, 256, 0, sp, w.rres, w.rres, (const float *)nullptr,
+              (const float *)nullptr, (const float *)nullptr, (const float *)nullptr, 0.0, 0, w.st);
+    BT_CUDA(cudaMemcpyAsync(rr.data(), sg->red, sizeof(double) * nseg, cudaMemcpyDeviceToHost, ctx->stream));
+    BT_CUDA(cudaStreamSynchronize(ctx->stream));
+    double rel = 0.0;
+    int work = 0;
+    bool finite = true;
+    for (int q = 0; q < nseg; ++q) {
+      const double r = std::sqrt(rr[q]);
+      if (!std::isfinite(r)) finite = false;
+      const double rq = bn[q] > 0.0 ? r / bn[q] : 0.0;
+      const bool need = sg->active[q] && bn[q] > 0.0 && r > prm.rel_tol * bn[q];
+      skip[q] = need ? 0 : 1;
+      work += need;
+      if (sg->active[q]) rel = std::max(rel, rq);
+    }
+    rep->rel_residual = rel;
+    if (!finite) {
+      status = fail(BARTELS_E_NONFINITE, "PCG residual is not finite");
+      break;
+    }
+    if (work == 0) {
+      rep->converged = 1;
+      break;
+    }
+    if (pass == prm.max_refinements || rep->iterations >= prm.max_iters) {
+      status = fail(BARTELS_E_NOT_CONVERGED, "PCG did not reach the residual target");
+      break;
+    }
+    rep->refinements = pass + 1;
+    BT_CUDA(cudaMemcpyAsync(sg->done, skip.data(), sizeof(int) * nseg, cudaMemcpyHostToDevice, ctx->stream));
+    BT_LAUNCH_PDL(ctx, k_seg_init, gv, 256, 0, nV, sg->vseg, sg->done, w.rres, op.mg ? (const float *)nullptr : w.minv,
+                  w.x, w.r, w.z, w.pa, w.pb, w.st);
+    if (op.mg) BT_CHECK(mg_enqueue_apply(ctx, plan, op.values, op.sm, w.r, w.z, w.ap, w.part_b, w.st, false));
+    BT_LAUNCH_PDL(ctx, k_seg_scalars<kSegInit>, nseg, 256, 0, sp, w.r, w.z, w.r, w.r, (const float *)nullptr,
+                  (const float *)nullptr, prm.inner_rel_tol * prm.inner_rel_tol, prm.max_iters - rep->iterations,
+                  w.st);
+    BT_LAUNCH_PDL(ctx, k_seg_dir, gv, 256, 0, nV, sg->vseg, sg->beta, w.z, w.pa, w.pb, w.st);
+    for (;;) {
+      BT_CUDA(cudaGraphLaunch(exec, ctx->stream));
+      BT_CUDA(cudaMemcpyAsync(&hs, w.st, sizeof(PcgState), cudaMemcpyDeviceToHost, ctx->stream));
+      BT_CUDA(cudaStreamSynchronize(ctx->stream));
+      if (device_loop) {
+        ctx->launches += graph_launches * (int64_t)std::max(1u, hs.loops);
+        break;
+      }
+      ctx->launches += graph_launches;
+      if (hs.done) break;
+    }
+    rep->iterations += hs.it;
+    BT_LAUNCH(ctx, k_axpy64, grid_vec(ctx, n), 256, 0, n, w.x, x, w.xh, w.xl);
+  }
+  cudaGraphExecDestroy(exec);
+  sg->last_iters.resize(nseg);
+  BT_CUDA(cudaMemcpyAsync(sg->last_iters.data(), sg->iters, sizeof(int) * nseg, cudaMemcpyDeviceToHost, ctx->stream));
+  BT_CUDA(cudaStreamSynchronize(ctx->stream));
+  return status;
+}
+
 // Multigrid hierarchy values for a Hessian: the level-0 smoother (block-Jacobi
 // inverse blocks, or the network's factor), Galerkin products, bounds.
 static int mg_values(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, bool learned, MgSmoother &sm) {
@@ -1086,6 +1449,81 @@ int plan_precond_apply(bartels_ctx ctx, bartels_mesh_plan plan, const float *val
   return BARTELS_OK;
 }
 
+SegInfo::~SegInfo() {
+  for (void *q : allocs) cudaFree(q);
+}
+
+// Segments of a packed plan: offsets checked (monotone, covering the mesh,
+// every tet inside its segment), per-vertex and per-tet segment maps and the
+// per-segment scalar buffers.
+int plan_set_segments(bartels_mesh_plan plan, int nseg, const int *voff, const int64_t *toff) {
+  bartels_ctx ctx = plan->ctx;
+  delete plan->seg;
+  plan->seg = nullptr;
+  if (nseg == 0) return BARTELS_OK;
+  if (nseg < 0 || !voff || !toff) return fail(BARTELS_E_INVALID_ARG, "bad segment arguments");
+  if (voff[0] != 0 || voff[nseg] != plan->nV || toff[0] != 0 || toff[nseg] != plan->nT)
+    return fail(BARTELS_E_INVALID_ARG, "segment offsets must start at 0 and end at the vertex / tet counts");
+  for (int q = 0; q < nseg; ++q)
+    if (voff[q + 1] < voff[q] || toff[q + 1] < toff[q])
+      return fail(BARTELS_E_INVALID_ARG, "segment offsets must not decrease");
+  std::vector<int4> E(plan->nT);
+  BT_CUDA(cudaMemcpy(E.data(), plan->E, sizeof(int4) * E.size(), cudaMemcpyDeviceToHost));
+  std::vector<int> vseg(plan->nV), tseg(plan->nT);
+  for (int q = 0; q < nseg; ++q) {
+    for (int v = voff[q]; v < voff[q + 1]; ++v) vseg[v] = q;
+    for (int64_t t = toff[q]; t < toff[q + 1]; ++t) {
+      tseg[t] = q;
+      const int id[4] = {E[t].x, E[t].y, E[t].z, E[t].w};
+      for (int a = 0; a < 4; ++a)
+        if (id[a] < voff[q] || id[a] >= voff[q + 1])
+          return fail(BARTELS_E_INVALID_ARG, "tet " + std::to_string(t) + " has a vertex outside its segment");
+    }
+  }
+  auto *sg = new SegInfo();
+  plan->seg = sg;
+  sg->nseg = nseg;
+  sg->h_voff.assign(voff, voff + nseg + 1);
+  sg->h_toff.assign(toff, toff + nseg + 1);
+  sg->active.assign(nseg, 1);
+  auto alloc = [&](void **dst, size_t bytes) -> int {
+    BT_CUDA(cudaMalloc(dst, std::max<size_t>(bytes, 16)));
+    sg->allocs.push_back(*dst);
+    return BARTELS_OK;
+  };
+  BT_CHECK(alloc((void **)&sg->voff, sizeof(int) * (nseg + 1)));
+  BT_CHECK(alloc((void **)&sg->toff, sizeof(int64_t) * (nseg + 1)));
+  BT_CHECK(alloc((void **)&sg->vseg, sizeof(int) * plan->nV));
+  BT_CHECK(alloc((void **)&sg->tseg, sizeof(int) * plan->nT));
+  for (double **d : {&sg->rz, &sg->rr, &sg->tol2, &sg->abs2, &sg->red, &sg->red2, &sg->alpha64})
+    BT_CHECK(alloc((void **)d, sizeof(double) * nseg));
+  BT_CHECK(alloc((void **)&sg->alpha, sizeof(float) * nseg));
+  BT_CHECK(alloc((void **)&sg->beta, sizeof(float) * nseg));
+  BT_CHECK(alloc((void **)&sg->done, sizeof(int) * nseg));
+  BT_CHECK(alloc((void **)&sg->iters, sizeof(int) * nseg));
+  BT_CHECK(alloc((void **)&sg->et, sizeof(double) * plan->nT));
+  BT_CHECK(alloc((void **)&sg->ev, sizeof(double) * plan->nV));
+  BT_CUDA(cudaMemcpy(sg->voff, voff, sizeof(int) * (nseg + 1), cudaMemcpyHostToDevice));
+  BT_CUDA(cudaMemcpy(sg->toff, toff, sizeof(int64_t) * (nseg + 1), cudaMemcpyHostToDevice));
+  BT_CUDA(cudaMemcpy(sg->vseg, vseg.data(), sizeof(int) * plan->nV, cudaMemcpyHostToDevice));
+  BT_CUDA(cudaMemcpy(sg->tseg, tseg.data(), sizeof(int) * plan->nT, cudaMemcpyHostToDevice));
+  (void)ctx;
+  return BARTELS_OK;
+}
+
+// The plan's solve: per-segment scalars for packed meshes (block-Jacobi or a
+// multigrid V-cycle; the single-level factor preconditioner runs as block-
+// Jacobi there), one system otherwise.
+static int solve_any(bartels_ctx ctx, PcgOperator op, int n, const double *b, double *x, DevBuf &wbuf,
+                     const bartels_pcg_params &prm, bartels_pcg_report *rep) {
+  if (op.plan && op.plan->seg && op.plan->seg->nseg > 0) {
+    op.gl = op.gu = nullptr;
+    op.fp = nullptr;
+    return seg_pcg_solve(ctx, op, b, x, wbuf, prm, rep);
+  }
+  return pcg_solve(ctx, op, n, b, x, wbuf, prm, rep);
+}
+
 static int plan_pcg_impl(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const double *b, double *x,
                          const bartels_pcg_params &prm, bartels_pcg_report *rep, int *fallback, double *t_factor) {
   const int n = 3 * plan->nV;
@@ -1106,7 +1544,7 @@ static int plan_pcg_impl(bartels_ctx ctx, bartels_mesh_plan plan, const float *v
       if (t_factor) *t_factor += now_s() - t0;
       op.mg = true;
       op.sm = sm;
-      s = pcg_solve(ctx, op, n, b, x, plan->w_pcg, prm, rep);
+      s = solve_any(ctx, op, n, b, x, plan->w_pcg, prm, rep);
       if (s == BARTELS_OK && rep->converged) return BARTELS_OK;
       if (s != BARTELS_OK && s != BARTELS_E_NOT_CONVERGED && s != BARTELS_E_NONFINITE) return s;
       // not converged or not finite: solve again with block-Jacobi
@@ -1115,7 +1553,7 @@ static int plan_pcg_impl(bartels_ctx ctx, bartels_mesh_plan plan, const float *v
       op.mg = false;
       op.sm = MgSmoother();
       BT_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, ctx->stream));
-      s = pcg_solve(ctx, op, n, b, x, plan->w_pcg, prm, rep);
+      s = solve_any(ctx, op, n, b, x, plan->w_pcg, prm, rep);
       rep->iterations += used;
       return s;
     }
@@ -1131,7 +1569,7 @@ static int plan_pcg_impl(bartels_ctx ctx, bartels_mesh_plan plan, const float *v
     op.gl = gl;
     op.gu = gu;
     op.fp = plan->factor;
-    int s = pcg_solve(ctx, op, n, b, x, plan->w_pcg, prm, rep);
+    int s = solve_any(ctx, op, n, b, x, plan->w_pcg, prm, rep);
     if (s == BARTELS_OK && rep->converged) return BARTELS_OK;
     if (s != BARTELS_OK && s != BARTELS_E_NOT_CONVERGED && s != BARTELS_E_NONFINITE) return s;
     if (fallback) *fallback = 1;
@@ -1139,11 +1577,11 @@ static int plan_pcg_impl(bartels_ctx ctx, bartels_mesh_plan plan, const float *v
     op.gl = op.gu = nullptr;
     op.fp = nullptr;
     BT_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, ctx->stream));
-    s = pcg_solve(ctx, op, n, b, x, plan->w_pcg, prm, rep);
+    s = solve_any(ctx, op, n, b, x, plan->w_pcg, prm, rep);
     rep->iterations += used;
     return s;
   }
-  return pcg_solve(ctx, op, n, b, x, plan->w_pcg, prm, rep);
+  return solve_any(ctx, op, n, b, x, plan->w_pcg, prm, rep);
 }
 
 int plan_pcg(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const double *b, double *x,
@@ -1208,6 +1646,68 @@ struct NvtxStage {
   }
 };
 
+// The reference's line search (src/linesearch_backtracking_bisection.cpp:17-30)
+// for every segment of a packed plan at once, each with its own step: segment
+// s accepts alpha_s when f_s(x + alpha_s d) - f_s(x) <= c g_s.d_s, else halves
+// it (up to max_iterations_ls times); inactive segments take no step.
+static int seg_linesearch(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params &p,
+                          const ObjectiveDev &obj, double *x, const NewtonWork &w, bartels_newton_report *rep) {
+  SegInfo *sg = plan->seg;
+  const int nseg = sg->nseg;
+  BT_LAUNCH(ctx, k_seg_dot64, nseg, 256, 0, sg->voff, 3, (const int64_t *)nullptr, w.g, w.d, sg->red2);
+  std::vector<double> gd(nseg), alpha(nseg), trial(nseg), det(nseg), dev(nseg);
+  std::vector<int> searching(nseg), back(nseg, 0);
+  BT_CUDA(cudaMemcpyAsync(gd.data(), sg->red2, sizeof(double) * nseg, cudaMemcpyDeviceToHost, ctx->stream));
+  BT_CUDA(cudaStreamSynchronize(ctx->stream));
+  for (int q = 0; q < nseg; ++q) {
+    searching[q] = sg->active[q] ? 1 : 0;
+    alpha[q] = sg->active[q] ? p.ls_alpha : 0.0;
+  }
+  double df_total = 0.0;
+  for (int it = 0;; ++it) {
+    int any = 0;
+    for (int q = 0; q < nseg; ++q) {
+      trial[q] = searching[q] ? alpha[q] : 0.0;
+      any += searching[q];
+    }
+    if (!any) break;
+    BT_CUDA(cudaMemcpyAsync(sg->alpha64, trial.data(), sizeof(double) * nseg, cudaMemcpyHostToDevice, ctx->stream));
+    BT_CHECK(energy_diff_seg(ctx, plan, p.model, obj, x, w.d, sg->alpha64, sg->tseg, sg->vseg, sg->et, sg->ev));
+    BT_LAUNCH(ctx, k_seg_dot64, nseg, 256, 0, (const int *)nullptr, 0, sg->toff, sg->et, (const double *)nullptr,
+              sg->red);
+    BT_LAUNCH(ctx, k_seg_dot64, nseg, 256, 0, sg->voff, 1, (const int64_t *)nullptr, sg->ev, (const double *)nullptr,
+              sg->red2);
+    BT_CUDA(cudaMemcpyAsync(det.data(), sg->red, sizeof(double) * nseg, cudaMemcpyDeviceToHost, ctx->stream));
+    BT_CUDA(cudaMemcpyAsync(dev.data(), sg->red2, sizeof(double) * nseg, cudaMemcpyDeviceToHost, ctx->stream));
+    BT_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (int q = 0; q < nseg; ++q) {
+      if (!searching[q]) continue;
+      const double df = det[q] + dev[q];
+      const bool reject = !std::isfinite(df) || df > p.ls_c * gd[q];
+      if (reject && it < p.max_iterations_ls) {
+        alpha[q] *= p.ls_p;
+        back[q]++;
+      } else {
+        searching[q] = 0;
+        if (reject) rep->ls_failures++;
+        else df_total += df;
+      }
+    }
+  }
+  BT_CUDA(cudaMemcpyAsync(sg->alpha64, alpha.data(), sizeof(double) * nseg, cudaMemcpyHostToDevice, ctx->stream));
+  BT_LAUNCH(ctx, k_seg_axpy, grid_vec(ctx, plan->nV), 256, 0, plan->nV, sg->vseg, sg->alpha64, w.d, x);
+  int most = 0;
+  double amin = HUGE_VAL;
+  for (int q = 0; q < nseg; ++q) {
+    most = std::max(most, back[q]);
+    if (sg->active[q]) amin = std::min(amin, alpha[q]);
+  }
+  rep->ls_iterations += most;
+  rep->last_alpha = amin < HUGE_VAL ? amin : 0.0;
+  rep->energy_change = df_total;
+  return BARTELS_OK;
+}
+
 int newton_iterate(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params &p, double *x,
                    double g0_norm, int *done, bartels_newton_report *rep) {
   NvtxStage stage;
@@ -1262,6 +1762,13 @@ int newton_iterate(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton
   // f(x + alpha d) > f(x) + c g.d and it < max: alpha *= p. The difference
   // f(x + alpha d) - f(x) is evaluated element by element (energy_diff) so that
   // it stays accurate when it is many orders below |f| near the minimum.
+  if (plan->seg && plan->seg->nseg > 0) {
+    BT_CHECK(seg_linesearch(ctx, plan, p, obj, x, w, rep));
+    BT_CUDA(cudaStreamSynchronize(ctx->stream));
+    rep->t_linesearch += now_s() - t3;
+    rep->iterations += 1;
+    return BARTELS_OK;
+  }
   double gd;
   BT_CHECK(dot(ctx, w.g, w.d, n, w.scal));
   BT_CHECK(read_scalar(ctx, w.scal, &gd));

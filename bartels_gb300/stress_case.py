@@ -11,8 +11,8 @@ load steps (each starts from the previous solution compressed affinely in z),
 quasi-static Newton per step to 1e-5 relative gradient norm (projected Newton
 converges only linearly here: the PSD projection is active at the compressed
 equilibrium, so the tolerance and a 40-iteration cap are set for that). Each Newton system is solved by PCG to 1e-8
-relative residual with block-Jacobi and with the learned factor (block-Jacobi
-as fallback). Reported: Newton and PCG iteration counts, fallbacks, time, and
+relative residual with block-Jacobi, the learned factor, the multigrid V-cycle
+and the V-cycle with the learned smoother (block-Jacobi as fallback). Reported: Newton and PCG iteration counts, fallbacks, time, and
 the energy of the final state (tests/test_gpu_stress.py checks the final
 state against the FP64 CPU restatement). Synthetic, seeded inputs.
 """
@@ -58,9 +58,15 @@ def run(prob, precond, net=None, steps=10, compression=0.5, gradient_tol=1e-5, m
     pinned = (prob["bottom"] | prob["top"]).astype(np.uint8)
     if precond == "learned":
         net.attach(plan)
+    elif precond == "learned_multigrid":
+        net.attach(plan, multigrid=True)
+    elif precond == "multigrid":
+        _lib.check(L.bartels_plan_set_preconditioner(plan.handle, _lib.PRECOND_MULTIGRID, None), "precond")
     prm = bg.newton_params(model="neohookean", psd_mode=_lib.PSD_SIMPLE_FIX, psd_tol=1e-6, mass_coeff=0.0, scale=1.0,
                            force_scale=0.0, gradient_tol=gradient_tol, relative=1, max_iterations=max_newton)
     prm.pcg.max_iters = 60000
+    if precond in ("multigrid", "learned_multigrid"):
+        prm.pcg.inner_rel_tol = 1e-2
     zmin, zmax = V[:, 2].min(), V[:, 2].max()
     q = V.copy()
     x = torch.zeros(3 * len(V), dtype=torch.float64, device="cuda")
@@ -107,6 +113,8 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--weights", default=None)
     ap.add_argument("--gradient-tol", type=float, default=1e-5)
+    ap.add_argument("--preconds", default="jacobi,learned,multigrid,learned_multigrid",
+                    help="comma-separated preconditioners to compare")
     args = ap.parse_args(argv)
     import bartels_gb300 as bg
     from bartels_gb300 import lpcg
@@ -117,12 +125,14 @@ def main(argv=None):
                           top=int(prob["top"].sum()), build_s=round(time.time() - t, 1))), flush=True)
     net = lpcg.LearnedPreconditioner.load(args.weights or lpcg.WEIGHTS, bg.Context.default())
     out = {}
-    for pc in ("jacobi", "learned"):
+    for pc in args.preconds.split(","):
         _, tot, _ = run(prob, pc, net, steps=args.steps, gradient_tol=args.gradient_tol,
                         log=lambda s: print(s, flush=True))
         out[pc] = tot
         print(json.dumps(dict(summary=pc, **tot)), flush=True)
-    out["learned_over_jacobi_seconds"] = out["jacobi"]["seconds"] / out["learned"]["seconds"]
+    for pc in out.copy():
+        if pc != "jacobi" and "jacobi" in out:
+            out[f"{pc}_over_jacobi_seconds"] = out["jacobi"]["seconds"] / out[pc]["seconds"]
     print(json.dumps(out), flush=True)
     return out
 

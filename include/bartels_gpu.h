@@ -463,11 +463,40 @@ int bartels_plan_autotune(bartels_ctx ctx, bartels_mesh_plan plan, const float *
  * vertex_offsets_d[s+1]-1 (device arrays, nseg + 1 offsets). */
 int bartels_segment_sumsq_d(bartels_ctx ctx, int nseg, const int *vertex_offsets_d, const double *v_d,
                             double *out_d);
+/* Declare the plan's mesh as nseg independent packed meshes (segments):
+ * vertex_offsets (nseg + 1) and tet_offsets (nseg + 1), host arrays, every
+ * tet's vertices inside its own segment's range. The plan's PCG solves then
+ * keep separate scalars per segment (alpha, beta, r.z, convergence against
+ * the segment's own residual target), and the Newton line search backtracks
+ * each segment on its own energy difference with its own step, so that each
+ * packed mesh follows the iterates it would follow alone (the reference runs
+ * one newtons_method_bisection per problem,
+ * include/optimization_gradient_based.h:77-106, each with its own
+ * linesearch_backtracking_bisection, src/linesearch_backtracking_bisection.cpp:17-30).
+ * The preconditioners (block-Jacobi, multigrid) are block diagonal over the
+ * segments already. nseg = 0 returns to one system. Every segment starts
+ * active. */
+int bartels_plan_set_segments(bartels_mesh_plan plan, int nseg, const int *vertex_offsets,
+                              const int64_t *tet_offsets);
+/* Segments with active[s] = 0 (host, nseg bytes) take no Newton step and no
+ * PCG iteration (their search direction is 0), e.g. instances that have met
+ * their convergence test. */
+int bartels_plan_set_segment_active(bartels_mesh_plan plan, const unsigned char *active);
+/* PCG iterations each segment took in the plan's last solve (host, nseg). */
+int bartels_plan_segment_pcg_iterations(bartels_mesh_plan plan, int *iterations);
 /* Building block: Y = act(X W^T + bias) on the tensor cores (tcgen05, TMA);
  * X: M x K BF16 (row stride ldx elements), W: N x K BF16, bias: N FP32 or NULL,
  * Y: M x N FP32 (row stride ldy); N, K in {64, 128}; device pointers. */
 int bartels_gemm_bf16_d(bartels_ctx ctx, int M, int N, int K, const void *x_d, int ldx, const void *w_d,
                         const float *bias_d, int relu, float *y_d, int ldy);
+/* Failure-path probe of the same tensor-core GEMM (for tests): every CTA
+ * issues no copy and no MMA and polls its first mbarrier, which nothing
+ * arrives on, `polls` times; the bounded wait runs out and the kernel takes
+ * its time-out path (error flag set, no output written, tensor memory freed),
+ * which this call reports as BARTELS_E_TIMEOUT like a real time-out. Nothing
+ * is in flight when the wait gives up. No counterpart in the reference. */
+int bartels_gemm_bf16_wait_probe_d(bartels_ctx ctx, int M, int N, int K, const void *x_d, int ldx,
+                                   const void *w_d, float *y_d, int ldy, int polls);
 
 /* ------------------------------------------------- device-pointer variants -- */
 /* Hessian H = coeff_M M + coeff_K K(q) of the plan's element data into FP32

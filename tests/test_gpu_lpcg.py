@@ -50,6 +50,30 @@ def test_tcgen05_gemm_strided_input():
     assert np.abs(y.cpu().numpy() - ref).max() <= 1e-4 * np.abs(ref).max()
 
 
+def test_tcgen05_gemm_wait_timeout_is_reported_and_the_context_stays_usable():
+    """The GEMM's bounded mbarrier wait running out: the probe issues no copy
+    and no MMA, so nothing is in flight while its first wait polls a barrier
+    that nothing arrives on. The C ABI must report BARTELS_E_TIMEOUT, and a
+    normal GEMM right after must still be exact."""
+    torch = _torch()
+    import bartels_gb300 as bg
+    from bartels_gb300 import _lib, lpcg
+    ctx = bg.Context.default()
+    g = torch.Generator().manual_seed(9)
+    x = torch.randn(300, 64, generator=g).to(torch.bfloat16).cuda()
+    w = torch.randn(128, 64, generator=g).to(torch.bfloat16).cuda()
+    y = torch.full((300, 128), 7.0, device="cuda")
+    s = bg.lib().bartels_gemm_bf16_wait_probe_d(ctx.handle, 300, 128, 64, C.c_void_p(x.data_ptr()), 64,
+                                                C.c_void_p(w.data_ptr()), C.c_void_p(y.data_ptr()), 128, 16)
+    assert s == _lib.E_TIMEOUT
+    assert b"bounded wait" in bg.lib().bartels_last_error()
+    assert torch.all(y == 7.0)  # the time-out path writes no output
+    # the context is unharmed: an ordinary GEMM afterwards
+    y2 = lpcg.gemm_bf16(ctx, x, w)
+    ref = x.double().cpu().numpy() @ w.double().cpu().numpy().T
+    assert np.abs(y2.cpu().numpy() - ref).max() <= 1e-4 * np.abs(ref).max()
+
+
 def _system(n=4, coeff=1e-2, seed=0):
     """A plan with an implicit-Euler-like Hessian M + coeff K on the device, and
     the same system as oracle blocks."""
