@@ -106,12 +106,16 @@ def solve(packed, dt=0.01, tol=1e-8, max_newton=60, precond="jacobi", net=None, 
     tuned = None
     if autotune:
         q = torch.from_numpy(packed["q_base"].ravel()).to(dev)
+        hc, hb = C.c_int(), C.c_int()
+        _lib.check(L.bartels_plan_autotune_hessian(ctx.handle, plan.handle, 0, C.c_void_p(q.data_ptr()), 0,
+                                                   C.byref(hc), C.byref(hb)), "autotune_hessian")
         _lib.check(L.bartels_plan_hessian_d(ctx.handle, plan.handle, 0, _lib.PSD_SIMPLE_FIX, 1e-6, 0, dt * dt, 1.0,
                                             C.c_void_p(q.data_ptr()), None), "hessian")
         a, b = C.c_int(), C.c_int()
         t1 = time.perf_counter()
         _lib.check(L.bartels_plan_autotune(ctx.handle, plan.handle, None, 0, C.byref(a), C.byref(b)), "autotune")
-        tuned = dict(spmv_lanes=a.value, factor_lanes=b.value, seconds=round(time.perf_counter() - t1, 3))
+        tuned = dict(spmv_lanes=a.value, factor_lanes=b.value, hessian_chunk_vertices=hc.value, psd_block=hb.value,
+                     seconds=round(time.perf_counter() - t1, 3))
     if precond == "learned":
         net.attach(plan)
     elif precond == "learned_multigrid":

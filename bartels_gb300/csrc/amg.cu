@@ -1170,6 +1170,37 @@ __global__ void __launch_bounds__(256) k_mg_sumsq(int64_t n, const float *__rest
   if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
+// Packed meshes: squared norms of v over each segment's DOFs (one CTA per
+// segment, fixed order)
+__global__ void __launch_bounds__(256)
+k_mg_seg_sumsq(const int *__restrict__ voff, const float *__restrict__ v, double *__restrict__ out) {
+  const int s = blockIdx.x;
+  float acc = 0.f;
+  for (int i = 3 * voff[s] + threadIdx.x; i < 3 * voff[s + 1]; i += blockDim.x) {
+    const float t = v[i];
+    acc += t * t;
+  }
+  const double r = cta_sum_f(acc);
+  if (threadIdx.x == 0) out[s] = r;
+}
+
+// The power iteration of a block-diagonal operator runs independently in each
+// block, so the per-segment norm ratios estimate every segment's own largest
+// eigenvalue; their maximum bounds all of them (a ratio over the whole vector
+// is dominated by the largest segments and can miss a small stiff one).
+// Written as norms (1, max ratio) for k_mg_coef.
+__global__ void k_mg_seg_lmax(int nseg, const double *__restrict__ prev, const double *__restrict__ last,
+                              double *__restrict__ norms) {
+  double m = 0.0;
+  for (int s = threadIdx.x; s < nseg; s += blockDim.x)
+    if (prev[s] > 0.0 && last[s] > 0.0 && isfinite(last[s])) m = fmax(m, last[s] / prev[s]);
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (threadIdx.x == 0) {
+    norms[0] = 1.0;
+    norms[1] = m > 0.0 ? m : 1.0;
+  }
+}
+
 struct MgDegrees {
   int deg[kMgMaxLevels];
   int nlev;
@@ -1373,7 +1404,13 @@ int mg_setup_numeric(bartels_ctx ctx, bartels_mesh_plan plan, const float *value
     BT_CUDA(cudaFuncSetAttribute(k_mg_dense_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     BT_LAUNCH(ctx, k_mg_dense_inv, 1, 1024, smem, c.n, c.rp, c.ci, c.val, mg->ainv);
   }
-  // largest eigenvalue of M A on every smoothed level (power iteration)
+  // largest eigenvalue of M A on every smoothed level (power iteration; per
+  // segment on the finest level of a packed plan)
+  const int nseg = (plan->seg && plan->seg->nseg > 0) ? plan->seg->nseg : 0;
+  if (nseg > mg->segn_n) {
+    BT_CHECK(dalloc_n(mg, &mg->segn, 2 * (size_t)nseg));
+    mg->segn_n = nseg;
+  }
   MgDegrees dg{};
   dg.nlev = L;
   for (int l = 0; l < L; ++l) {
@@ -1399,8 +1436,14 @@ int mg_setup_numeric(bartels_ctx ctx, bartels_mesh_plan plan, const float *value
       }
       if (it == kPowerIters - 2) BT_CHECK(sumsq_into(ctx, mg, n, y, mg->norms + 2 * l));
       if (it == kPowerIters - 1) BT_CHECK(sumsq_into(ctx, mg, n, y, mg->norms + 2 * l + 1));
+      if (l == 0 && nseg > 0 && it >= kPowerIters - 2)
+        BT_LAUNCH(ctx, k_mg_seg_sumsq, nseg, 256, 0, plan->seg->voff, y,
+                  mg->segn + (it == kPowerIters - 1 ? nseg : 0));
       std::swap(x, y);
     }
+    if (l == 0 && nseg > 0)
+      BT_LAUNCH(ctx, k_mg_seg_lmax, 1, 32, 0, nseg, (const double *)mg->segn, (const double *)(mg->segn + nseg),
+                mg->norms);
   }
   BT_LAUNCH(ctx, k_mg_coef, 1, 32, 0, dg, mg->norms, mg->coef);
   return BARTELS_OK;

@@ -51,6 +51,8 @@ struct MgHierarchy {
   int pinned_gen = -1;    // plan->pinned_gen the hierarchy was built for
   int64_t coarse_nnz = 0; // stored entries of all coarse levels (operator complexity)
   PcgState *st_once = nullptr;  // state for a single application outside PCG
+  double *segn = nullptr;       // per-segment norms of the finest level's last two power iterates
+  int segn_n = 0;
   // BF16 copy of the finest level's values (the plan's layout), made exactly
   // symmetric, for the V-cycle's own SpMVs (nullptr: the FP32 values are used)
   __nv_bfloat16 *a16 = nullptr;

@@ -36,6 +36,9 @@ int noalloc_gradient(bartels_ctx ctx, bartels_mesh_plan plan, int model, const d
 int plan_pcg(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const double *b, double *x,
              const bartels_pcg_params &prm, bartels_pcg_report *rep);
 int plan_set_segments(bartels_mesh_plan plan, int nseg, const int *voff, const int64_t *toff);
+int plan_autotune_hessian(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q, int force,
+                          int *chunk_out, int *block_out);
+int plan_set_hessian_tuning(bartels_mesh_plan plan, int chunk, int block);
 int newton_gradient(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params &p, const double *x,
                     double *g);
 int newton_energy(bartels_ctx ctx, bartels_mesh_plan plan, const bartels_newton_params &p, const double *x,
@@ -804,6 +807,18 @@ int bartels_plan_autotune(bartels_ctx ctx, bartels_mesh_plan plan, const float *
     values_d = plan->w_values.as<float>();
   }
   return plan_autotune(ctx, plan, values_d, force, spmv_lanes, factor_lanes);
+}
+
+int bartels_plan_autotune_hessian(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q_d, int force,
+                                  int *chunk_vertices, int *psd_block) {
+  BT_CHECK(check_plan(ctx, plan));
+  if (!q_d || !valid_model(model)) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  return plan_autotune_hessian(ctx, plan, model, q_d, force, chunk_vertices, psd_block);
+}
+
+int bartels_plan_set_hessian_tuning(bartels_mesh_plan plan, int chunk_vertices, int psd_block) {
+  if (!plan) return fail(BARTELS_E_INVALID_ARG, "null plan");
+  return plan_set_hessian_tuning(plan, chunk_vertices, psd_block);
 }
 
 int bartels_plan_set_segments(bartels_mesh_plan plan, int nseg, const int *vertex_offsets,

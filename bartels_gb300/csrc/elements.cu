@@ -466,7 +466,7 @@ __device__ __forceinline__ void with_law(const float *F, const float *pv, int co
 // order of the list does not matter: each entry writes only its own tet).
 // F and the flag are stored per tet (12 floats) for the assembly kernel.
 template <int MODEL>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(256)
 k_psd_test(int nT, const TetRec32 *__restrict__ rec, const float4 *__restrict__ u, const float4 *__restrict__ ul,
            int add_identity, float tol,
            int corot_exact, float4 *__restrict__ fslot, int *__restrict__ list, int *__restrict__ count) {
@@ -502,7 +502,7 @@ k_psd_test(int nT, const TetRec32 *__restrict__ rec, const float4 *__restrict__ 
 // PSD pre-pass, part 2, one thread per flagged tet: the projected 9x9 N
 // (packed, 45 floats) of simple_psd_fix.
 template <int MODEL>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(256)
 k_psd_eig(const int *__restrict__ list, const int *__restrict__ count, const TetRec32 *__restrict__ rec,
           const float4 *__restrict__ u, const float4 *__restrict__ ul, int add_identity, float tol, int corot_exact,
           float *__restrict__ Nbuf) {
@@ -969,12 +969,15 @@ int gradient(bartels_ctx ctx, bartels_mesh_plan plan, int model, const Objective
 template <int MODEL, bool PSD>
 static int launch_hess_t(bartels_ctx ctx, bartels_mesh_plan plan, const float4 *u, int add_identity, float cK,
                          float cM, float tol, int corot_exact, float *values) {
-  const int smem = kChunkFloats * (int)sizeof(float);
+  const bool small = plan->hess_chunk == 64 && plan->chunk_v64;
+  const int smem = (small ? kChunkFloats / 2 : kChunkFloats) * (int)sizeof(float);
   static bool attr_set = false;  // per template instance
   if (!attr_set) {
-    BT_CUDA(cudaFuncSetAttribute(k_hess<MODEL, PSD>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    BT_CUDA(cudaFuncSetAttribute(k_hess<MODEL, PSD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 kChunkFloats * (int)sizeof(float)));
     attr_set = true;
   }
+  const int pb = plan->psd_block;
   float4 *fslot = nullptr;
   float *nbuf = nullptr;
   const float4 *ul = u + plan->nV;  // lo parts of the displacement pairs follow the hi parts
@@ -987,14 +990,14 @@ static int launch_hess_t(bartels_ctx ctx, bartels_mesh_plan plan, const float4 *
     int *list = reinterpret_cast<int *>(nbuf + 45 * nT);
     int *count = list + nT;
     BT_CUDA(cudaMemsetAsync(count, 0, sizeof(int), ctx->stream));
-    BT_LAUNCH(ctx, k_psd_test<MODEL>, grid_for(ctx, plan->nT, 128), 128, 0, plan->nT, plan->rec32, u, ul,
+    BT_LAUNCH(ctx, k_psd_test<MODEL>, grid_for(ctx, plan->nT, pb), pb, 0, plan->nT, plan->rec32, u, ul,
               add_identity, tol, corot_exact, fslot, list, count);
-    BT_LAUNCH(ctx, k_psd_eig<MODEL>, grid_for(ctx, plan->nT, 128), 128, 0, list, count, plan->rec32, u, ul,
+    BT_LAUNCH(ctx, k_psd_eig<MODEL>, grid_for(ctx, plan->nT, pb), pb, 0, list, count, plan->rec32, u, ul,
               add_identity, tol, corot_exact, nbuf);
   }
-  BT_LAUNCH(ctx, (k_hess<MODEL, PSD>), plan->nchunks, kChunkMaxVerts, smem, plan->chunk_v, plan->brp, plan->inc_ptr,
-            plan->inc_tet, plan->inc_pos, plan->rec32, u, ul, add_identity, cK, cM, tol, corot_exact, fslot, nbuf,
-            values);
+  BT_LAUNCH(ctx, (k_hess<MODEL, PSD>), small ? plan->nchunks64 : plan->nchunks, small ? 64 : kChunkMaxVerts, smem,
+            small ? plan->chunk_v64 : plan->chunk_v, plan->brp, plan->inc_ptr, plan->inc_tet, plan->inc_pos,
+            plan->rec32, u, ul, add_identity, cK, cM, tol, corot_exact, fslot, nbuf, values);
   return BARTELS_OK;
 }
 

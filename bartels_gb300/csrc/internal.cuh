@@ -140,6 +140,8 @@ struct bartels_ctx_s {
   int tri_lanes = 4;
   // autotuner results per size bucket (floor(log2 nV)): {SpMV lanes, factor-pass lanes}
   std::map<int, std::pair<int, int>> tune_cache;
+  // Hessian autotuner results per size bucket: {vertices per assembly CTA, PSD block size}
+  std::map<int, std::pair<int, int>> tune_cache_hess;
   // pinned host staging for small read-backs
   double *host_scalars = nullptr;
   // device scratch for reductions
@@ -174,6 +176,12 @@ struct bartels_mesh_plan_s {
   // assembly chunks (consecutive vertex ranges whose values fit in shared memory)
   int *chunk_v = nullptr;     // nchunks + 1
   int nchunks = 0;
+  // half-size chunks (<= 64 vertices, 32 KB), made when the tuning asks for them
+  int *chunk_v64 = nullptr;
+  int nchunks64 = 0;
+  // Hessian tuning: vertices per assembly CTA (128, or 64 with chunk_v64) and
+  // threads per CTA of the PSD pre-pass kernels (64, 128 or 256)
+  int hess_chunk = 128, psd_block = 128;
   std::vector<int> h_brp, h_bcol, h_chunk_v;  // host copies
   // lazily built scalar CSR pattern (device)
   int *csr_rp = nullptr, *csr_col = nullptr;
@@ -207,6 +215,8 @@ constexpr int kChunkMaxVerts = 128;
 
 // Kernel-side entry points implemented in the .cu files.
 int plan_build(bartels_mesh_plan plan, const double *V_host, const int *E_host);
+// the half-size assembly chunks (built once, on first use)
+int plan_chunks64(bartels_mesh_plan plan);
 int plan_refresh_records(bartels_mesh_plan plan);
 int plan_build_csr_pattern(bartels_mesh_plan plan);
 
@@ -239,9 +249,6 @@ int gradient(bartels_ctx ctx, bartels_mesh_plan plan, int model, const Objective
 // f(x + alpha dx) - f(x), element by element (line search)
 int energy_diff(bartels_ctx ctx, bartels_mesh_plan plan, int model, const ObjectiveDev &obj, const double *x,
                 const double *dx, double alpha, double *d_out);
-int hessian(bartels_ctx ctx, bartels_mesh_plan plan, int model, int psd_mode, float psd_tol, int flags,
-            double coeff_K, double coeff_M, const double *q_or_null, const ObjectiveDev &obj, const double *x,
-            float *values);
 int mass_values(bartels_ctx ctx, bartels_mesh_plan plan, float *values32, double *values64);
 int ext_force(bartels_ctx ctx, bartels_mesh_plan plan, const double traction[3], double *f);
 int values_to_double(bartels_ctx ctx, const float *v32, double *v64, int64_t n);

@@ -255,6 +255,31 @@ void FactorPattern::release() {
 
 // Lower / upper storage maps of a triangular factor on the plan's block
 // pattern (rows are sorted, so the lower part of a row is a prefix of it).
+// Chunks of at most 64 consecutive vertices whose values fit in 32 KB: the
+// assembly's smaller CTA shape (more CTAs per SM, less shared memory each).
+int plan_chunks64(bartels_mesh_plan plan) {
+  if (plan->chunk_v64) return BARTELS_OK;
+  constexpr int kVerts = 64, kFloats = kChunkFloats / 2;
+  std::vector<int> chunks{0};
+  int start = 0;
+  int64_t floats = 0;
+  for (int v = 0; v < plan->nV; ++v) {
+    const int64_t need = 9ll * (plan->h_brp[v + 1] - plan->h_brp[v]);
+    if (need > kFloats) return fail(BARTELS_E_UNSUPPORTED, "vertex row too long for the half-size chunks");
+    if (v - start >= kVerts || floats + need > kFloats) {
+      chunks.push_back(v);
+      start = v;
+      floats = 0;
+    }
+    floats += need;
+  }
+  if (chunks.back() != plan->nV) chunks.push_back(plan->nV);
+  BT_CUDA(cudaMalloc(&plan->chunk_v64, sizeof(int) * chunks.size()));
+  BT_CUDA(cudaMemcpy(plan->chunk_v64, chunks.data(), sizeof(int) * chunks.size(), cudaMemcpyHostToDevice));
+  plan->nchunks64 = (int)chunks.size() - 1;
+  return BARTELS_OK;
+}
+
 int plan_factor_pattern(bartels_mesh_plan plan, FactorPattern **out) {
   if (!plan->factor) plan->factor = new FactorPattern();
   FactorPattern &f = *plan->factor;
@@ -329,6 +354,8 @@ void plan_free(bartels_mesh_plan plan) {
   plan->mg = nullptr;
   delete plan->seg;
   plan->seg = nullptr;
+  if (plan->chunk_v64) cudaFree(plan->chunk_v64);
+  plan->chunk_v64 = nullptr;
   void *ptrs[] = {plan->X,        plan->E,      plan->dphi64,  plan->vol,     plan->params,  plan->density,
                   plan->rec32,    plan->rec64,  plan->inc_ptr, plan->inc_tet, plan->inc_pos, plan->brp,
                   plan->bcol,     plan->diag_pos, plan->chunk_v, plan->csr_rp, plan->csr_col, plan->q_base,

@@ -1886,6 +1886,79 @@ int plan_spmv(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, cons
   return BARTELS_OK;
 }
 
+// Hessian autotuner: time the fused PSD-projected assembly at positions q
+// (3 warm-up + 5 timed calls, CUDA events on the context's stream) for every
+// pair of assembly CTA shape (128 vertices / 64 KB or 64 vertices / 32 KB of
+// shared memory) and PSD pre-pass block size (64, 128, 256 threads); keep the
+// fastest in the plan and in the context's cache for the size bucket
+// floor(log2 nV), which later plans of that bucket take without timing. The
+// assembled values do not depend on the choice (each entry is still summed by
+// its row's thread in tet order).
+int plan_autotune_hessian(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q, int force,
+                          int *chunk_out, int *block_out) {
+  int bucket = 0;
+  for (int v = plan->nV; v > 1; v >>= 1) bucket++;
+  auto hit = ctx->tune_cache_hess.find(bucket);
+  if (!force && hit != ctx->tune_cache_hess.end()) {
+    if (hit->second.first == 64) BT_CHECK(plan_chunks64(plan));
+    plan->hess_chunk = hit->second.first;
+    plan->psd_block = hit->second.second;
+  } else {
+    // the half-size chunks exist unless a vertex row needs more than their shared memory
+    const bool have64 = plan_chunks64(plan) == BARTELS_OK;
+    BT_CHECK(plan->w_u.ensure(2 * sizeof(float4) * (size_t)plan->nV));
+    BT_CHECK(plan->w_values.ensure(sizeof(float) * 9 * (size_t)plan->nnzb));
+    float *vals = plan->w_values.as<float>();
+    float4 *u = plan->w_u.as<float4>();
+    BT_CHECK(launch_prep_u(ctx, plan, q, nullptr, 1.0, plan->dphi_matches_rest, u));
+    cudaEvent_t e0, e1;
+    BT_CUDA(cudaEventCreate(&e0));
+    BT_CUDA(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int bc = 128, bb = 128;
+    int status = BARTELS_OK;
+    const int chunks[2] = {128, 64}, blocks[3] = {64, 128, 256};
+    for (int c : chunks)
+      for (int bl : blocks) {
+        if (c == 64 && !have64) continue;
+        plan->hess_chunk = c;
+        plan->psd_block = bl;
+        for (int k = 0; k < 8 && status == BARTELS_OK; ++k) {
+          if (k == 3) cudaEventRecord(e0, ctx->stream);
+          status = launch_hess(ctx, plan, model, BARTELS_PSD_SIMPLE_FIX, u, plan->dphi_matches_rest ? 1 : 0, 1.f,
+                               0.f, 1e-6f, 0, vals);
+        }
+        cudaEventRecord(e1, ctx->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (status == BARTELS_OK && ms < best) {
+          best = ms;
+          bc = c;
+          bb = bl;
+        }
+      }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (status != BARTELS_OK) return status;
+    plan->hess_chunk = bc;
+    plan->psd_block = bb;
+    ctx->tune_cache_hess[bucket] = {bc, bb};
+  }
+  if (chunk_out) *chunk_out = plan->hess_chunk;
+  if (block_out) *block_out = plan->psd_block;
+  return BARTELS_OK;
+}
+
+int plan_set_hessian_tuning(bartels_mesh_plan plan, int chunk, int block) {
+  if ((chunk != 64 && chunk != 128) || (block != 64 && block != 128 && block != 256))
+    return fail(BARTELS_E_INVALID_ARG, "assembly CTA shape must be 64 or 128 vertices, PSD block 64, 128 or 256");
+  if (chunk == 64) BT_CHECK(plan_chunks64(plan));
+  plan->hess_chunk = chunk;
+  plan->psd_block = block;
+  return BARTELS_OK;
+}
+
 // Autotuner: time the block-row SpMV with 4, 8 and 16 lanes per vertex row and
 // the factor passes with 4 and 8 lanes on this plan (CUDA events on the
 // context's stream, 3 warm-up + 10 timed launches each), keep the fastest in
@@ -1944,10 +2017,17 @@ int plan_autotune(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, 
     const int cand_s[3] = {4, 8, 16};
     for (int G : cand_s) {
       const int g = grid_spmv(ctx, (int64_t)nV * G / 32 + 1);
+      // the PCG loop's own SpMV (A p and the partials of p.Ap) on a scratch state
       const float ms = timed([&] {
-        if (G == 4) k_spmv_blk_g<4><<<g, 256, 0, ctx->stream>>>(nV, plan->brp, plan->bcol, values, x, y, plan->pinned);
-        else if (G == 8) k_spmv_blk_g<8><<<g, 256, 0, ctx->stream>>>(nV, plan->brp, plan->bcol, values, x, y, plan->pinned);
-        else k_spmv_blk_g<16><<<g, 256, 0, ctx->stream>>>(nV, plan->brp, plan->bcol, values, x, y, plan->pinned);
+        if (G == 4)
+          k_pcg_spmv_blk<4><<<g, 256, 0, ctx->stream>>>(nV, plan->brp, plan->bcol, values, x, x, y, plan->pinned,
+                                                        part, st);
+        else if (G == 8)
+          k_pcg_spmv_blk<8><<<g, 256, 0, ctx->stream>>>(nV, plan->brp, plan->bcol, values, x, x, y, plan->pinned,
+                                                        part, st);
+        else
+          k_pcg_spmv_blk<16><<<g, 256, 0, ctx->stream>>>(nV, plan->brp, plan->bcol, values, x, x, y, plan->pinned,
+                                                         part, st);
       });
       if (ms < best) {
         best = ms;

@@ -199,13 +199,19 @@ def run_gpu(args, rank, world):
     if not args.no_autotune:
         hv = torch.empty(plan.nnz, dtype=torch.float32, device=f"cuda:{dev}")
         q0 = torch.from_numpy(qt).to(f"cuda:{dev}")
+        # assembly CTA shape and PSD pre-pass block size (values do not depend on them)
+        h_c, h_b = C.c_int(), C.c_int()
+        _lib.check(L.bartels_plan_autotune_hessian(ctx.handle, plan.handle, bg.api.MODELS[args.model],
+                                                   C.c_void_p(q0.data_ptr()), 0, C.byref(h_c), C.byref(h_b)),
+                   "autotune_hessian")
         _lib.check(L.bartels_plan_hessian_d(ctx.handle, plan.handle, bg.api.MODELS[args.model], psd, 1e-6, 0,
                                             pb["dt"] ** 2, 1.0, C.c_void_p(q0.data_ptr()), C.c_void_p(hv.data_ptr())),
                    "hessian")
         a_l, b_l = C.c_int(), C.c_int()
         _lib.check(L.bartels_plan_autotune(ctx.handle, plan.handle, C.c_void_p(hv.data_ptr()), 0, C.byref(a_l),
                                            C.byref(b_l)), "autotune")
-        lanes = {"spmv": a_l.value, "factor": b_l.value}
+        lanes = {"spmv": a_l.value, "factor": b_l.value, "hessian_chunk_vertices": h_c.value,
+                 "psd_block": h_b.value}
         del hv, q0
     net = None
     if args.precond in ("learned", "learned_multigrid"):

@@ -450,13 +450,25 @@ int bartels_plan_precond_apply_d(bartels_ctx ctx, bartels_mesh_plan plan, const 
 int bartels_plan_pcg_d(bartels_ctx ctx, bartels_mesh_plan plan, const float *values_d, const double *b_d,
                        double *x_d, const bartels_pcg_params *params, bartels_pcg_report *report);
 /* ---------------------------------------------------------------- batching -- */
-/* Autotuner: times the block-row SpMV (4, 8, 16 lanes per vertex row) and the
+/* Autotuner: times the PCG loop's block-row SpMV (4, 8, 16 lanes per vertex row) and the
  * factor passes (4, 8 lanes) on this plan's Hessian (values_d, or NULL for the
  * plan's internal buffer) and keeps the fastest for the plan's PCG solves. The
  * choice is cached in the context per size bucket floor(log2 nV) and reused by
  * later plans of that bucket unless force != 0. No counterpart in the reference. */
 int bartels_plan_autotune(bartels_ctx ctx, bartels_mesh_plan plan, const float *values_d, int force,
                           int *spmv_lanes, int *factor_lanes);
+/* Hessian autotuner: times the fused simple_psd_fix-projected assembly of the
+ * plan at device positions q_d for the assembly's CTA shapes (128 vertices
+ * per CTA with 64 KB of shared memory, or 64 vertices with 32 KB) and the PSD
+ * pre-pass block sizes (64, 128, 256 threads), keeps the fastest pair for the
+ * plan's Hessians and caches it in the context per size bucket floor(log2 nV)
+ * (reused by later plans of that bucket unless force != 0). The assembled
+ * values do not depend on the choice. No counterpart in the reference. */
+int bartels_plan_autotune_hessian(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q_d, int force,
+                                  int *chunk_vertices, int *psd_block);
+/* Set the same choice by hand (chunk_vertices 64 or 128, psd_block 64, 128
+ * or 256). */
+int bartels_plan_set_hessian_tuning(bartels_mesh_plan plan, int chunk_vertices, int psd_block);
 /* Batched solves pack many meshes into one plan (a block-diagonal system, one
  * launch per Newton stage for all of them); per-mesh convergence uses
  * out_d[s] = sum of v_d^2 over the DOFs of vertices vertex_offsets_d[s] ..

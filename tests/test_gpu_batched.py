@@ -47,6 +47,55 @@ def test_autotuner_picks_valid_lanes_and_caches_per_bucket():
     assert res[0] == res[1]
 
 
+def test_hessian_autotuner_choice_is_cached_and_does_not_change_values():
+    """Every assembly CTA shape and PSD block size gives the same Hessian bits;
+    the autotuner picks one of them and a second plan of the same size bucket
+    takes it from the context's cache."""
+    torch = pytest.importorskip("torch")
+    import bartels_gb300 as bg
+    from bartels_gb300 import _lib
+    from bartels_gb300.meshes import kuhn_cube, material_params
+    L = bg.lib()
+    ctx = bg.Context.default()
+    V, E = kuhn_cube(26)
+    plan = bg.MeshPlan(V, E, ctx)
+    plan.set_element_data(params=material_params("neohookean", len(E), 2e6, 0.45), density=np.full(len(E), 1e3))
+    rng = np.random.default_rng(4)
+    q = torch.from_numpy((V * np.array([1.0, 1.0, 0.6]) + 0.01 * rng.standard_normal(V.shape)).ravel()).cuda()
+
+    def hess():
+        vals = torch.empty(plan.nnz, dtype=torch.float32, device="cuda")
+        _lib.check(L.bartels_plan_hessian_d(ctx.handle, plan.handle, 0, _lib.PSD_SIMPLE_FIX, 1e-6, 0, 1e-4, 1.0,
+                                            C.c_void_p(q.data_ptr()), C.c_void_p(vals.data_ptr())), "hessian")
+        ctx.synchronize()
+        return vals.cpu().numpy()
+
+    ref = None
+    for chunk in (128, 64):
+        for block in (64, 128, 256):
+            _lib.check(L.bartels_plan_set_hessian_tuning(plan.handle, chunk, block), "set tuning")
+            h = hess()
+            if ref is None:
+                ref = h
+            assert np.array_equal(h, ref), (chunk, block)
+    assert L.bartels_plan_set_hessian_tuning(plan.handle, 96, 128) != 0
+    c, b = C.c_int(), C.c_int()
+    _lib.check(L.bartels_plan_autotune_hessian(ctx.handle, plan.handle, 0, C.c_void_p(q.data_ptr()), 1,
+                                               C.byref(c), C.byref(b)), "autotune_hessian")
+    assert c.value in (64, 128) and b.value in (64, 128, 256)
+    assert np.array_equal(hess(), ref)
+    plan.close()
+    V2, E2 = kuhn_cube(28)  # 24,389 vertices against 19,683: the same bucket
+    plan2 = bg.MeshPlan(V2, E2, ctx)
+    plan2.set_element_data(params=material_params("neohookean", len(E2), 2e6, 0.45))
+    q2 = torch.from_numpy(V2.ravel().copy()).cuda()
+    c2, b2 = C.c_int(), C.c_int()
+    _lib.check(L.bartels_plan_autotune_hessian(ctx.handle, plan2.handle, 0, C.c_void_p(q2.data_ptr()), 0,
+                                               C.byref(c2), C.byref(b2)), "autotune_hessian")
+    assert (c2.value, b2.value) == (c.value, b.value)
+    plan2.close()
+
+
 @pytest.mark.parametrize("precond", ["jacobi", "learned"])
 def test_batched_step_matches_one_by_one(precond):
     pytest.importorskip("torch")
