@@ -68,6 +68,17 @@ class Context:
     def synchronize(self):
         check(lib().bartels_ctx_synchronize(self.handle), "bartels_ctx_synchronize")
 
+    def torch_stream(self):
+        """The context's CUDA stream as a torch stream. The library enqueues on
+        its own non-blocking stream, so tensors that torch writes for a device
+        call (or reads from one) are ordered with it by running those torch ops
+        under `with torch.cuda.stream(ctx.torch_stream()):`."""
+        if getattr(self, "_torch_stream", None) is None:
+            import torch
+            self._torch_stream = torch.cuda.ExternalStream(int(lib().bartels_ctx_stream(self.handle)),
+                                                           device=f"cuda:{self.device}")
+        return self._torch_stream
+
     @property
     def kernel_launches(self) -> int:
         return int(lib().bartels_ctx_kernel_launches(self.handle))

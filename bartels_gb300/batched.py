@@ -90,10 +90,11 @@ def solve(packed, dt=0.01, tol=1e-8, max_newton=60, precond="jacobi", net=None, 
     prm = bg.newton_params(model="neohookean", psd_mode=_lib.PSD_SIMPLE_FIX, psd_tol=1e-6, mass_coeff=1.0, scale=dt,
                            force_scale=dt, gradient_tol=0.0, relative=0, max_iterations=1 << 30)
     dev = torch.device(f"cuda:{ctx.device}")
-    x = torch.zeros(3 * nV, dtype=torch.float64, device=dev)
-    g = torch.empty_like(x)
-    off = torch.from_numpy(packed["voff"]).to(dev)
-    ss = torch.empty(ns, dtype=torch.float64, device=dev)
+    with torch.cuda.stream(ctx.torch_stream()):  # ordered with the library's kernels
+        x = torch.zeros(3 * nV, dtype=torch.float64, device=dev)
+        g = torch.empty_like(x)
+        off = torch.from_numpy(packed["voff"]).to(dev)
+        ss = torch.empty(ns, dtype=torch.float64, device=dev)
     xp, gp = C.c_void_p(x.data_ptr()), C.c_void_p(g.data_ptr())
 
     def inst_norms():
@@ -105,7 +106,8 @@ def solve(packed, dt=0.01, tol=1e-8, max_newton=60, precond="jacobi", net=None, 
 
     tuned = None
     if autotune:
-        q = torch.from_numpy(packed["q_base"].ravel()).to(dev)
+        with torch.cuda.stream(ctx.torch_stream()):
+            q = torch.from_numpy(packed["q_base"].ravel()).to(dev)
         hc, hb = C.c_int(), C.c_int()
         _lib.check(L.bartels_plan_autotune_hessian(ctx.handle, plan.handle, 0, C.c_void_p(q.data_ptr()), 0,
                                                    C.byref(hc), C.byref(hb)), "autotune_hessian")

@@ -14,6 +14,7 @@
 
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <vector>
@@ -856,6 +857,16 @@ static int launch_cond(bartels_ctx ctx, cudaGraphConditionalHandle h, PcgState *
 // end with no host round trip and no iteration after convergence). Fallback:
 // a fixed run of `chunk` iterations whose kernels turn into no-ops once the
 // state is done. *launches: kernel launches per body / chunk.
+// BARTELS_PCG_DEVICE_LOOP=0 selects the fixed-length form (kernel profilers
+// that replay launches one by one handle plain graphs only).
+static bool device_loop_allowed() {
+  static const bool allowed = [] {
+    const char *e = std::getenv("BARTELS_PCG_DEVICE_LOOP");
+    return !(e && e[0] == '0');
+  }();
+  return allowed;
+}
+
 static int build_loop_graph(bartels_ctx ctx, PcgState *st, const std::function<int(int)> &enqueue, int chunk,
                             cudaGraphExec_t *exec, int64_t *launches, bool *device_loop) {
   *exec = nullptr;
@@ -865,7 +876,8 @@ static int build_loop_graph(bartels_ctx ctx, PcgState *st, const std::function<i
   cudaGraphConditionalHandle h;
   cudaGraphNodeParams cp = {};
   cudaGraphNode_t node;
-  cudaError_t e = cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault);
+  cudaError_t e = device_loop_allowed() ? cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault)
+                                        : cudaErrorNotSupported;
   if (e == cudaSuccess) {
     cp.type = cudaGraphNodeTypeConditional;
     cp.conditional.handle = h;

@@ -283,17 +283,20 @@ def newton_systems(ctx: Context, cfg: dict, newton_iters: int = 3, model: str | 
     dt = cfg["dt"]
     prm = newton_params(model=model, psd_mode=_lib.PSD_SIMPLE_FIX, psd_tol=1e-6, mass_coeff=1.0, scale=dt,
                         force_scale=dt, gradient_tol=1e-8, relative=1, max_iterations=newton_iters)
-    x = torch.zeros(3 * len(V), dtype=torch.float64, device=dev)
-    qb = torch.from_numpy(q_base).to(dev)
+    stream = ctx.torch_stream()  # torch ops below are ordered with the library's kernels
+    with torch.cuda.stream(stream):
+        x = torch.zeros(3 * len(V), dtype=torch.float64, device=dev)
+        qb = torch.from_numpy(q_base).to(dev)
     nnzb = plan.nnz // 9
     out = []
     g0 = -1.0
     for it in range(newton_iters):
-        values = torch.empty(9 * nnzb, dtype=torch.float32, device=dev)
-        q = qb + dt * x
+        with torch.cuda.stream(stream):
+            values = torch.empty(9 * nnzb, dtype=torch.float32, device=dev)
+            q = qb + dt * x
+            g = torch.empty_like(x)
         check(lib().bartels_plan_hessian_d(ctx.handle, plan.handle, MODELS[model], _lib.PSD_SIMPLE_FIX, 1e-6, 0,
                                            dt * dt, 1.0, _ptr(q), _ptr(values)), "bartels_plan_hessian_d")
-        g = torch.empty_like(x)
         check(lib().bartels_newton_gradient_d(ctx.handle, plan.handle, C.byref(prm), _ptr(x), _ptr(g)),
               "bartels_newton_gradient_d")
         ctx.synchronize()
@@ -306,6 +309,108 @@ def newton_systems(ctx: Context, cfg: dict, newton_iters: int = 3, model: str | 
         if done.value:
             break
     return out
+
+
+def packed_newton_systems(ctx: Context, count: int, seed: int, n_range=(8, 40), newton_iters: int = 4,
+                          dt: float = 0.01):
+    """Yield the (Hessian, residual) pairs of the first newton_iters implicit-Euler
+    Newton iterations of `count` instances drawn as bartels_gb300.batched draws
+    them (Neo-Hookean cubes, n uniform in n_range, E log-uniform in [1e5, 1e7],
+    nu uniform in [0.30, 0.48], per-axis stretch uniform in [0.7, 1.3] plus
+    vertex noise, z = 0 pinned, gravity, dt = 0.01), packed into one plan with
+    per-instance PCG and line search (bartels_plan_set_segments) and stepped by
+    the library's own Newton solver with block-Jacobi PCG. Each yielded System
+    holds `count` instance systems; its residual is scaled per instance to unit
+    root-mean-square, so that every instance weighs the same in the residual
+    probe. The caller closes the plan (System.plan) when it is done with the
+    systems."""
+    import torch
+    from . import batched
+    from .api import volume as _volume
+    dev = torch.device(f"cuda:{ctx.device}")
+    pk = batched.pack(batched.make_instances(count, seed, n_range))
+    V, E = pk["V"], pk["E"]
+    plan = MeshPlan(V, E, ctx)
+    plan.set_element_data(params=pk["params"], density=np.full(len(E), 1000.0))
+    f_g = plan.const_ext_force(_volume(V, E), np.array([0.0, 0.0, -9.81 * 1000.0]))
+    plan.set_problem(q_base=pk["q_base"].ravel(), x_hat=np.zeros(3 * len(V)), f_ext=f_g, pinned=pk["pinned"])
+    voff = np.ascontiguousarray(pk["voff"], np.int32)
+    toff = np.ascontiguousarray(pk["toff"], np.int64)
+    check(lib().bartels_plan_set_segments(plan.handle, count, voff.ctypes.data_as(C.POINTER(C.c_int)),
+                                          toff.ctypes.data_as(C.POINTER(C.c_int64))), "bartels_plan_set_segments")
+    prm = newton_params(model="neohookean", psd_mode=_lib.PSD_SIMPLE_FIX, psd_tol=1e-6, mass_coeff=1.0, scale=dt,
+                        force_scale=dt, gradient_tol=0.0, relative=0, max_iterations=1 << 30)
+    stream = ctx.torch_stream()  # torch ops below are ordered with the library's kernels
+    with torch.cuda.stream(stream):
+        x = torch.zeros(3 * len(V), dtype=torch.float64, device=dev)
+        qb = torch.from_numpy(pk["q_base"].ravel().copy()).to(dev)
+        seg = torch.from_numpy(np.repeat(np.arange(count), 3 * np.diff(voff))).to(dev)
+        dof = torch.from_numpy(3 * np.diff(voff).astype(np.float64)).to(dev)
+    for it in range(newton_iters):
+        with torch.cuda.stream(stream):
+            values = torch.empty(plan.nnz, dtype=torch.float32, device=dev)
+            q = qb + dt * x
+            g = torch.empty_like(x)
+        check(lib().bartels_plan_hessian_d(ctx.handle, plan.handle, MODELS["neohookean"], _lib.PSD_SIMPLE_FIX,
+                                           1e-6, 0, dt * dt, 1.0, _ptr(q), _ptr(values)), "bartels_plan_hessian_d")
+        check(lib().bartels_newton_gradient_d(ctx.handle, plan.handle, C.byref(prm), _ptr(x), _ptr(g)),
+              "bartels_newton_gradient_d")
+        with torch.cuda.stream(stream):
+            ss = torch.zeros(count, dtype=torch.float64, device=dev).index_add_(0, seg, g * g)
+            g = g * torch.sqrt(dof / torch.clamp(ss, min=1e-300))[seg]
+        ctx.synchronize()
+        yield System(plan, values, g, dict(instances=count, seed=seed, newton_iteration=it))
+        if it + 1 < newton_iters:
+            done = C.c_int()
+            rep = _lib.NewtonReport()
+            check(lib().bartels_newton_iterate_d(ctx.handle, plan.handle, C.byref(prm), _ptr(x), C.c_double(1.0),
+                                                 C.byref(done), C.byref(rep)), "bartels_newton_iterate_d")
+
+
+def train_stream(net: LearnedPreconditioner, ctx: Context, systems: int, steps: int, per_pack: int = 16,
+                 n_range=(8, 40), newton_iters: int = 4, pool: int = 8, lr: float = 2e-3, lr_end: float = 1e-4,
+                 nprobes: int = 4, seed: int = 0, log=None):
+    """Adam on the Kaporin loss over a stream of Newton systems: packs of
+    per_pack instances are drawn and stepped (packed_newton_systems) until
+    `systems` instance systems have been produced; each packed system enters a
+    rolling pool of the `pool` most recent ones, and steps / (packed systems)
+    training steps are taken after each arrival on systems drawn from the pool.
+    No more than the pool's Hessians (and the plans they belong to) are held."""
+    rng = np.random.default_rng(seed)
+    packs = max(1, -(-systems // (per_pack * newton_iters)))
+    per_arrival = steps / float(packs * newton_iters)
+    hist, recent = [], []
+    t0 = time.time()
+    produced, done_steps, owed, next_log = 0, 0, 0.0, 0
+    def drop_oldest():
+        old = recent.pop(0)
+        if all(r.plan is not old.plan for r in recent) and old.plan is not current[0]:
+            old.plan.close()
+
+    current = [None]
+    for k in range(packs):
+        for sysm in packed_newton_systems(ctx, per_pack, seed * 100003 + k, n_range, newton_iters):
+            current[0] = sysm.plan
+            recent.append(sysm)
+            if len(recent) > pool:
+                drop_oldest()
+            produced += per_pack
+            owed += per_arrival
+            while owed >= 1.0 and done_steps < steps:
+                pick = recent[int(rng.integers(len(recent)))]
+                a = lr_end + 0.5 * (lr - lr_end) * (1 + math.cos(math.pi * done_steps / max(steps, 1)))
+                hist.append(net.train_step(pick.plan, pick.values, pick.residual, nprobes=nprobes,
+                                           seed=int(rng.integers(1 << 31)), lr=a, clip=1.0))
+                done_steps += 1
+                owed -= 1.0
+            if log and done_steps >= next_log:
+                next_log += max(steps // 20, 1)
+                log(f"systems {produced:6d}  step {done_steps:6d}  loss {np.mean(hist[-50:]) if hist else 0:.4f}  "
+                    f"{time.time() - t0:.1f}s")
+        current[0] = None
+    while recent:
+        drop_oldest()
+    return hist, produced
 
 
 def perturbed_systems(ctx: Context, cfg: dict, count: int = 1, noise: float = 0.02, model: str | None = None):
@@ -322,8 +427,9 @@ def perturbed_systems(ctx: Context, cfg: dict, count: int = 1, noise: float = 0.
     rng = np.random.default_rng(cfg.get("seed", 0))
     out = []
     for k in range(count):
-        q = torch.from_numpy((V + noise / cfg["n"] * rng.uniform(-1, 1, V.shape)).ravel()).to(dev)
-        values = torch.empty(plan.nnz, dtype=torch.float32, device=dev)
+        with torch.cuda.stream(ctx.torch_stream()):  # ordered with the library's kernels
+            q = torch.from_numpy((V + noise / cfg["n"] * rng.uniform(-1, 1, V.shape)).ravel()).to(dev)
+            values = torch.empty(plan.nnz, dtype=torch.float32, device=dev)
         check(lib().bartels_plan_hessian_d(ctx.handle, plan.handle, MODELS[model], _lib.PSD_SIMPLE_FIX, 1e-6, 0,
                                            cfg["dt"] ** 2, 1.0, _ptr(q), _ptr(values)), "bartels_plan_hessian_d")
         out.append(System(plan, values, None, dict(cfg, sample=k)))

@@ -6,6 +6,9 @@
         (the recipe of the shipped weights)
     python -m bartels_gb300.train_lpcg --systems 0 --steps 0 --init bartels_gb300/weights/lpcg_neohookean.npz --eval 96
         (evaluation only: PCG iterations and seconds, learned vs block-Jacobi)
+    python -m bartels_gb300.train_lpcg --kind stream --systems 20000 --per-pack 16 --newton-iters 4 --nmin 8 \
+        --nmax 40 --steps 6000 --probes 4 --lr 2e-3 --eval 40,96 --out weights.npz
+        (Newton systems of packed batched-style instances, streamed: 20k instance systems, never all held)
 
 Training systems are (Hessian, residual) pairs from implicit-Euler Newton
 iterations on Neo-Hookean Kuhn cubes of random size, stiffness, Poisson ratio,
@@ -75,8 +78,12 @@ def main(argv=None):
     ap.add_argument("--ratio", default="30,30000", help="range of E dt^2 / (rho h^2) of the training cubes")
     ap.add_argument("--nu", default="0.30,0.48", help="range of Poisson ratios")
     ap.add_argument("--stretch", type=float, default=0.15, help="initial per-axis stretch range 1 +- s")
-    ap.add_argument("--kind", default="newton", choices=["newton", "rest"],
-                    help="newton: Newton-iteration Hessians with residuals; rest: Hessians at perturbed rest states")
+    ap.add_argument("--kind", default="newton", choices=["newton", "rest", "stream"],
+                    help="newton: Newton-iteration Hessians with residuals; rest: Hessians at perturbed rest states; "
+                         "stream: Newton systems of packed batched-style instances, streamed through a rolling pool "
+                         "(--systems counts instance systems)")
+    ap.add_argument("--per-pack", type=int, default=16, help="stream: instances per packed plan")
+    ap.add_argument("--pool", type=int, default=8, help="stream: packed systems held for sampling")
     ap.add_argument("--no-residual", action="store_true", help="train with Rademacher probes only")
     ap.add_argument("--hetero", type=float, default=0.0,
                     help="sigma of a log-normal per-tet stiffness factor on a fraction of the cubes")
@@ -90,6 +97,22 @@ def main(argv=None):
     models = tuple(m for m in args.models.split(",") if m)
     rr = tuple(float(v) for v in args.ratio.split(","))
     nr = tuple(float(v) for v in args.nu.split(","))
+    if args.kind == "stream":
+        net = lpcg.LearnedPreconditioner.load(args.init, ctx) if args.init else lpcg.LearnedPreconditioner(
+            ctx, seed=args.seed)
+        hist, produced = lpcg.train_stream(net, ctx, args.systems, args.steps, per_pack=args.per_pack,
+                                           n_range=(args.nmin, args.nmax), newton_iters=args.newton_iters,
+                                           pool=args.pool, lr=args.lr, lr_end=args.lr_end, nprobes=args.probes,
+                                           seed=args.seed, log=lambda s: print(s, flush=True))
+        t_train = time.time() - t0
+        print(f"stream training: {produced} instance systems, {len(hist)} steps in {t_train:.1f}s", flush=True)
+        rows = evaluate(ctx, net, [int(s) for s in args.eval.split(",") if s])
+        if args.out and hist:
+            net.save(args.out, loss_first=np.mean(hist[:20]), loss_last=np.mean(hist[-50:]), steps=len(hist),
+                     systems=produced, seed=args.seed, lr=args.lr, probes=args.probes, kind="stream",
+                     eval_ratio=np.mean([r["ratio"] for r in rows]) if rows else np.nan)
+            print("wrote", args.out, flush=True)
+        return rows
     for cfg in lpcg.sample_configs(args.systems, seed=args.seed, n_range=(args.nmin, args.nmax), models=models,
                                    ratio_range=rr, nu_range=nr, stretch=args.stretch, hetero=args.hetero,
                                    hetero_frac=args.hetero_frac):

@@ -199,6 +199,7 @@ def run_gpu(args, rank, world):
     if not args.no_autotune:
         hv = torch.empty(plan.nnz, dtype=torch.float32, device=f"cuda:{dev}")
         q0 = torch.from_numpy(qt).to(f"cuda:{dev}")
+        torch.cuda.synchronize()  # x and q0 written on torch's stream before the library reads them
         # assembly CTA shape and PSD pre-pass block size (values do not depend on them)
         h_c, h_b = C.c_int(), C.c_int()
         _lib.check(L.bartels_plan_autotune_hessian(ctx.handle, plan.handle, bg.api.MODELS[args.model],
@@ -357,6 +358,7 @@ def run_gpu(args, rank, world):
     n_dof = 3 * nV
     xs = torch.randn(n_dof, dtype=torch.float32, device=f"cuda:{dev}")
     ys = torch.empty_like(xs)
+    torch.cuda.synchronize()  # torch's stream before the library's
     nnz = plan.nnz
     nnzb = nnz // 9
 
@@ -377,6 +379,7 @@ def run_gpu(args, rank, world):
                                                                   C.c_void_p(ys.data_ptr())), "spmv"), 30)
     spmv_bytes = 4 * nnz + 4 * nnzb + 4 * (nV + 1) + 12 * nV + 12 * nV
     qd = torch.from_numpy(V.ravel().copy()).to(f"cuda:{dev}")
+    torch.cuda.synchronize()
     model_id = bg.api.MODELS[args.model]
 
     def hess_time(psd_mode):

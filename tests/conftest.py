@@ -17,6 +17,28 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
 
 
+@pytest.fixture(autouse=True)
+def _torch_on_library_stream(request):
+    """GPU tests run torch's ops on the default context's stream: the library
+    enqueues on its own non-blocking stream, so inputs that torch writes
+    (zeros, host copies, arithmetic) are then ordered with the library's
+    kernels without a host synchronisation after every tensor op."""
+    if request.node.get_closest_marker("gpu") is None:
+        yield
+        return
+    try:
+        import torch
+        ok = torch.cuda.is_available()
+    except ImportError:
+        ok = False
+    if not ok:
+        yield
+        return
+    import bartels_gb300 as bg
+    with torch.cuda.stream(bg.Context.default().torch_stream()):
+        yield
+
+
 def load_golden_mesh(name):
     g = np.load(os.path.join(GOLDEN, name + ".npz"))
     return g["V"].astype(np.float64), g["E"].astype(np.int32)

@@ -295,3 +295,40 @@ def test_committed_weights_beat_block_jacobi():
         assert rj.converged and rl.converged
         assert rl.iterations <= 0.7 * rj.iterations, (rl.iterations, rj.iterations)
     net.close()
+
+
+def test_streamed_newton_systems_train_and_release_their_plans():
+    """Streaming training on packed Newton systems: 2 packs of 3 instances
+    (n = 4..6), 3 Newton iterations each (18 instance systems) through a pool of
+    2 packed systems; the loss stays finite, each yielded residual has unit
+    root-mean-square per instance, and every pack's plan is closed at the end."""
+    torch = _torch()
+    import bartels_gb300 as bg
+    from bartels_gb300 import lpcg
+    ctx = bg.Context.default()
+    seen = []
+    gen = lpcg.packed_newton_systems(ctx, 3, seed=11, n_range=(4, 6), newton_iters=2)
+    for sysm in gen:
+        seen.append(sysm)
+        assert torch.isfinite(sysm.residual).all()
+    plan = seen[0].plan
+    r = seen[0].residual.cpu().numpy()
+    assert abs(np.sqrt(np.mean(r ** 2)) - 1.0) < 1e-9
+    plan.close()
+    net = lpcg.LearnedPreconditioner(ctx, seed=0)
+    plans = []
+    orig = lpcg.packed_newton_systems
+
+    def spy(*a, **k):
+        for s in orig(*a, **k):
+            plans.append(s.plan)
+            yield s
+    lpcg.packed_newton_systems = spy
+    try:
+        hist, produced = lpcg.train_stream(net, ctx, systems=18, steps=6, per_pack=3, n_range=(4, 6),
+                                           newton_iters=3, pool=2, nprobes=2, seed=0)
+    finally:
+        lpcg.packed_newton_systems = orig
+    assert produced == 18 and len(hist) == 6 and np.all(np.isfinite(hist))
+    assert len({id(p) for p in plans}) == 2 and all(p.handle is None for p in plans)
+    net.close()
