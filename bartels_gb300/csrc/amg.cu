@@ -39,6 +39,7 @@
 // is set, so fixed-length CUDA graphs of PCG iterations can contain it.
 #include <algorithm>
 #include <climits>
+#include <type_traits>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -401,7 +402,18 @@ int mg_prepare(bartels_ctx ctx, bartels_mesh_plan plan) {
     BT_CHECK(dalloc_n(mg, &d.d, nv));
     if (l > 0) BT_CHECK(dalloc_n(mg, &d.d2, nv));
   }
-  if (env_int("BARTELS_MG_FINE_BF16", 1, 0, 1)) BT_CHECK(dalloc_n(mg, &mg->a16, 9 * (size_t)plan->nnzb));
+  if (env_int("BARTELS_MG_FINE_BF16", 1, 0, 1)) {
+    std::vector<int> off(plan->nV + 1, 0);
+    for (int v = 0; v < plan->nV; ++v) {
+      const int64_t next = off[v] + 3ll * padded_row(plan->h_brp[v + 1] - plan->h_brp[v]);
+      if (next > INT_MAX) return fail(BARTELS_E_UNSUPPORTED, "multigrid: BF16 copy larger than 2^31 entries");
+      off[v + 1] = (int)next;
+    }
+    BT_CHECK(upload(mg, &mg->a16_off, off));
+    BT_CHECK(dalloc_n(mg, &mg->a16, (size_t)off[plan->nV] + 4));
+    // the pads stay zero (the conversion writes only the entries)
+    BT_CUDA(cudaMemset(mg->a16, 0, sizeof(__nv_bfloat16) * ((size_t)off[plan->nV] + 4)));
+  }
   if (mg->dense) {
     mg->nd = 6 * mg->lv.back().n;
     BT_CHECK(dalloc_n(mg, &mg->ainv, (size_t)mg->nd * mg->nd));
@@ -789,12 +801,13 @@ k_mg0_update(int nV, const float *__restrict__ pa, const float *__restrict__ pb,
 // per vertex row, one lane per block.
 __global__ void __launch_bounds__(256)
 k_mg0_to_bf16(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, const int *__restrict__ rev,
-              const float *__restrict__ val, __nv_bfloat16 *__restrict__ a16) {
+              const float *__restrict__ val, const int *__restrict__ a16_off, __nv_bfloat16 *__restrict__ a16) {
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   for (int v = warp; v < nV; v += nwarps) {
-    const int rb = brp[v], nb = brp[v + 1] - rb, rs = 3 * nb;
+    const int rb = brp[v], nb = brp[v + 1] - rb, rs = 3 * nb, rsp = padded_row(nb);
+    __nv_bfloat16 *out = a16 + __ldg(a16_off + v);
     for (int j = lane; j < nb; j += 32) {
       const int w = __ldg(bcol + rb + j);
       const int q = __ldg(rev + rb + j);
@@ -805,9 +818,23 @@ k_mg0_to_bf16(int nV, const int *__restrict__ brp, const int *__restrict__ bcol,
         for (int l = 0; l < 3; ++l) {
           const float a = __ldg(val + 9ll * rb + k * rs + 3 * j + l);
           const float t = __ldg(val + 9ll * rbw + l * rsw + 3 * jq + k);
-          a16[9ll * rb + k * rs + 3 * j + l] = __float2bfloat16_rn(0.5f * (a + t));
+          out[k * rsp + 3 * j + l] = __float2bfloat16_rn(0.5f * (a + t));
         }
     }
+  }
+}
+
+// One row of the finest level: the FP32 values in the plan's layout
+// (off == nullptr), or the padded BF16 copy (4 values per 8-byte load).
+template <int G, class VT, class XV>
+__device__ __forceinline__ void row0_acc(int v, int sl, const int *__restrict__ brp, const int *__restrict__ bcol,
+                                         const VT *__restrict__ val, const int *__restrict__ off, XV &&xval,
+                                         float &s0, float &s1, float &s2) {
+  if constexpr (std::is_same<VT, __nv_bfloat16>::value) {
+    const int rb = __ldg(brp + v), nb = __ldg(brp + v + 1) - rb;
+    tri_row_acc4<G>(sl, bcol + rb, val + __ldg(off + v), 3 * nb, padded_row(nb), xval, s0, s1, s2);
+  } else {
+    spmv_row_acc<G>(v, sl, brp, bcol, val, xval, s0, s1, s2);
   }
 }
 
@@ -815,14 +842,14 @@ k_mg0_to_bf16(int nV, const int *__restrict__ brp, const int *__restrict__ bcol,
 template <int G, class VT>
 __global__ void __launch_bounds__(256)
 k_mg0_resid(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, const VT *__restrict__ val,
-            const float *__restrict__ b, const float *__restrict__ x, float *__restrict__ out,
-            const unsigned char *__restrict__ pinned, const PcgState *__restrict__ st) {
+            const int *__restrict__ off, const float *__restrict__ b, const float *__restrict__ x,
+            float *__restrict__ out, const unsigned char *__restrict__ pinned, const PcgState *__restrict__ st) {
   pdl_wait();
   pdl_trigger();
   if (st && st->done) return;
   BT_ROW_LOOP_BEGIN(G)
   float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-  if (active) spmv_row_acc<G>(v, sl, brp, bcol, val, [&](int c) { return __ldcg(x + c); }, s0, s1, s2);
+  if (active) row0_acc<G>(v, sl, brp, bcol, val, off, [&](int c) { return __ldcg(x + c); }, s0, s1, s2);
   group_reduce<G>(s0, s1, s2);
   if (active && sl == 0) {
     if (b) {
@@ -844,9 +871,9 @@ k_mg0_resid(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, c
 template <int G, class VT>
 __global__ void __launch_bounds__(256)
 k_mg0_post_bj(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, const VT *__restrict__ val,
-              const float *__restrict__ minv, const float *__restrict__ b, const float *__restrict__ x,
-              float *__restrict__ z, const unsigned char *__restrict__ pinned, const float *__restrict__ coef,
-              double *__restrict__ part, PcgState *__restrict__ st) {
+              const int *__restrict__ off, const float *__restrict__ minv, const float *__restrict__ b,
+              const float *__restrict__ x, float *__restrict__ z, const unsigned char *__restrict__ pinned,
+              const float *__restrict__ coef, double *__restrict__ part, PcgState *__restrict__ st) {
   pdl_wait();
   pdl_trigger();
   if (st->done) return;
@@ -854,7 +881,7 @@ k_mg0_post_bj(int nV, const int *__restrict__ brp, const int *__restrict__ bcol,
   float acc = 0.f;
   BT_ROW_LOOP_BEGIN(G)
   float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-  if (active) spmv_row_acc<G>(v, sl, brp, bcol, val, [&](int cc) { return __ldcg(x + cc); }, s0, s1, s2);
+  if (active) row0_acc<G>(v, sl, brp, bcol, val, off, [&](int cc) { return __ldcg(x + cc); }, s0, s1, s2);
   group_reduce<G>(s0, s1, s2);
   if (active && sl == 0) {
     float bv[3], rv[3], zv[3];
@@ -1356,16 +1383,20 @@ int fac_upper(bartels_ctx ctx, bartels_mesh_plan plan, const MgSmoother &sm, con
 // out = b - A x on the finest level, with the V-cycle's BF16 copy of A when it has one
 int resid0(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const float *b, const float *x, float *out,
            const PcgState *st) {
-  const int G = plan_lanes_spmv(ctx, plan);
-  const int g = grid_rows(ctx, plan->nV, G);
   using B16 = __nv_bfloat16;
   const B16 *a16 = plan->mg ? plan->mg->a16 : nullptr;
-  if (a16)
-    BT_MG_G(G, BT_LAUNCH_PDL(ctx, (k_mg0_resid<GL, B16>), g, 256, 0, plan->nV, plan->brp, plan->bcol, a16, b, x, out,
-                             plan->pinned, st));
-  else
-    BT_MG_G(G, BT_LAUNCH_PDL(ctx, (k_mg0_resid<GL, float>), g, 256, 0, plan->nV, plan->brp, plan->bcol, values, b, x,
-                             out, plan->pinned, st));
+  if (a16) {
+    // padded BF16 rows: the factor passes' lane count (4 values per lane step)
+    const int G = plan_lanes_tri(ctx, plan);
+    const int g = grid_rows(ctx, plan->nV, G);
+    BT_MG_G(G, BT_LAUNCH_PDL(ctx, (k_mg0_resid<GL, B16>), g, 256, 0, plan->nV, plan->brp, plan->bcol, a16,
+                             (const int *)plan->mg->a16_off, b, x, out, plan->pinned, st));
+  } else {
+    const int G = plan_lanes_spmv(ctx, plan);
+    const int g = grid_rows(ctx, plan->nV, G);
+    BT_MG_G(G, BT_LAUNCH_PDL(ctx, (k_mg0_resid<GL, float>), g, 256, 0, plan->nV, plan->brp, plan->bcol, values,
+                             (const int *)nullptr, b, x, out, plan->pinned, st));
+  }
   return BARTELS_OK;
 }
 
@@ -1387,7 +1418,7 @@ int mg_setup_numeric(bartels_ctx ctx, bartels_mesh_plan plan, const float *value
     FactorPattern *fp = nullptr;
     BT_CHECK(plan_factor_pattern(plan, &fp));
     BT_LAUNCH(ctx, k_mg0_to_bf16, grid_rows(ctx, plan->nV, 32), 256, 0, plan->nV, plan->brp, plan->bcol, fp->rev,
-              values, mg->a16);
+              values, (const int *)mg->a16_off, mg->a16);
   }
   for (int l = 0; l + 1 < L; ++l) {
     MgLevel &f = mg->lv[l], &c = mg->lv[l + 1];
@@ -1479,15 +1510,19 @@ int mg_enqueue_apply(bartels_ctx ctx, bartels_mesh_plan plan, const float *value
     BT_CHECK(fac_lower(ctx, plan, sm, l0.r, y, st));
     BT_CHECK(fac_upper(ctx, plan, sm, y, l0.x, z, c0, r, part, st));
   } else {
-    const int G = plan_lanes_spmv(ctx, plan);
-    const int g = grid_rows(ctx, nV, G);
     using B16 = __nv_bfloat16;
-    if (mg->a16)
+    if (mg->a16) {
+      const int G = plan_lanes_tri(ctx, plan);
+      const int g = grid_rows(ctx, nV, G);
       BT_MG_G(G, BT_LAUNCH_PDL(ctx, (k_mg0_post_bj<GL, B16>), g, 256, 0, nV, plan->brp, plan->bcol,
-                               (const B16 *)mg->a16, sm.minv, r, l0.x, z, plan->pinned, c0, part, st));
-    else
-      BT_MG_G(G, BT_LAUNCH_PDL(ctx, (k_mg0_post_bj<GL, float>), g, 256, 0, nV, plan->brp, plan->bcol, values, sm.minv,
-                               r, l0.x, z, plan->pinned, c0, part, st));
+                               (const B16 *)mg->a16, (const int *)mg->a16_off, sm.minv, r, l0.x, z, plan->pinned, c0,
+                               part, st));
+    } else {
+      const int G = plan_lanes_spmv(ctx, plan);
+      const int g = grid_rows(ctx, nV, G);
+      BT_MG_G(G, BT_LAUNCH_PDL(ctx, (k_mg0_post_bj<GL, float>), g, 256, 0, nV, plan->brp, plan->bcol, values,
+                               (const int *)nullptr, sm.minv, r, l0.x, z, plan->pinned, c0, part, st));
+    }
   }
   return BARTELS_OK;
 }

@@ -53,9 +53,13 @@ struct MgHierarchy {
   PcgState *st_once = nullptr;  // state for a single application outside PCG
   double *segn = nullptr;       // per-segment norms of the finest level's last two power iterates
   int segn_n = 0;
-  // BF16 copy of the finest level's values (the plan's layout), made exactly
-  // symmetric, for the V-cycle's own SpMVs (nullptr: the FP32 values are used)
+  // BF16 copy of the finest level's values, made exactly symmetric, for the
+  // V-cycle's own SpMVs (nullptr: the FP32 values are used). Vertex v's three
+  // scalar rows start at a16_off[v] and are each padded with zeros to
+  // padded_row(nb) entries (a multiple of 4), so a lane reads 4 values with
+  // one 8-byte load.
   __nv_bfloat16 *a16 = nullptr;
+  int *a16_off = nullptr;
   std::vector<void *> allocs;
   ~MgHierarchy();
 };
