@@ -382,7 +382,19 @@ int mg_prepare(bartels_ctx ctx, bartels_mesh_plan plan) {
       BT_CHECK(upload(mg, &d.ci, h.ci));
       BT_CHECK(upload(mg, &d.dpos, dpos));
       BT_CHECK(dalloc_n(mg, &d.val, 36 * (size_t)d.nnzb));
+      BT_CHECK(dalloc_n(mg, &d.val16, 36 * (size_t)d.nnzb));
       BT_CHECK(dalloc_n(mg, &d.dinv, 36 * (size_t)d.n));
+      // position of block (J, I) for each block (I, J) (Galerkin patterns are symmetric)
+      std::vector<int> rev(d.nnzb, -1);
+      for (int v = 0; v < h.n; ++v)
+        for (int k = h.rp[v]; k < h.rp[v + 1]; ++k) {
+          const int w = h.ci[k];
+          const int *b = h.ci.data() + h.rp[w], *e = h.ci.data() + h.rp[w + 1];
+          const int *f = std::lower_bound(b, e, v);
+          if (f == e || *f != v) return fail(BARTELS_E_DEVICE, "multigrid: coarse pattern is not symmetric");
+          rev[k] = (int)(f - h.ci.data());
+        }
+      BT_CHECK(upload(mg, &d.rev, rev));
     } else {
       d.nnzb = plan->nnzb;
     }
@@ -427,6 +439,37 @@ int mg_prepare(bartels_ctx ctx, bartels_mesh_plan plan) {
 }
 
 // ===================================================== numeric set-up ======
+// Galerkin kernels: a group of kGalLanes consecutive lanes per coarse block;
+// lane l of the group takes the block's contributions l, l + kGalLanes, ...
+// in list order, and the group's partial sums are combined by a fixed
+// butterfly, so each coarse entry is summed in the same order on every run.
+// The heavy blocks (a diagonal block sums every pair of its aggregate's
+// members, ~400 contributions at n = 96) no longer hold up a whole warp.
+constexpr int kGalLanes = 8;
+#define GAL_GROUP_LOOP_BEGIN                                                                       \
+  const int gl = threadIdx.x % kGalLanes;                                                          \
+  const int64_t gid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGalLanes;                \
+  const int64_t ngroups = ((int64_t)gridDim.x * blockDim.x) / kGalLanes;                           \
+  for (int64_t b0 = gid - gid % (32 / kGalLanes); b0 < ncb; b0 += ngroups) {                        \
+    const int64_t b = b0 + gid % (32 / kGalLanes);                                                 \
+    const bool active = b < ncb;
+#define GAL_GROUP_LOOP_END }
+
+// butterfly sum over the group (every lane of the warp takes part), then the
+// group's lanes store the block's 9 float4s round-robin
+__device__ __forceinline__ void gal_group_store(float C[36], bool active, int gl, float *__restrict__ out) {
+#pragma unroll
+  for (int o = kGalLanes / 2; o > 0; o >>= 1)
+#pragma unroll
+    for (int i = 0; i < 36; ++i) C[i] += __shfl_xor_sync(0xffffffffu, C[i], o);
+  if (active) {
+    float4 *o4 = reinterpret_cast<float4 *>(out);
+#pragma unroll
+    for (int i = 0; i < 9; ++i)
+      if (i % kGalLanes == gl) o4[i] = make_float4(C[4 * i], C[4 * i + 1], C[4 * i + 2], C[4 * i + 3]);
+  }
+}
+
 // Galerkin product level 0 -> 1: C_IJ = sum over the block's contributions
 // (v, k) of Q_v^T A_vw Q_w, A_vw read from the plan's value layout (row 3v+a
 // of block row v holds its blocks' columns contiguously). One thread per
@@ -435,12 +478,12 @@ __global__ void __launch_bounds__(128)
 k_mg_gal0(int64_t ncb, const int *__restrict__ gptr, const int2 *__restrict__ gent, const int *__restrict__ brp,
           const int *__restrict__ bcol, const float *__restrict__ val, const float *__restrict__ Q,
           float *__restrict__ cval) {
-  for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < ncb; b += (int64_t)gridDim.x * blockDim.x) {
+  GAL_GROUP_LOOP_BEGIN
     float C[36];
 #pragma unroll
     for (int i = 0; i < 36; ++i) C[i] = 0.f;
-    const int e1 = gptr[b + 1];
-    for (int e = gptr[b]; e < e1; ++e) {
+    const int e1 = active ? gptr[b + 1] : 0;
+    for (int e = (active ? gptr[b] : 0) + gl; e < e1; e += kGalLanes) {
       const int2 g = __ldg(gent + e);
       const int v = g.x, k = g.y;
       const int rb = __ldg(brp + v), rs = 3 * (__ldg(brp + v + 1) - rb);
@@ -470,22 +513,20 @@ k_mg_gal0(int64_t ncb, const int *__restrict__ gptr, const int2 *__restrict__ ge
           for (int d = 0; d < 6; ++d) C[6 * c + d] += q[c] * T[6 * a + d];
       }
     }
-    float4 *o = reinterpret_cast<float4 *>(cval + 36 * b);
-#pragma unroll
-    for (int i = 0; i < 9; ++i) o[i] = make_float4(C[4 * i], C[4 * i + 1], C[4 * i + 2], C[4 * i + 3]);
-  }
+    gal_group_store(C, active, gl, cval + 36 * b);
+  GAL_GROUP_LOOP_END
 }
 
 // Galerkin product between coarse levels (6x6 blocks, 6x6 prolongator blocks).
 __global__ void __launch_bounds__(128)
 k_mg_galc(int64_t ncb, const int *__restrict__ gptr, const int2 *__restrict__ gent, const int *__restrict__ ci,
           const float *__restrict__ val, const float *__restrict__ Q, float *__restrict__ cval) {
-  for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < ncb; b += (int64_t)gridDim.x * blockDim.x) {
+  GAL_GROUP_LOOP_BEGIN
     float C[36];
 #pragma unroll
     for (int i = 0; i < 36; ++i) C[i] = 0.f;
-    const int e1 = gptr[b + 1];
-    for (int e = gptr[b]; e < e1; ++e) {
+    const int e1 = active ? gptr[b + 1] : 0;
+    for (int e = (active ? gptr[b] : 0) + gl; e < e1; e += kGalLanes) {
       const int2 g = __ldg(gent + e);
       const int v = g.x, k = g.y;
       const int w = __ldg(ci + k);
@@ -517,10 +558,8 @@ k_mg_galc(int64_t ncb, const int *__restrict__ gptr, const int2 *__restrict__ ge
           for (int d = 0; d < 6; ++d) C[6 * c + d] += q[c] * T[6 * a + d];
       }
     }
-    float4 *o = reinterpret_cast<float4 *>(cval + 36 * b);
-#pragma unroll
-    for (int i = 0; i < 9; ++i) o[i] = make_float4(C[4 * i], C[4 * i + 1], C[4 * i + 2], C[4 * i + 3]);
-  }
+    gal_group_store(C, active, gl, cval + 36 * b);
+  GAL_GROUP_LOOP_END
 }
 
 // Inverse of each node's 6x6 diagonal block (symmetrised, FP64 Gauss-Jordan,
@@ -986,23 +1025,44 @@ k_mg0_fac_upper(int nV, const int4 *__restrict__ meta, const int *__restrict__ b
   }
 }
 
+// BF16 copy of a coarse level, exactly symmetric: block k gets
+// (C_k + C_rev(k)^T) / 2, rounded once (C_k and C_rev(k) come from separate
+// Galerkin sums and may differ in their last bits).
+__global__ void __launch_bounds__(256)
+k_mgc_to_bf16(int64_t nnzb, const int *__restrict__ rev, const float *__restrict__ val,
+              __nv_bfloat16 *__restrict__ val16) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nnzb; k += (int64_t)gridDim.x * blockDim.x) {
+    const float *a = val + 36 * k, *t = val + 36ll * __ldg(rev + k);
+    __nv_bfloat16 *o = val16 + 36 * k;
+#pragma unroll
+    for (int r = 0; r < 6; ++r)
+#pragma unroll
+      for (int c = 0; c < 6; ++c)
+        o[6 * r + c] = __float2bfloat16_rn(0.5f * (__ldg(a + 6 * r + c) + __ldg(t + 6 * c + r)));
+  }
+}
+
 // ======================================================== coarse levels ===
 // Row I of a 6x6-block level: G lanes stride the row's blocks; s = A_I. x
 template <int G, class XV>
 __device__ __forceinline__ void crow_acc(int I, int sl, const int *__restrict__ rp, const int *__restrict__ ci,
-                                         const float *__restrict__ val, XV &&xv, float s[6]) {
+                                         const __nv_bfloat16 *__restrict__ val, XV &&xv, float s[6]) {
   const int k1 = __ldg(rp + I + 1);
   for (int k = __ldg(rp + I) + sl; k < k1; k += G) {
     const int J = __ldg(ci + k);
     float xj[6];
 #pragma unroll
     for (int c = 0; c < 6; ++c) xj[c] = xv(6 * J + c);
-    const float4 *a4 = reinterpret_cast<const float4 *>(val + 36ll * k);
+    // 36 BF16 values = 9 x 8 bytes
+    const uint2 *a2 = reinterpret_cast<const uint2 *>(val + 36ll * k);
     float a[36];
 #pragma unroll
     for (int q = 0; q < 9; ++q) {
-      const float4 t = __ldg(a4 + q);
-      a[4 * q] = t.x; a[4 * q + 1] = t.y; a[4 * q + 2] = t.z; a[4 * q + 3] = t.w;
+      const uint2 t = __ldg(a2 + q);
+      a[4 * q] = __uint_as_float(t.x << 16);
+      a[4 * q + 1] = __uint_as_float(t.x & 0xFFFF0000u);
+      a[4 * q + 2] = __uint_as_float(t.y << 16);
+      a[4 * q + 3] = __uint_as_float(t.y & 0xFFFF0000u);
     }
 #pragma unroll
     for (int r = 0; r < 6; ++r)
@@ -1056,7 +1116,7 @@ k_mgc_first(int n, const float *__restrict__ dinv, const float *__restrict__ b, 
 // Chebyshev step j >= 1: r -= A d_in; d_out = c1 d_in + c2 Dinv r; x += d_out
 template <int G>
 __global__ void __launch_bounds__(256)
-k_mgc_cheb(int n, const int *__restrict__ rp, const int *__restrict__ ci, const float *__restrict__ val,
+k_mgc_cheb(int n, const int *__restrict__ rp, const int *__restrict__ ci, const __nv_bfloat16 *__restrict__ val,
            const float *__restrict__ dinv, const float *__restrict__ d_in, float *__restrict__ d_out,
            float *__restrict__ r, float *__restrict__ x, const float *__restrict__ coef, int j,
            const PcgState *__restrict__ st) {
@@ -1089,7 +1149,7 @@ k_mgc_cheb(int n, const int *__restrict__ rp, const int *__restrict__ ci, const 
 // r = b - A x
 template <int G>
 __global__ void __launch_bounds__(256)
-k_mgc_resid(int n, const int *__restrict__ rp, const int *__restrict__ ci, const float *__restrict__ val,
+k_mgc_resid(int n, const int *__restrict__ rp, const int *__restrict__ ci, const __nv_bfloat16 *__restrict__ val,
             const float *__restrict__ b, const float *__restrict__ x, float *__restrict__ r,
             const PcgState *__restrict__ st) {
   pdl_wait();
@@ -1108,7 +1168,7 @@ k_mgc_resid(int n, const int *__restrict__ rp, const int *__restrict__ ci, const
 // first post-smoothing step: r = b - A x; d = c0 Dinv r; x_out = x + d
 template <int G>
 __global__ void __launch_bounds__(256)
-k_mgc_post_first(int n, const int *__restrict__ rp, const int *__restrict__ ci, const float *__restrict__ val,
+k_mgc_post_first(int n, const int *__restrict__ rp, const int *__restrict__ ci, const __nv_bfloat16 *__restrict__ val,
                  const float *__restrict__ dinv, const float *__restrict__ b, const float *__restrict__ x,
                  float *__restrict__ x_out, float *__restrict__ r, float *__restrict__ d,
                  const float *__restrict__ coef, const PcgState *__restrict__ st) {
@@ -1141,7 +1201,7 @@ k_mgc_post_first(int n, const int *__restrict__ rp, const int *__restrict__ ci, 
 // y = Dinv (A x) (power iteration on a coarse level)
 template <int G>
 __global__ void __launch_bounds__(256)
-k_mgc_MA(int n, const int *__restrict__ rp, const int *__restrict__ ci, const float *__restrict__ val,
+k_mgc_MA(int n, const int *__restrict__ rp, const int *__restrict__ ci, const __nv_bfloat16 *__restrict__ val,
          const float *__restrict__ dinv, const float *__restrict__ x, float *__restrict__ y) {
   BT_CROW_LOOP_BEGIN(G)
   float s[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -1286,7 +1346,7 @@ int cheb_from_zero(bartels_ctx ctx, const MgLevel &c, const float *coef, bool fi
     BT_LAUNCH_PDL(ctx, k_mgc_first, grid_n(ctx, c.n), 256, 0, c.n, c.dinv, c.b, c.x, c.r, c.d, coef, st);
   float *dc = c.d, *dn = c.d2;
   for (int j = 1; j < c.deg; ++j) {
-    BT_LAUNCH_PDL(ctx, k_mgc_cheb<kGc>, gr, 256, 0, c.n, c.rp, c.ci, c.val, c.dinv, dc, dn, c.r, c.x, coef, j, st);
+    BT_LAUNCH_PDL(ctx, k_mgc_cheb<kGc>, gr, 256, 0, c.n, c.rp, c.ci, c.val16, c.dinv, dc, dn, c.r, c.x, coef, j, st);
     std::swap(dc, dn);
   }
   return BARTELS_OK;
@@ -1332,16 +1392,16 @@ int enqueue_coarse(bartels_ctx ctx, MgHierarchy *mg, int l, bool first_done, con
   }
   const int gr = grid_rows(ctx, c.n, kGc);
   BT_CHECK(cheb_from_zero(ctx, c, coef, first_done, st));
-  BT_LAUNCH_PDL(ctx, k_mgc_resid<kGc>, gr, 256, 0, c.n, c.rp, c.ci, c.val, c.b, c.x, c.r, st);
+  BT_LAUNCH_PDL(ctx, k_mgc_resid<kGc>, gr, 256, 0, c.n, c.rp, c.ci, c.val16, c.b, c.x, c.r, st);
   bool next_first = false;
   BT_CHECK(restrict_into<6>(ctx, mg, c, c.r, l + 1, st, &next_first));
   BT_CHECK(enqueue_coarse(ctx, mg, l + 1, next_first, st));
   BT_LAUNCH_PDL(ctx, k_mg_prolong<6>, grid_n(ctx, c.n), 256, 0, c.n, c.agg, c.Q, level_result(mg, l + 1), c.x, st);
-  BT_LAUNCH_PDL(ctx, k_mgc_post_first<kGc>, gr, 256, 0, c.n, c.rp, c.ci, c.val, c.dinv, c.b, c.x, c.x2, c.r, c.d, coef,
+  BT_LAUNCH_PDL(ctx, k_mgc_post_first<kGc>, gr, 256, 0, c.n, c.rp, c.ci, c.val16, c.dinv, c.b, c.x, c.x2, c.r, c.d, coef,
             st);
   float *dc = c.d, *dn = c.d2;
   for (int j = 1; j < c.deg; ++j) {
-    BT_LAUNCH_PDL(ctx, k_mgc_cheb<kGc>, gr, 256, 0, c.n, c.rp, c.ci, c.val, c.dinv, dc, dn, c.r, c.x2, coef, j, st);
+    BT_LAUNCH_PDL(ctx, k_mgc_cheb<kGc>, gr, 256, 0, c.n, c.rp, c.ci, c.val16, c.dinv, dc, dn, c.r, c.x2, coef, j, st);
     std::swap(dc, dn);
   }
   return BARTELS_OK;
@@ -1422,12 +1482,14 @@ int mg_setup_numeric(bartels_ctx ctx, bartels_mesh_plan plan, const float *value
   }
   for (int l = 0; l + 1 < L; ++l) {
     MgLevel &f = mg->lv[l], &c = mg->lv[l + 1];
-    const int g = grid_n(ctx, c.nnzb, 128);
+    const int g = grid_n(ctx, c.nnzb * kGalLanes, 128);  // kGalLanes lanes per coarse block
     if (l == 0)
       BT_LAUNCH(ctx, k_mg_gal0, g, 128, 0, c.nnzb, f.gptr, f.gent, plan->brp, plan->bcol, values, f.Q, c.val);
     else
       BT_LAUNCH(ctx, k_mg_galc, g, 128, 0, c.nnzb, f.gptr, f.gent, f.ci, f.val, f.Q, c.val);
     BT_LAUNCH(ctx, k_mg_inv6, grid_n(ctx, c.n, 128), 128, 0, c.n, c.dpos, c.val, c.dinv);
+    BT_LAUNCH(ctx, k_mgc_to_bf16, grid_n(ctx, c.nnzb), 256, 0, c.nnzb, (const int *)c.rev, (const float *)c.val,
+              c.val16);
   }
   if (mg->dense) {
     const MgLevel &c = mg->lv[L - 1];
@@ -1463,7 +1525,7 @@ int mg_setup_numeric(bartels_ctx ctx, bartels_mesh_plan plan, const float *value
                     (const PcgState *)nullptr);
         }
       } else {
-        BT_LAUNCH(ctx, k_mgc_MA<kGc>, grid_rows(ctx, c.n, kGc), 256, 0, c.n, c.rp, c.ci, c.val, c.dinv, x, y);
+        BT_LAUNCH(ctx, k_mgc_MA<kGc>, grid_rows(ctx, c.n, kGc), 256, 0, c.n, c.rp, c.ci, c.val16, c.dinv, x, y);
       }
       if (it == kPowerIters - 2) BT_CHECK(sumsq_into(ctx, mg, n, y, mg->norms + 2 * l));
       if (it == kPowerIters - 1) BT_CHECK(sumsq_into(ctx, mg, n, y, mg->norms + 2 * l + 1));

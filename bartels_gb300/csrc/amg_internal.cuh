@@ -22,6 +22,11 @@ struct MgLevel {
   int64_t nnzb = 0;
   int *rp = nullptr, *ci = nullptr, *dpos = nullptr;  // coarse levels: block pattern, diagonal positions
   float *val = nullptr;                               // coarse levels: 36 floats per block
+  // coarse levels: BF16 copy (A + A^T) / 2 of val, exactly symmetric, read by
+  // the smoothing, residual and power-iteration kernels; rev = position of
+  // the transposed block
+  __nv_bfloat16 *val16 = nullptr;
+  int *rev = nullptr;
   float *dinv = nullptr;                              // coarse levels: 36 floats per node (inverse diagonal block)
   // transfer to the next coarser level (none on the coarsest)
   int nc = 0;                         // nodes of the next level
