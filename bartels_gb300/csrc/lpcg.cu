@@ -350,30 +350,29 @@ k_lp_msg(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, cons
     if (!(pinned && pinned[v])) {
       const float2 P = reinterpret_cast<const float2 *>(pq + 2ll * kH * v)[lane];
       const int rb = brp[v], re = brp[v + 1];
-      // two edges per step (their loads overlap); contributions added in edge order
-      for (int p = rb; p < re; p += 2) {
-        const bool has1 = p + 1 < re;
-        const int j0 = __ldg(bcol + p), j1 = has1 ? __ldg(bcol + p + 1) : v;
-        const bool ok0 = j0 != v && !(pinned && pinned[j0]);
-        const bool ok1 = has1 && j1 != v && !(pinned && pinned[j1]);
-        float r0 = 0.f, r1 = 0.f, s0 = 0.f, s1 = 0.f;
-        float2 Q0 = make_float2(0.f, 0.f), Q1 = make_float2(0.f, 0.f);
-        if (ok0) {
-          ew.apply(fe + (int64_t)kFe * p, r0, r1);
-          Q0 = reinterpret_cast<const float2 *>(pq + 2ll * kH * j0 + kH)[lane];
+      // four edges per step: every load of the step is issued before any is
+      // used (an edge past the row's end reads its own vertex's data and is
+      // masked, as are the self edge and pinned neighbours); contributions are
+      // added in edge order
+      for (int p = rb; p < re; p += 4) {
+        int j[4];
+        bool ok[4];
+        float2 Q[4];
+        float r[4][2];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) j[q] = p + q < re ? __ldg(bcol + p + q) : v;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          Q[q] = reinterpret_cast<const float2 *>(pq + 2ll * kH * j[q] + kH)[lane];
+          ew.apply(fe + (int64_t)kFe * (p + q < re ? p + q : p), r[q][0], r[q][1]);
+          ok[q] = p + q < re && j[q] != v && !(pinned && pinned[j[q]]);
         }
-        if (ok1) {
-          ew.apply(fe + (int64_t)kFe * (p + 1), s0, s1);
-          Q1 = reinterpret_cast<const float2 *>(pq + 2ll * kH * j1 + kH)[lane];
-        }
-        if (ok0) {
-          a0 += fmaxf(P.x + Q0.x + r0, 0.f);
-          a1 += fmaxf(P.y + Q0.y + r1, 0.f);
-        }
-        if (ok1) {
-          a0 += fmaxf(P.x + Q1.x + s0, 0.f);
-          a1 += fmaxf(P.y + Q1.y + s1, 0.f);
-        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (ok[q]) {
+            a0 += fmaxf(P.x + Q[q].x + r[q][0], 0.f);
+            a1 += fmaxf(P.y + Q[q].y + r[q][1], 0.f);
+          }
       }
       const float s = invdeg[v];
       a0 *= s;
