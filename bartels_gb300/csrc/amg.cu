@@ -361,13 +361,18 @@ int mg_prepare(bartels_ctx ctx, bartels_mesh_plan plan) {
   mg->coarse_blockdiag = dense ? 0 : coarse_blockdiag;
   const int deg0 = env_int("BARTELS_MG_DEG0", 1, 1, 1);
   const int degc = env_int("BARTELS_MG_DEGC", 3, 1, (kMgCoef - 1) / 2 + 1);
+  // Chebyshev degree on the coarse levels below level 1: their steps are
+  // cheap (small levels), and more of them cut the PCG iterations (n = 96:
+  // degrees 3 / 4 / 5 / 6 give 70 / 66 / 63 / 62 iterations per solve; 5 is
+  // the fastest solve)
+  const int degc2 = env_int("BARTELS_MG_DEGC2", 5, 1, (kMgCoef - 1) / 2 + 1);
   mg->lv.resize(H.size());
   for (size_t l = 0; l < H.size(); ++l) {
     HostLevel &h = H[l];
     MgLevel &d = mg->lv[l];
     d.n = h.n;
     d.bs = h.bs;
-    d.deg = l == 0 ? deg0 : (l + 1 == H.size() ? kCoarsestDeg : degc);
+    d.deg = l == 0 ? deg0 : (l + 1 == H.size() ? kCoarsestDeg : (l == 1 ? degc : degc2));
     d.nc = h.nc;
     if (l > 0) {
       d.nnzb = h.rp[h.n];
