@@ -360,11 +360,13 @@ int mg_prepare(bartels_ctx ctx, bartels_mesh_plan plan) {
   mg->dense = dense;
   mg->coarse_blockdiag = dense ? 0 : coarse_blockdiag;
   const int deg0 = env_int("BARTELS_MG_DEG0", 1, 1, 1);
-  const int degc = env_int("BARTELS_MG_DEGC", 3, 1, (kMgCoef - 1) / 2 + 1);
-  // Chebyshev degree on the coarse levels below level 1: their steps are
-  // cheap (small levels), and more of them cut the PCG iterations (n = 96:
-  // degrees 3 / 4 / 5 / 6 give 70 / 66 / 63 / 62 iterations per solve; 5 is
-  // the fastest solve)
+  // Chebyshev degrees: level 1 (the largest coarse level; its one step is
+  // fused into the restriction) and the levels below it, whose steps are
+  // cheap and cut the PCG iterations. n = 96, one multigrid solve: level 1 at
+  // 3 with 3 / 4 / 5 / 6 below gives 70 / 66 / 63 / 62 iterations and 50.4 /
+  // 49.5 / 49.1 / 50.1 ms; with 5 below, level 1 at 1 / 2 / 3 / 4 gives
+  // 47.1 / 48.2 / 48.8 / 50.2 ms.
+  const int degc = env_int("BARTELS_MG_DEGC", 1, 1, (kMgCoef - 1) / 2 + 1);
   const int degc2 = env_int("BARTELS_MG_DEGC2", 5, 1, (kMgCoef - 1) / 2 + 1);
   mg->lv.resize(H.size());
   for (size_t l = 0; l < H.size(); ++l) {
