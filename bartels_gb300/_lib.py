@@ -116,6 +116,7 @@ SIGNATURES = [
     ("bartels_segment_sumsq_d", C.c_int, [_P, C.c_int, _P, _P, _P]),
     ("bartels_plan_set_segments", C.c_int, [_P, C.c_int, _I, C.POINTER(C.c_int64)]),
     ("bartels_plan_autotune_hessian", C.c_int, [_P, _P, C.c_int, _P, C.c_int, _I, _I]),
+    ("bartels_plan_pcg_spmv_time_d", C.c_int, [_P, _P, _P, _P, _P, C.c_int, C.POINTER(C.c_double)]),
     ("bartels_plan_set_hessian_tuning", C.c_int, [_P, C.c_int, C.c_int]),
     ("bartels_plan_set_segment_active", C.c_int, [_P, _P]),
     ("bartels_plan_segment_pcg_iterations", C.c_int, [_P, _I]),

@@ -36,6 +36,8 @@ int noalloc_gradient(bartels_ctx ctx, bartels_mesh_plan plan, int model, const d
 int plan_pcg(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const double *b, double *x,
              const bartels_pcg_params &prm, bartels_pcg_report *rep);
 int plan_set_segments(bartels_mesh_plan plan, int nseg, const int *voff, const int64_t *toff);
+int plan_pcg_spmv_time(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const float *x, float *y,
+                       int reps, double *us);
 int plan_autotune_hessian(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q, int force,
                           int *chunk_out, int *block_out);
 int plan_set_hessian_tuning(bartels_mesh_plan plan, int chunk, int block);
@@ -807,6 +809,18 @@ int bartels_plan_autotune(bartels_ctx ctx, bartels_mesh_plan plan, const float *
     values_d = plan->w_values.as<float>();
   }
   return plan_autotune(ctx, plan, values_d, force, spmv_lanes, factor_lanes);
+}
+
+int bartels_plan_pcg_spmv_time_d(bartels_ctx ctx, bartels_mesh_plan plan, const float *values_d, const float *x_d,
+                                 float *y_d, int reps, double *us_per_launch) {
+  BT_CHECK(check_plan(ctx, plan));
+  if (!x_d || !y_d || !us_per_launch || reps < 1) return fail(BARTELS_E_INVALID_ARG, "bad arguments");
+  if (!values_d) {
+    if (plan->w_values.bytes < sizeof(float) * 9 * (size_t)plan->nnzb)
+      return fail(BARTELS_E_INVALID_ARG, "the plan has no assembled Hessian yet");
+    values_d = plan->w_values.as<float>();
+  }
+  return plan_pcg_spmv_time(ctx, plan, values_d, x_d, y_d, reps, us_per_launch);
 }
 
 int bartels_plan_autotune_hessian(bartels_ctx ctx, bartels_mesh_plan plan, int model, const double *q_d, int force,

@@ -135,7 +135,7 @@ struct bartels_ctx_s {
   int64_t launches = 0;
   // lanes per vertex row in the block-layout SpMV (4, 8 or 16; tuned per GPU,
   // overridable with BARTELS_SPMV_LANES)
-  int spmv_lanes = 16;
+  int spmv_lanes = 8;
   // lanes per vertex row in the triangular factor passes (4 or 8; BARTELS_TRI_LANES)
   int tri_lanes = 4;
   // autotuner results per size bucket (floor(log2 nV)): {SpMV lanes, factor-pass lanes}
@@ -178,6 +178,11 @@ struct bartels_mesh_plan_s {
   int nchunks = 0;
   // half-size chunks (<= 64 vertices, 32 KB), made when the tuning asks for them
   int *chunk_v64 = nullptr;
+  // padded copy of the FP32 values for the PCG loop's SpMV: vertex v's three
+  // scalar rows start at pad_off[v] (pad_total entries in all), each padded
+  // with zeros to a multiple of 4 entries; w_vpad holds the copy
+  int *pad_off = nullptr;
+  int64_t pad_total = 0;
   int nchunks64 = 0;
   // Hessian tuning: vertices per assembly CTA (128, or 64 with chunk_v64) and
   // threads per CTA of the PSD pre-pass kernels (64, 128 or 256)
@@ -204,7 +209,7 @@ struct bartels_mesh_plan_s {
   // packed-mesh segments (nullptr: one system)
   bartels::SegInfo *seg = nullptr;
   // solver workspace
-  bartels::DevBuf w_values, w_minv, w_vec, w_grad_e, w_energy, w_u, w_pcg, w_psd, w_spmv;
+  bartels::DevBuf w_values, w_minv, w_vec, w_grad_e, w_energy, w_u, w_pcg, w_psd, w_spmv, w_vpad;
 };
 
 namespace bartels {

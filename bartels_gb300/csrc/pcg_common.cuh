@@ -197,4 +197,30 @@ __device__ __forceinline__ void tri_row_acc4(int sl, const int *__restrict__ col
   }
 }
 
+// Row v of the padded FP32 copy of the values (three scalar rows of rs
+// entries, each padded with zeros to rsp, a multiple of 4): each lane takes 4
+// consecutive columns per step with one 16-byte load per scalar row.
+template <int G, class XV>
+__device__ __forceinline__ void row_acc4f(int sl, const int *__restrict__ cols, const float *__restrict__ r0, int rs,
+                                          int rsp, XV &&xval, float &s0, float &s1, float &s2) {
+  for (int e0 = 4 * sl; e0 < rs; e0 += 4 * G) {
+    const float4 w0 = __ldcs(reinterpret_cast<const float4 *>(r0 + e0));
+    const float4 w1 = __ldcs(reinterpret_cast<const float4 *>(r0 + rsp + e0));
+    const float4 w2 = __ldcs(reinterpret_cast<const float4 *>(r0 + 2 * rsp + e0));
+    const int j0 = e0 / 3, l0 = e0 - 3 * j0;
+    const int c0 = __ldg(cols + j0);
+    const int c1 = 3 * (j0 + 1) < rs ? __ldg(cols + j0 + 1) : 0;
+    float xv[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int l = l0 + q;
+      const int c = l >= 3 ? c1 : c0;
+      xv[q] = e0 + q < rs ? xval(3 * c + (l >= 3 ? l - 3 : l)) : 0.f;
+    }
+    s0 += w0.x * xv[0] + w0.y * xv[1] + w0.z * xv[2] + w0.w * xv[3];
+    s1 += w1.x * xv[0] + w1.y * xv[1] + w1.z * xv[2] + w1.w * xv[3];
+    s2 += w2.x * xv[0] + w2.y * xv[1] + w2.z * xv[2] + w2.w * xv[3];
+  }
+}
+
 }  // namespace bartels

@@ -355,6 +355,7 @@ void plan_free(bartels_mesh_plan plan) {
   delete plan->seg;
   plan->seg = nullptr;
   if (plan->chunk_v64) cudaFree(plan->chunk_v64);
+  if (plan->pad_off) cudaFree(plan->pad_off);
   plan->chunk_v64 = nullptr;
   void *ptrs[] = {plan->X,        plan->E,      plan->dphi64,  plan->vol,     plan->params,  plan->density,
                   plan->rec32,    plan->rec64,  plan->inc_ptr, plan->inc_tet, plan->inc_pos, plan->brp,
@@ -371,6 +372,7 @@ void plan_free(bartels_mesh_plan plan) {
   plan->w_pcg.release();
   plan->w_psd.release();
   plan->w_spmv.release();
+  plan->w_vpad.release();
 }
 
 }  // namespace bartels

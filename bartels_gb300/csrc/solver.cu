@@ -13,6 +13,7 @@
 #include <nvtx3/nvToolsExt.h>
 
 #include <chrono>
+#include <climits>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -229,12 +230,15 @@ k_pcg_dir(int n, const float *__restrict__ z, float *__restrict__ pa, float *__r
     p_new[i] = z[i] + beta * p_old[i];
 }
 
-// ap = A p (block layout), partials of p.Ap; alpha in the last block.
-template <int G>
+// ap = A p (block layout), partials of p.Ap; alpha in the last block. PAD:
+// val is the padded copy of the values (rows at off[v], 4 per 16-byte load),
+// otherwise the plan's own layout.
+template <int G, bool PAD>
 __global__ void __launch_bounds__(256)
 k_pcg_spmv_blk(int nV, const int *__restrict__ brp, const int *__restrict__ bcol, const float *__restrict__ val,
-               const float *__restrict__ pa, const float *__restrict__ pb, float *__restrict__ ap,
-               const unsigned char *__restrict__ pinned, double *__restrict__ part, PcgState *__restrict__ st) {
+               const int *__restrict__ off, const float *__restrict__ pa, const float *__restrict__ pb,
+               float *__restrict__ ap, const unsigned char *__restrict__ pinned, double *__restrict__ part,
+               PcgState *__restrict__ st) {
   pdl_wait();
   pdl_trigger();
   if (st->done) return;
@@ -242,7 +246,15 @@ k_pcg_spmv_blk(int nV, const int *__restrict__ brp, const int *__restrict__ bcol
   float acc = 0.f;
   BT_ROW_LOOP_BEGIN(G)
   float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-  if (active) spmv_row_acc<G>(v, sl, brp, bcol, val, [&](int c) { return __ldcg(p + c); }, s0, s1, s2);
+  if (active) {
+    if constexpr (PAD) {
+      const int rb = __ldg(brp + v), nb = __ldg(brp + v + 1) - rb;
+      row_acc4f<G>(sl, bcol + rb, val + __ldg(off + v), 3 * nb, padded_row(nb), [&](int c) { return __ldcg(p + c); },
+                   s0, s1, s2);
+    } else {
+      spmv_row_acc<G>(v, sl, brp, bcol, val, [&](int c) { return __ldcg(p + c); }, s0, s1, s2);
+    }
+  }
   group_reduce<G>(s0, s1, s2);
   if (active && sl == 0) {
     if (pinned && pinned[v]) s0 = s1 = s2 = 0.f;
@@ -261,6 +273,24 @@ k_pcg_spmv_blk(int nV, const int *__restrict__ brp, const int *__restrict__ bcol
       st->alpha = (float)(st->rz / pap);
       st->count = 0;
     }
+  }
+}
+
+// Copy of the values into the padded layout (warp per vertex row); the pads
+// are zeroed when the buffer is allocated and never written.
+__global__ void __launch_bounds__(256)
+k_pad_values(int nV, const int *__restrict__ brp, const int *__restrict__ off, const float *__restrict__ val,
+             float *__restrict__ vpad) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int v = warp; v < nV; v += nwarps) {
+    const int rb = brp[v], nb = brp[v + 1] - rb, rs = 3 * nb, rsp = padded_row(nb);
+    const float *src = val + 9ll * rb;
+    float *dst = vpad + off[v];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      for (int e = lane; e < rs; e += 32) dst[k * rsp + e] = __ldcs(src + k * rs + e);
   }
 }
 
@@ -708,6 +738,8 @@ struct PcgOperator {
   // block layout (plan)
   bartels_mesh_plan plan = nullptr;
   const float *values = nullptr;
+  const float *vpad = nullptr;    // padded copy of values for the loop's SpMV (nullptr: values' own layout)
+  const int *pad_off = nullptr;
   const unsigned char *pinned = nullptr;
   // generic CSR
   int n = 0;
@@ -782,12 +814,18 @@ static int pcg_enqueue_mg(bartels_ctx ctx, const PcgOperator &op, const PcgWork 
 }
 
 static int pcg_spmv_blk(bartels_ctx ctx, const PcgOperator &op, const PcgWork &w, int lanes, int gs) {
-#define BT_K0(G)                                                                                                 \
-  BT_LAUNCH_PDL(ctx, k_pcg_spmv_blk<G>, gs, 256, 0, op.plan->nV, op.plan->brp, op.plan->bcol, op.values, w.pa, w.pb, \
-            w.ap, op.pinned, w.part_a, w.st)
-  if (lanes == 4) BT_K0(4);
-  else if (lanes == 16) BT_K0(16);
-  else BT_K0(8);
+#define BT_K0(G, PAD, VAL, OFF)                                                                                 \
+  BT_LAUNCH_PDL(ctx, (k_pcg_spmv_blk<G, PAD>), gs, 256, 0, op.plan->nV, op.plan->brp, op.plan->bcol, VAL, OFF, \
+                w.pa, w.pb, w.ap, op.pinned, w.part_a, w.st)
+  if (op.vpad) {
+    if (lanes == 4) BT_K0(4, true, op.vpad, op.pad_off);
+    else if (lanes == 16) BT_K0(16, true, op.vpad, op.pad_off);
+    else BT_K0(8, true, op.vpad, op.pad_off);
+  } else {
+    if (lanes == 4) BT_K0(4, false, op.values, (const int *)nullptr);
+    else if (lanes == 16) BT_K0(16, false, op.values, (const int *)nullptr);
+    else BT_K0(8, false, op.values, (const int *)nullptr);
+  }
 #undef BT_K0
   return BARTELS_OK;
 }
@@ -814,13 +852,7 @@ static int pcg_enqueue_iters(bartels_ctx ctx, const PcgOperator &op, const PcgWo
     // with the factor preconditioner the direction is formed by k_pcg_prec_upper
     if (!fac) BT_LAUNCH_PDL(ctx, k_pcg_dir, gd, 256, 0, n, w.z, w.pa, w.pb, w.st);
     if (blk) {
-#define BT_K1(G)                                                                                                 \
-  BT_LAUNCH_PDL(ctx, k_pcg_spmv_blk<G>, gs, 256, 0, op.plan->nV, op.plan->brp, op.plan->bcol, op.values, w.pa, w.pb, \
-            w.ap, op.pinned, w.part_a, w.st)
-      if (lanes == 4) BT_K1(4);
-      else if (lanes == 16) BT_K1(16);
-      else BT_K1(8);
-#undef BT_K1
+      BT_CHECK(pcg_spmv_blk(ctx, op, w, lanes, gs));
     } else {
       BT_LAUNCH_PDL(ctx, k_pcg_spmv_csr, gs, 256, 0, n, op.rp, op.ci, op.values, w.pa, w.pb, w.ap, w.part_a, w.st);
     }
@@ -1523,6 +1555,48 @@ int plan_set_segments(bartels_mesh_plan plan, int nseg, const int *voff, const i
   return BARTELS_OK;
 }
 
+// The PCG loop's SpMV reads a padded copy of the values (three scalar rows
+// per vertex, each padded with zeros to a multiple of 4 entries, so that a
+// lane reads 4 values with one 16-byte load); the copy is made once per
+// linear solve. BARTELS_PCG_PADDED=0 keeps the values' own layout.
+static bool padded_spmv_enabled() {
+  static const bool on = [] {
+    const char *e = std::getenv("BARTELS_PCG_PADDED");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
+static int plan_pad_offsets(bartels_mesh_plan plan) {
+  if (plan->pad_off) return BARTELS_OK;
+  std::vector<int> off(plan->nV + 1, 0);
+  for (int v = 0; v < plan->nV; ++v) {
+    const int64_t next = off[v] + 3ll * padded_row(plan->h_brp[v + 1] - plan->h_brp[v]);
+    if (next > INT_MAX) return fail(BARTELS_E_UNSUPPORTED, "padded values larger than 2^31 entries");
+    off[v + 1] = (int)next;
+  }
+  BT_CUDA(cudaMalloc(&plan->pad_off, sizeof(int) * off.size()));
+  BT_CUDA(cudaMemcpy(plan->pad_off, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice));
+  plan->pad_total = off[plan->nV];
+  return BARTELS_OK;
+}
+
+// *out = the padded copy of values (nullptr when the padded SpMV is off)
+int plan_padded_values(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const float **out) {
+  *out = nullptr;
+  if (!padded_spmv_enabled() || !values) return BARTELS_OK;
+  BT_CHECK(plan_pad_offsets(plan));
+  const size_t bytes = sizeof(float) * ((size_t)plan->pad_total + 4);
+  if (plan->w_vpad.bytes < bytes) {
+    BT_CHECK(plan->w_vpad.ensure(bytes));
+    BT_CUDA(cudaMemsetAsync(plan->w_vpad.p, 0, plan->w_vpad.bytes, ctx->stream));
+  }
+  BT_LAUNCH(ctx, k_pad_values, grid_spmv(ctx, plan->nV), 256, 0, plan->nV, plan->brp, (const int *)plan->pad_off,
+            values, plan->w_vpad.as<float>());
+  *out = plan->w_vpad.as<float>();
+  return BARTELS_OK;
+}
+
 // The plan's solve: per-segment scalars for packed meshes (block-Jacobi or a
 // multigrid V-cycle; the single-level factor preconditioner runs as block-
 // Jacobi there), one system otherwise.
@@ -1543,6 +1617,8 @@ static int plan_pcg_impl(bartels_ctx ctx, bartels_mesh_plan plan, const float *v
   op.plan = plan;
   op.values = values;
   op.pinned = plan->pinned;
+  BT_CHECK(plan_padded_values(ctx, plan, values, &op.vpad));
+  op.pad_off = plan->pad_off;
   if (fallback) *fallback = 0;
   const bool mg_learned = plan->precond == BARTELS_PRECOND_LEARNED_MULTIGRID && plan->lpcg_net;
   if (plan->precond == BARTELS_PRECOND_MULTIGRID || mg_learned) {
@@ -1888,13 +1964,67 @@ int plan_spmv(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, cons
   }
   double *part = plan->w_spmv.as<double>();
   PcgState *st = reinterpret_cast<PcgState *>(plan->w_spmv.as<char>() + o_st);
-#define BT_SPMV(G)                                                                                              \
-  BT_LAUNCH_PDL(ctx, k_pcg_spmv_blk<G>, g, 256, 0, plan->nV, plan->brp, plan->bcol, values, x, x, y, plan->pinned, \
-            part, st)
+#define BT_SPMV(G)                                                                                               \
+  BT_LAUNCH_PDL(ctx, (k_pcg_spmv_blk<G, false>), g, 256, 0, plan->nV, plan->brp, plan->bcol, values, (const int *)nullptr, \
+                x, x, y, plan->pinned, part, st)
   if (lanes == 4) BT_SPMV(4);
   else if (lanes == 16) BT_SPMV(16);
   else BT_SPMV(8);
 #undef BT_SPMV
+  return BARTELS_OK;
+}
+
+// The PCG loop's SpMV kernel on these values (over the padded copy when the
+// loop uses one, made once here), y = A x: 3 warm-up launches, then reps
+// launches timed with CUDA events on the context's stream; *us = microseconds
+// per launch.
+int plan_pcg_spmv_time(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const float *x, float *y,
+                       int reps, double *us) {
+  const int lanes = lanes_spmv(ctx, plan);
+  const int g = grid_spmv(ctx, (int64_t)plan->nV * lanes / 32 + 1);
+  const size_t o_st = (sizeof(double) * g + 255) & ~size_t(255);
+  const size_t need = o_st + sizeof(PcgState);
+  if (plan->w_spmv.bytes < need) {
+    BT_CHECK(plan->w_spmv.ensure(need));
+    BT_CUDA(cudaMemsetAsync(plan->w_spmv.p, 0, plan->w_spmv.bytes, ctx->stream));
+  }
+  double *part = plan->w_spmv.as<double>();
+  PcgState *st = reinterpret_cast<PcgState *>(plan->w_spmv.as<char>() + o_st);
+  const float *vpad = nullptr;
+  BT_CHECK(plan_padded_values(ctx, plan, values, &vpad));
+  const int *poff = plan->pad_off;
+  const int nV = plan->nV;
+  auto launch = [&]() {
+#define BT_TL(GG)                                                                                                  \
+  do {                                                                                                             \
+    if (vpad)                                                                                                      \
+      k_pcg_spmv_blk<GG, true><<<g, 256, 0, ctx->stream>>>(nV, plan->brp, plan->bcol, vpad, poff, x, x, y,         \
+                                                           plan->pinned, part, st);                                \
+    else                                                                                                           \
+      k_pcg_spmv_blk<GG, false><<<g, 256, 0, ctx->stream>>>(nV, plan->brp, plan->bcol, values, nullptr, x, x, y,   \
+                                                            plan->pinned, part, st);                               \
+  } while (0)
+    if (lanes == 4) BT_TL(4);
+    else if (lanes == 16) BT_TL(16);
+    else BT_TL(8);
+#undef BT_TL
+  };
+  cudaEvent_t e0, e1;
+  BT_CUDA(cudaEventCreate(&e0));
+  BT_CUDA(cudaEventCreate(&e1));
+  for (int k = 0; k < 3; ++k) launch();
+  cudaEventRecord(e0, ctx->stream);
+  for (int k = 0; k < reps; ++k) launch();
+  cudaEventRecord(e1, ctx->stream);
+  cudaError_t e = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (e != cudaSuccess) return fail(BARTELS_E_DEVICE, std::string("SpMV timing: ") + cudaGetErrorString(e));
+  ctx->launches += 3 + reps;
+  *us = 1e3 * ms / reps;
   return BARTELS_OK;
 }
 
@@ -2033,6 +2163,12 @@ int plan_autotune(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, 
     cudaMemsetAsync(gl, 0, 2 * (size_t)fp->lsize + 16, ctx->stream);
     cudaMemsetAsync(st, 0, sizeof(PcgState), ctx->stream);
     const int nV = plan->nV;
+    const float *vpad = nullptr;
+    if (plan_padded_values(ctx, plan, values, &vpad) != BARTELS_OK) {
+      cleanup();
+      return BARTELS_E_DEVICE;
+    }
+    const int *poff = plan->pad_off;
     // three rounds over the candidates, each candidate's best time kept (the
     // clocks may still be ramping up when a plan is set up)
     constexpr int kRounds = 3;
@@ -2045,15 +2181,19 @@ int plan_autotune(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, 
       const int g = grid_spmv(ctx, (int64_t)nV * G / 32 + 1);
       // the PCG loop's own SpMV (A p and the partials of p.Ap) on a scratch state
       const float ms = timed([&] {
-        if (G == 4)
-          k_pcg_spmv_blk<4><<<g, 256, 0, ctx->stream>>>(nV, plan->brp, plan->bcol, values, x, x, y, plan->pinned,
-                                                        part, st);
-        else if (G == 8)
-          k_pcg_spmv_blk<8><<<g, 256, 0, ctx->stream>>>(nV, plan->brp, plan->bcol, values, x, x, y, plan->pinned,
-                                                        part, st);
-        else
-          k_pcg_spmv_blk<16><<<g, 256, 0, ctx->stream>>>(nV, plan->brp, plan->bcol, values, x, x, y, plan->pinned,
-                                                         part, st);
+#define BT_TS(GG)                                                                                             \
+  do {                                                                                                        \
+    if (vpad)                                                                                                 \
+      k_pcg_spmv_blk<GG, true><<<g, 256, 0, ctx->stream>>>(nV, plan->brp, plan->bcol, vpad, poff, x, x, y,    \
+                                                           plan->pinned, part, st);                           \
+    else                                                                                                      \
+      k_pcg_spmv_blk<GG, false><<<g, 256, 0, ctx->stream>>>(nV, plan->brp, plan->bcol, values, nullptr, x, x, \
+                                                            y, plan->pinned, part, st);                       \
+  } while (0)
+        if (G == 4) BT_TS(4);
+        else if (G == 8) BT_TS(8);
+        else BT_TS(16);
+#undef BT_TS
       });
       t_s[ci] = std::min(t_s[ci], ms);
     }

@@ -457,6 +457,17 @@ int bartels_plan_pcg_d(bartels_ctx ctx, bartels_mesh_plan plan, const float *val
  * later plans of that bucket unless force != 0. No counterpart in the reference. */
 int bartels_plan_autotune(bartels_ctx ctx, bartels_mesh_plan plan, const float *values_d, int force,
                           int *spmv_lanes, int *factor_lanes);
+/* The PCG loop's SpMV kernel, y_d = A x_d with A the FP32 values_d (NULL:
+ * the plan's last assembled Hessian), timed: 3 warm-up launches, then reps
+ * launches between CUDA events on the context's stream; *us_per_launch gets
+ * the mean. The loop reads a copy of the values whose scalar rows are padded
+ * to multiples of 4 entries (4 values per 16-byte load); the copy is made
+ * here once, as the solver makes it once per linear solve (environment
+ * BARTELS_PCG_PADDED=0 keeps the values' own layout). For measurement; no
+ * counterpart in the reference. */
+int bartels_plan_pcg_spmv_time_d(bartels_ctx ctx, bartels_mesh_plan plan, const float *values_d, const float *x_d,
+                                 float *y_d, int reps, double *us_per_launch);
+
 /* Hessian autotuner: times the fused simple_psd_fix-projected assembly of the
  * plan at device positions q_d for the assembly's CTA shapes (128 vertices
  * per CTA with 64 KB of shared memory, or 64 vertices with 32 KB) and the PSD

@@ -3,8 +3,8 @@ the reference's golden files.
 
 Tolerances: FP64 paths (dphi_dX, volume, q, dq, mass, force) 1e-10 relative or
 bit-exact where the operation order is the reference's; FP32 Hessians
-1e-5 relative to the largest entry (the benchmark spec's bound for per-element
-results); CSR patterns bit-exact.
+1e-5 relative to the largest entry and to each row's own largest entry (per
+element: tests/test_gpu_elements.py); CSR patterns bit-exact.
 """
 import numpy as np
 import pytest
@@ -321,6 +321,16 @@ def test_device_hessian_and_spmv(oracle):
         ref = H @ x.cpu().double().numpy()
         got = y.cpu().double().numpy()
         assert np.linalg.norm(got - ref) <= 1e-5 * np.linalg.norm(ref), lanes
+        # the PCG loop's own SpMV over the padded copy of the values
+        y.zero_()
+        torch.cuda.synchronize()
+        us = C.c_double()
+        _lib.check(L.bartels_plan_pcg_spmv_time_d(ctx2.handle, plan2.handle, None, C.c_void_p(x.data_ptr()),
+                                                  C.c_void_p(y.data_ptr()), 2, C.byref(us)), "pcg_spmv_time")
+        ctx2.synchronize()
+        got = y.cpu().double().numpy()
+        assert np.linalg.norm(got - ref) <= 1e-5 * np.linalg.norm(ref), ("padded", lanes)
+        assert us.value > 0
         plan2.close()
         ctx2.close()
         ctx.close()
