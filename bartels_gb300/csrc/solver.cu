@@ -1635,9 +1635,23 @@ static int plan_pcg_impl(bartels_ctx ctx, bartels_mesh_plan plan, const float *v
       s = solve_any(ctx, op, n, b, x, plan->w_pcg, prm, rep);
       if (s == BARTELS_OK && rep->converged) return BARTELS_OK;
       if (s != BARTELS_OK && s != BARTELS_E_NOT_CONVERGED && s != BARTELS_E_NONFINITE) return s;
-      // not converged or not finite: solve again with block-Jacobi
       if (fallback) *fallback = 1;
-      const int used = rep->iterations;
+      int used = rep->iterations;
+      if (mg_learned) {
+        // the learned smoother failed this system: the same V-cycle with
+        // block-Jacobi smoothing first (a block-Jacobi solve costs ~25x the
+        // iterations on these systems)
+        MgSmoother bj;
+        BT_CHECK(mg_values(ctx, plan, values, false, bj));
+        op.sm = bj;
+        BT_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, ctx->stream));
+        s = solve_any(ctx, op, n, b, x, plan->w_pcg, prm, rep);
+        rep->iterations += used;
+        if (s == BARTELS_OK && rep->converged) return BARTELS_OK;
+        if (s != BARTELS_OK && s != BARTELS_E_NOT_CONVERGED && s != BARTELS_E_NONFINITE) return s;
+        used = rep->iterations;
+      }
+      // not converged or not finite: solve again with block-Jacobi
       op.mg = false;
       op.sm = MgSmoother();
       BT_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, ctx->stream));
