@@ -1632,7 +1632,13 @@ static int plan_pcg_impl(bartels_ctx ctx, bartels_mesh_plan plan, const float *v
       if (t_factor) *t_factor += now_s() - t0;
       op.mg = true;
       op.sm = sm;
-      s = solve_any(ctx, op, n, b, x, plan->w_pcg, prm, rep);
+      // a multigrid solve needs tens to a few hundred iterations on these
+      // systems; one that has not converged after kMgMaxIters has stagnated and
+      // moves on to the next preconditioner instead of running to the caller's cap
+      constexpr int kMgMaxIters = 1500;
+      bartels_pcg_params prm_mg = prm;
+      prm_mg.max_iters = std::min(prm.max_iters, kMgMaxIters);
+      s = solve_any(ctx, op, n, b, x, plan->w_pcg, prm_mg, rep);
       if (s == BARTELS_OK && rep->converged) return BARTELS_OK;
       if (s != BARTELS_OK && s != BARTELS_E_NOT_CONVERGED && s != BARTELS_E_NONFINITE) return s;
       if (fallback) *fallback = 1;
@@ -1645,7 +1651,7 @@ static int plan_pcg_impl(bartels_ctx ctx, bartels_mesh_plan plan, const float *v
         BT_CHECK(mg_values(ctx, plan, values, false, bj));
         op.sm = bj;
         BT_CUDA(cudaMemsetAsync(x, 0, sizeof(double) * n, ctx->stream));
-        s = solve_any(ctx, op, n, b, x, plan->w_pcg, prm, rep);
+        s = solve_any(ctx, op, n, b, x, plan->w_pcg, prm_mg, rep);
         rep->iterations += used;
         if (s == BARTELS_OK && rep->converged) return BARTELS_OK;
         if (s != BARTELS_OK && s != BARTELS_E_NOT_CONVERGED && s != BARTELS_E_NONFINITE) return s;
