@@ -378,10 +378,10 @@ def train_stream(net: LearnedPreconditioner, ctx: Context, systems: int, steps: 
     No more than the pool's Hessians (and the plans they belong to) are held."""
     rng = np.random.default_rng(seed)
     packs = max(1, -(-systems // (per_pack * newton_iters)))
-    per_arrival = steps / float(packs * newton_iters)
+    arrivals_total = packs * newton_iters
     hist, recent = [], []
     t0 = time.time()
-    produced, done_steps, owed, next_log = 0, 0, 0.0, 0
+    produced, done_steps, arrivals, next_log = 0, 0, 0, 0
     def drop_oldest():
         old = recent.pop(0)
         if all(r.plan is not old.plan for r in recent) and old.plan is not current[0]:
@@ -395,14 +395,16 @@ def train_stream(net: LearnedPreconditioner, ctx: Context, systems: int, steps: 
             if len(recent) > pool:
                 drop_oldest()
             produced += per_pack
-            owed += per_arrival
-            while owed >= 1.0 and done_steps < steps:
+            arrivals += 1
+            # steps owed after this arrival, in integers so that the last
+            # arrival reaches exactly `steps`
+            target = steps * arrivals // arrivals_total
+            while done_steps < target:
                 pick = recent[int(rng.integers(len(recent)))]
                 a = lr_end + 0.5 * (lr - lr_end) * (1 + math.cos(math.pi * done_steps / max(steps, 1)))
                 hist.append(net.train_step(pick.plan, pick.values, pick.residual, nprobes=nprobes,
                                            seed=int(rng.integers(1 << 31)), lr=a, clip=1.0))
                 done_steps += 1
-                owed -= 1.0
             if log and done_steps >= next_log:
                 next_log += max(steps // 20, 1)
                 log(f"systems {produced:6d}  step {done_steps:6d}  loss {np.mean(hist[-50:]) if hist else 0:.4f}  "
