@@ -1582,7 +1582,7 @@ static int plan_pad_offsets(bartels_mesh_plan plan) {
 }
 
 // *out = the padded copy of values (nullptr when the padded SpMV is off)
-int plan_padded_values(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const float **out) {
+static int plan_padded_values(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, const float **out) {
   *out = nullptr;
   if (!padded_spmv_enabled() || !values) return BARTELS_OK;
   BT_CHECK(plan_pad_offsets(plan));
@@ -2184,9 +2184,10 @@ int plan_autotune(bartels_ctx ctx, bartels_mesh_plan plan, const float *values, 
     cudaMemsetAsync(st, 0, sizeof(PcgState), ctx->stream);
     const int nV = plan->nV;
     const float *vpad = nullptr;
-    if (plan_padded_values(ctx, plan, values, &vpad) != BARTELS_OK) {
+    const int ps = plan_padded_values(ctx, plan, values, &vpad);
+    if (ps != BARTELS_OK) {
       cleanup();
-      return BARTELS_E_DEVICE;
+      return ps;  // with plan_padded_values' message
     }
     const int *poff = plan->pad_off;
     // three rounds over the candidates, each candidate's best time kept (the
