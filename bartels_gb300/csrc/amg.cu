@@ -33,10 +33,13 @@
 //
 // V-cycle (the PCG preconditioner, symmetric): on level 0 one Chebyshev step
 // of the smoother before and after the coarse correction; on coarse levels
-// `deg` steps (3 by default). The smoother of level 0 is block-Jacobi or the
-// learned factor M = G^T G (the network's output on the Hessian's lower
-// block pattern). Every kernel becomes a no-op once the PCG's convergence flag
-// is set, so fixed-length CUDA graphs of PCG iterations can contain it.
+// `deg` steps (1 on level 1, 5 below by default). The smoother of level 0 is
+// block-Jacobi or the learned factor M = G^T G (the network's output on the
+// Hessian's lower block pattern). The smoothing passes read exactly
+// symmetric BF16 copies of the operators (the fine one in padded rows); the
+// Galerkin products use the FP32 values. Every kernel becomes a no-op once
+// the PCG's convergence flag is set, so fixed-length CUDA graphs of PCG
+// iterations can contain it.
 #include <algorithm>
 #include <climits>
 #include <type_traits>
