@@ -23,6 +23,39 @@ def declared_functions():
     return sorted(set(re.findall(r"\b(bartels_[A-Za-z0-9_]+)\s*\(", text)) - {"bartels_objective_fn"})
 
 
+def declared_arity():
+    """Parameter count of every bartels_* function declared in include/*.h."""
+    inc = os.path.join(ROOT, "include")
+    text = "".join(open(os.path.join(inc, h)).read() for h in sorted(os.listdir(inc)) if h.endswith(".h"))
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    out = {}
+    for m in re.finditer(r"\b(bartels_[A-Za-z0-9_]+)\s*\(", text):
+        name, i, depth = m.group(1), m.end(), 1
+        j = i
+        while depth and j < len(text):
+            depth += {"(": 1, ")": -1}.get(text[j], 0)
+            j += 1
+        params = text[i:j - 1].strip()
+        if not params or params == "void":
+            n = 0
+        else:
+            n, d = 1, 0
+            for ch in params:
+                d += {"(": 1, ")": -1}.get(ch, 0)
+                n += ch == "," and d == 0
+        if text[j:j + 1].strip() in (";", "") or text[j:].lstrip().startswith(";"):
+            out.setdefault(name, n)
+    return out
+
+
+def test_bindings_match_header_arity():
+    """Every ctypes binding passes as many arguments as the header declares."""
+    ar = declared_arity()
+    wrong = [(name, len(args), ar[name]) for name, _, args in _lib.SIGNATURES if name in ar and len(args) != ar[name]]
+    assert not wrong, wrong
+
+
 def test_library_loads_and_exports_header():
     L = bg.lib()
     names = declared_functions()
