@@ -1501,7 +1501,6 @@ SegInfo::~SegInfo() {
 // every tet inside its segment), per-vertex and per-tet segment maps and the
 // per-segment scalar buffers.
 int plan_set_segments(bartels_mesh_plan plan, int nseg, const int *voff, const int64_t *toff) {
-  bartels_ctx ctx = plan->ctx;
   delete plan->seg;
   plan->seg = nullptr;
   if (nseg == 0) return BARTELS_OK;
@@ -1551,7 +1550,6 @@ int plan_set_segments(bartels_mesh_plan plan, int nseg, const int *voff, const i
   BT_CUDA(cudaMemcpy(sg->toff, toff, sizeof(int64_t) * (nseg + 1), cudaMemcpyHostToDevice));
   BT_CUDA(cudaMemcpy(sg->vseg, vseg.data(), sizeof(int) * plan->nV, cudaMemcpyHostToDevice));
   BT_CUDA(cudaMemcpy(sg->tseg, tseg.data(), sizeof(int) * plan->nT, cudaMemcpyHostToDevice));
-  (void)ctx;
   return BARTELS_OK;
 }
 
